@@ -1,0 +1,75 @@
+"""The oracle restatement against golden vectors produced by the reference's own code
+(tests/golden/make_golden.py).  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+FIELDS = O.FIELD_NAMES
+
+
+def _load(golden_dir, name):
+    return dict(np.load(os.path.join(golden_dir, name)))
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_expi_known_answers(oracle, golden_dir):
+    g = _load(golden_dir, "expi.npz")
+    for c, al, ref in zip(g["c"], g["alpha"], g["expi"]):
+        got = oracle.expi(float(c), al)
+        assert np.max(np.abs(got - ref)) < 5e-15, (c, al)
+        # unitary and special
+        assert np.max(np.abs(got @ got.conj().T - np.eye(3))) < 1e-14
+        assert abs(np.linalg.det(got) - 1.0) < 1e-14
+
+
+@pytest.mark.parametrize("tag,nsteps", [("s1", 1), ("s10", 10)])
+def test_leapfrog_matches_reference(oracle, golden_dir, tag, nsteps):
+    g = _load(golden_dir, "leapfrog_random.npz")
+    N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
+    f = {k: g["init_" + k].copy() for k in FIELDS}
+    oracle.update(f, N, a, dt, nsteps)
+    for k in FIELDS:
+        assert _rel(f[k], g[tag + "_" + k]) < 1e-12, k
+    ref_f = {k: g[tag + "_" + k].copy() for k in FIELDS}
+    assert np.allclose(oracle.bulk(ref_f, N, a), g[tag + "_bulk"], rtol=1e-12, atol=1e-12)
+    mx, avg = oracle.gauss(ref_f, N, a)
+    assert np.allclose([mx, avg], g[tag + "_gauss"], rtol=1e-12)
+    # the reference writes these two to text files with 15 significant digits
+    _, _, prof = oracle.gauss(ref_f, N, a, sync_first=True, profile=True)
+    assert np.allclose(prof, g[tag + "_gauss_profile"], rtol=1e-13, atol=1e-14)
+    emt = oracle.emt_map(ref_f, N, a)
+    assert np.allclose(emt, g[tag + "_emt"], rtol=1e-12, atol=1e-13)
+    umax, uavg = oracle.unitarity(ref_f, N)
+    assert umax < 1e-12 and g[tag + "_unitarity"][0] < 1e-12
+
+
+def test_coulomb_iterations_match_reference(oracle, golden_dir):
+    g = _load(golden_dir, "coulomb_mild.npz")
+    N, a = tuple(g["cfg_N"]), tuple(g["cfg_a"])
+    f = {"U": g["U"].copy(), "E": g["E"].copy()}
+    G = O.identity_gauge(N)
+    st, log, UG, EG = oracle.coulomb_fix(f, G, N, a, float(g["cfg_alpha"]), int(g["cfg_iters"]))
+    assert st == 0
+    # the reference's log file holds 6 significant digits
+    assert np.allclose(log, g["log"], rtol=2e-5, atol=1e-6)
+    assert np.max(np.abs(G - g["G"])) < 1e-12
+    assert np.max(np.abs(UG - g["UG"])) < 1e-12
+    assert np.max(np.abs(EG - g["EG"])) < 1e-12
+
+
+def test_mv_collision_evolution_matches_reference(oracle, golden_dir):
+    g = _load(golden_dir, "mv_collision.npz")
+    N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
+    f = {k: g["init_" + k].copy() for k in FIELDS}
+    assert np.allclose(oracle.bulk(f, N, a), g["t0_bulk"], rtol=1e-12, atol=1e-14)
+    oracle.update(f, N, a, dt, int(g["cfg_steps"]))
+    # B^2 sums 4*(3 - Re tr P) over sites with P ~ 1: absolute rounding ~ V * 12 * eps
+    assert np.allclose(oracle.bulk(f, N, a), g["t8_bulk"], rtol=1e-11, atol=1e-11)
+    assert np.allclose(oracle.gauss(f, N, a), g["t8_gauss"], rtol=1e-10, atol=1e-15)
+    assert np.allclose(oracle.emt_map(f, N, a), g["t8_emt"], rtol=1e-10, atol=1e-14)
