@@ -1,0 +1,428 @@
+"""Benchmark of the GB300 glasma leapfrog (one JSON line on rank 0).
+
+Workload: the production-size plain method, a 128x128x512 lattice (open z, a=1,
+dt=0.125a) advanced by the real-time SU(3) leapfrog Dynamics::SUNc::Update.  One
+"step" is one full leapfrog step of the whole lattice; the metric is
+site-updates/s (lattice sites x steps / second).
+
+  value     FP64, fields resident in HBM, CUDA events around K steps
+  e2e       FP64 through the C ABI with host buffers: every step uploads the six
+            dynamical fields from pinned host memory in the reference's host layout,
+            steps, and reads the bulk energy back
+  fp32      the same lattice in FP32 storage/arithmetic with FP64 reductions and
+            reunitarisation every 16 steps, with its energy error against FP64
+  roofline  for the dominant kernel (electric-field update), per-launch CUDA events
+  cpu_baseline  the oracle's CPU restatement on the host cores on a bounded slab
+
+`--impl reference` times the reference algorithm on the host CPU (the oracle port,
+all host threads) on a slab of the same workload and prints the same metric.
+
+Inputs are seeded synthetic fields with the workload's shapes: links
+exp(i 0.3 t^a r^a), E ~ N(0, 0.1^2), currents ~ N(0, 0.02^2), r ~ N(0,1).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_WORK = (128, 128, 512)
+A_WORK = (1.0, 1.0, 1.0)
+DT = 0.125
+SEED = 1002
+LINK_AMP, E_AMP, J_AMP = 0.3, 0.1, 0.02
+INPUT_FIELDS = ("U", "E", "Jp", "Jm", "JpStat", "JmStat")
+# compulsory HBM bytes per site of each kernel (read + write of what it must touch once)
+KERNEL_BYTES = {
+    "efield_jstat": {"fp64": 432 + 2 * 192 + 128 + 2 * 128, "fp32": 216 + 2 * 96 + 64 + 2 * 64},
+    "links_j": {"fp64": 192 + 2 * 432 + 128 + 2 * 128, "fp32": 96 + 2 * 216 + 64 + 2 * 64},
+}
+STEP_BYTES = {"fp64": 1760, "fp32": 880}  # every per-site state array read and written once
+FALLBACK_HBM_GBS = 6800.0
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        for k in ("hbm_gbs", "hbm_GBs", "hbm"):
+            if k in d:
+                v = d[k]
+                if isinstance(v, dict):
+                    v = v.get("value", v.get("burst"))
+                return float(v), "measured"
+    except Exception:
+        pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in getattr(self, "lines", []):
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- inputs
+def device_inputs(torch, N, seed, dev):
+    """Seeded synthetic fields in the reference's host layout (FP64), generated on the device."""
+    Nx, Ny, Nz = N
+    S = Nx * Ny * (Nz + 2)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    inv3 = 1.0 / 3.0 ** 0.5
+    U = torch.empty((S, 3, 3, 3), dtype=torch.complex128, device=dev)
+    Uf = U.view(S * 3, 3, 3)
+    chunk = 1 << 22
+    for c0 in range(0, S * 3, chunk):
+        c1 = min(S * 3, c0 + chunk)
+        al = LINK_AMP * torch.randn((c1 - c0, 8), generator=g, device=dev, dtype=torch.float64)
+        H = torch.zeros((c1 - c0, 3, 3), dtype=torch.complex128, device=dev)
+        H[:, 0, 0] = 0.5 * (al[:, 2] + al[:, 7] * inv3)
+        H[:, 1, 1] = -0.5 * (al[:, 2] - al[:, 7] * inv3)
+        H[:, 2, 2] = -al[:, 7] * inv3
+        H[:, 1, 0] = 0.5 * torch.complex(al[:, 0], al[:, 1])
+        H[:, 2, 0] = 0.5 * torch.complex(al[:, 3], al[:, 4])
+        H[:, 2, 1] = 0.5 * torch.complex(al[:, 5], al[:, 6])
+        H[:, 0, 1] = H[:, 1, 0].conj()
+        H[:, 0, 2] = H[:, 2, 0].conj()
+        H[:, 1, 2] = H[:, 2, 1].conj()
+        M = torch.linalg.matrix_exp(1j * H)  # [i, j]
+        Uf[c0:c1] = M.transpose(-1, -2)      # host layout stores element (i,j) at i + 3j
+        del al, H, M
+    f = {"U": U.view(Nz + 2, Ny, Nx, 3, 3, 3)}
+    f["E"] = E_AMP * torch.randn((Nz + 2, Ny, Nx, 3, 8), generator=g, device=dev, dtype=torch.float64)
+    for k in ("Jp", "Jm", "JpStat", "JmStat"):
+        f[k] = J_AMP * torch.randn((Nz + 2, Ny, Nx, 8), generator=g, device=dev, dtype=torch.float64)
+    for v in f.values():  # open-z ghost slices in sync
+        v[0] = v[1]
+        v[-1] = v[-2]
+    return f
+
+
+def host_slab(fields_dev, nz_slab):
+    """First nz_slab z-slices (plus ghosts) of the device inputs, as numpy arrays."""
+    out = {}
+    for k, v in fields_dev.items():
+        a = v[: nz_slab + 2].cpu().numpy().copy()
+        a[-1] = a[-2]
+        out[k] = a
+    import numpy as np
+
+    out["UOld"] = out["U"].copy()
+    return {k: np.ascontiguousarray(v) for k, v in out.items()}
+
+
+def numpy_inputs(N, seed):
+    """Same distribution as device_inputs, generated on the host (reference arm)."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    f = O.random_fields(N, seed, link_amp=LINK_AMP, e_amp=E_AMP, j_amp=J_AMP)
+    return {k: np.ascontiguousarray(v) for k, v in f.items()}
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def time_oracle(fields, N, threads, min_seconds, max_steps):
+    from oracle import oracle as O
+
+    orc = O.Oracle(threads=threads)
+    orc.update(fields, N, A_WORK, DT, 1, save_uold=False)  # warm-up
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps:
+        orc.update(fields, N, A_WORK, DT, 1, save_uold=False)
+        n += 1
+        if time.perf_counter() - t0 > min_seconds:
+            break
+    dt = time.perf_counter() - t0
+    sites = N[0] * N[1] * N[2]
+    return sites * n / dt, n, dt, orc.threads()
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    slab = (N_WORK[0], N_WORK[1], 32)
+    fields = numpy_inputs(slab, SEED)
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+
+    orc = O.Oracle(threads=threads)
+    for _ in range(args.warmup):
+        orc.update(fields, slab, A_WORK, DT, 1, save_uold=True)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.update(fields, slab, A_WORK, DT, 1, save_uold=True)
+        times.append(time.perf_counter() - t0)
+    sites = slab[0] * slab[1] * slab[2]
+    ms = 1e3 * sum(times) / len(times)
+    value = sites / (ms * 1e-3)
+    line = {
+        "impl": "reference",
+        "metric": "leapfrog site-updates/s",
+        "value": value,
+        "unit": "site-updates/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded SU(3) links / E / currents with the workload's shapes)",
+        "config": {"workload": "glasma leapfrog 128x128x512 FP64 (plain method, production size)",
+                   "lattice": list(N_WORK), "dt": DT},
+        "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": orc.threads(), "kind": "port",
+                         "sample": "each step = one full leapfrog step of a 128x128x32 slab of the workload "
+                                   "(Dynamics::SUNc::Update incl. SaveOldLink), oracle restatement, %d threads"
+                                   % orc.threads()},
+        "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU leg
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from soerenpragya3dglasma_gb300 import Lattice, build
+
+    if rank == 0:
+        build.build()
+    if world > 1:
+        dist.barrier()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    stream = torch.cuda.current_stream(dev)
+    N = N_WORK
+    vol = N[0] * N[1] * N[2]
+    inputs = device_inputs(torch, N, SEED + rank, dev)
+    torch.cuda.synchronize()
+
+    def make_lattice(precision):
+        lat = Lattice(N, A_WORK, precision=precision, reunitarize_every=16 if precision == "fp32" else 0,
+                      stream=stream)
+        for k in INPUT_FIELDS:
+            lat.upload_device(k, inputs[k].data_ptr())
+        lat.upload_device("UOld", inputs["U"].data_ptr())
+        return lat
+
+    # ---- FP64, resident fields
+    lat = make_lattice("fp64")
+    lat.step(DT, args.warmup, save_uold=False)
+    torch.cuda.synchronize()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        kernel_ms = lat.step_profiled(DT, args.steps, save_uold=False)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = world * vol / (ms_step * 1e-3)
+    e64 = lat.bulk()
+
+    peak, peak_kind = hbm_peak()
+    k_ms = {"efield_jstat": kernel_ms[0] / args.steps, "links_j": kernel_ms[1] / args.steps}
+    dom = max(k_ms, key=k_ms.get)
+    traffic = ncu_traffic()
+
+    def roofline(name, prec, ms):
+        alg = KERNEL_BYTES[name][prec] * vol
+        ach = alg / (ms * 1e-3) / 1e9
+        tr = traffic.get("%s_%s" % (name, prec))
+        return {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr,
+                "algorithmic_bytes_per_launch": alg, "launch_ms": ms}
+
+    rl = roofline(dom, "fp64", k_ms[dom])
+
+    # ---- FP32 on the same inputs
+    lat32 = make_lattice("fp32")
+    lat32.step(DT, args.warmup, save_uold=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    kms32 = lat32.step_profiled(DT, args.steps, save_uold=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1) / args.steps
+    e32 = lat32.bulk()
+    k32 = {"efield_jstat": kms32[0] / args.steps, "links_j": kms32[1] / args.steps}
+    dom32 = max(k32, key=k32.get)
+    fp32 = {"value": world * vol / (ms32 * 1e-3), "ms_per_step": ms32,
+            "step_hbm_frac": STEP_BYTES["fp32"] * vol / (ms32 * 1e-3) / 1e9 / peak,
+            "energy_rel_err_vs_fp64": abs(e32[9] - e64[9]) / abs(e64[9]),
+            "steps_compared": args.warmup + args.steps,
+            "roofline": roofline(dom32, "fp32", k32[dom32])}
+    del lat32
+
+    # ---- e2e through the C ABI with pinned host buffers
+    host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in inputs.items()}
+    for k in host:
+        host[k].copy_(inputs[k])
+    e2e_steps = max(1, min(args.steps, 5))
+    h2d = sum(host[k].numel() * host[k].element_size() for k in INPUT_FIELDS)
+    lat.upload("U", host["U"])
+    torch.cuda.synchronize()
+    barrier()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(e2e_steps):
+        for k in INPUT_FIELDS:
+            lat.upload(k, host[k])
+        lat.step(DT, 1, save_uold=False)
+        lat.bulk()  # device -> host read of the step's energy (7 doubles), synchronises
+    a1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = a0.elapsed_time(a1) / e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # ---- CPU baseline (rank 0 at N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        nz_slab = 64
+        hs = host_slab(inputs, nz_slab)
+        rate, n, secs, threads = time_oracle(hs, (N[0], N[1], nz_slab), os.cpu_count(), 10.0, 50)
+        cpu = {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
+               "sample": "%d leapfrog steps of a 128x128x%d slab of the workload in %.1f s, oracle "
+                         "restatement, %d threads" % (n, nz_slab, secs, threads)}
+    del lat
+    if world > 1:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    line = {
+        "metric": "leapfrog site-updates/s",
+        "value": value,
+        "unit": "site-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded SU(3) links exp(i 0.3 t.r), E ~ N(0,0.01), J ~ N(0,4e-4); workload shapes)",
+        "config": {"workload": "glasma leapfrog 128x128x512 FP64 (plain method, production size)",
+                   "lattice": list(N), "dt": DT, "a": list(A_WORK), "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (%.1f GB of FP64 state)" % (STEP_BYTES["fp64"] / 2 * vol / 1e9)},
+        "step_hbm_frac": STEP_BYTES["fp64"] * vol / (ms_step * 1e-3) / 1e9 / peak,
+        "roofline": rl,
+        "kernel_ms": k_ms,
+        "fp32": fp32,
+        "e2e": {"value": world * vol / (e2e_ms * 1e-3), "unit": "site-updates/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 7 * 8, "steps": e2e_steps},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": 2 * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,155 @@
+/* glasma_gb300.h -- C ABI of the GB300 real-time SU(3) glasma library.
+ *
+ * One handle = one lattice resident in GPU memory.  Every entry point returns an
+ * int status (GLASMA_OK = 0) and never exits the process; glasma_last_error()
+ * gives a message for the last failure on the calling thread.
+ *
+ * The reference program has no library boundary: its hot path is a set of C++
+ * namespaces compiled as one translation unit and driven by Simulation::Evolve
+ * (S/Simulation.cpp:212-321; S/ = the reference's SourceCode directory).  Each
+ * entry point below names the reference function it stands in for.  The C++
+ * drop-in shim with the reference's own class and namespace names is
+ * glasma_gb300_reference_api.hpp.
+ *
+ * Host buffers passed to upload/download use the reference's host layout, FP64,
+ * ghost slices included (S = Nx*Ny*(Nz+2) sites, site s = x + Nx*(y + Ny*(z+1))):
+ *   GLASMA_FIELD_U, _UOLD, _UG   complex double [S][3][9], element (i,j) at i+3j
+ *                                 (S/LATTICE/GaugeLinks.cpp:38-41)
+ *   GLASMA_FIELD_E, _EG           double [S][3][8]  (S/LATTICE/ElectricFields.cpp:31-35)
+ *   GLASMA_FIELD_JP ... _JMSTAT   double [S][8]     (S/LATTICE/ChargeDensity.cpp:24-33)
+ *   GLASMA_FIELD_G                complex double [S][9] (S/LATTICE/GaugeTransformations.cpp:25-38)
+ * Calls on one handle are not re-entrant; each handle issues its work on one CUDA
+ * stream (its own, or the one given to glasma_set_stream).
+ */
+#ifndef GLASMA_GB300_H
+#define GLASMA_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct glasma_lattice glasma_lattice;
+
+enum glasma_status {
+  GLASMA_OK = 0,
+  GLASMA_ERR_INVALID_ARGUMENT = 1, /* null handle / pointer, unknown field or flag    */
+  GLASMA_ERR_BAD_SHAPE = 2,        /* lattice extent or spacing out of range          */
+  GLASMA_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed                        */
+  GLASMA_ERR_CUDA = 4,             /* a CUDA call or kernel launch failed             */
+  GLASMA_ERR_NUMERICAL = 5,        /* numerical guard fired (reference: exit(0))      */
+  GLASMA_ERR_TIMEOUT = 6,          /* a bounded device wait ran out                   */
+  GLASMA_ERR_UNSUPPORTED = 7       /* operation not available for this handle         */
+};
+
+enum glasma_precision { GLASMA_FP64 = 0, GLASMA_FP32 = 1 };
+
+enum glasma_field {
+  GLASMA_FIELD_U = 0,
+  GLASMA_FIELD_UOLD = 1,
+  GLASMA_FIELD_E = 2,
+  GLASMA_FIELD_JP = 3,
+  GLASMA_FIELD_JM = 4,
+  GLASMA_FIELD_JPSTAT = 5,
+  GLASMA_FIELD_JMSTAT = 6,
+  GLASMA_FIELD_G = 7,
+  GLASMA_FIELD_UG = 8,
+  GLASMA_FIELD_EG = 9
+};
+
+/* glasma_step flags */
+#define GLASMA_STEP_SAVE_UOLD 0x1u /* write UOld = U(t+dt/2) of the last step (SaveOldLink) */
+
+/* glasma_coulomb_fix flags */
+#define GLASMA_GF_PROJECT_ZERO_MODE 0x1u /* drop the p=0 mode of the update (the reference keeps
+                                            it unnormalised); a documented deviation */
+
+/* Create a lattice (replaces Lattice::Init, S/LATTICE/SUNcVariables.cpp:71-90, and the
+ * container constructors, S/LATTICE/GaugeLinks.cpp:110-127): links set to the identity,
+ * E and the four currents to zero, ghost slices included.  precision: glasma_precision.
+ * reunitarize_every: FP32 only, project the links back onto SU(3) after every n-th step
+ * (0 = never).  Uses the current CUDA device. */
+int glasma_create(int nx, int ny, int nz, double ax, double ay, double az, int precision, int reunitarize_every,
+                  glasma_lattice** out);
+int glasma_destroy(glasma_lattice* h);
+
+/* Work is issued on `cuda_stream` (a cudaStream_t; NULL = the handle's own stream). */
+int glasma_set_stream(glasma_lattice* h, void* cuda_stream);
+/* The reference's Lattice::aScale (S/LATTICE/3DGrid.cpp:35-36), used by the observables. */
+int glasma_set_scale(glasma_lattice* h, double a_scale);
+int glasma_get_shape(const glasma_lattice* h, int* nx, int* ny, int* nz, int* precision);
+/* Number of doubles of one field in the host layout (with ghost slices). */
+long long glasma_field_doubles(const glasma_lattice* h, int field);
+
+/* Copy a whole field, ghost slices included, from / to host memory in the reference's host
+ * layout (replaces direct access to GaugeLinks::U, ElectricFields::E, ChargeDensity::J).
+ * Pinned host memory makes the copy asynchronous up to the stream synchronisation that
+ * download performs before it returns. */
+int glasma_upload(glasma_lattice* h, int field, const double* host);
+int glasma_download(glasma_lattice* h, int field, double* host);
+/* Same, from / to a device buffer holding the host layout. */
+int glasma_upload_device(glasma_lattice* h, int field, const double* device_aos);
+int glasma_download_device(glasma_lattice* h, int field, double* device_aos);
+
+/* nsteps x Dynamics::SUNc::Update (S/DYNAMICS/SUNcDynamics.cpp:353-378) with time step dt.
+ * The electric-field/JStat sub-steps and the link/J sub-steps are fused into two kernels
+ * per step.  SaveOldLink runs when GLASMA_STEP_SAVE_UOLD is set (for the last step of the
+ * call, which leaves UOld exactly as the reference leaves it). */
+int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags);
+
+/* glasma_step with CUDA events recorded on the handle's stream around each of the two
+ * kernels of every step; kernel_ms[0] / kernel_ms[1] receive the summed milliseconds of the
+ * electric-field/JStat kernel and of the link/J kernel.  Waits for the last event. */
+int glasma_step_profiled(glasma_lattice* h, double dt, int nsteps, unsigned flags, double* kernel_ms);
+
+/* The individual sub-steps, each with the reference's ghost synchronisation:
+ * UpdateElectricFields (:134-203), UpdateJStat (:205-236), UpdateGaugeLinks(dt_arg) (:62-106;
+ * U <- exp(i (-dt_arg a_mu^2/a^3) t.E_mu) U), SaveOldLink (:108-128), UpdateJ (:238-269). */
+int glasma_update_efield(glasma_lattice* h, double dt);
+int glasma_update_jstat(glasma_lattice* h, double dt);
+int glasma_update_links(glasma_lattice* h, double dt_arg);
+int glasma_save_old_link(glasma_lattice* h);
+int glasma_update_j(glasma_lattice* h, double dt);
+
+/* Observables::Bulk::Update and its accessors (S/OBSERVABLES/BulkObservables.cpp:22-183).
+ * out[0..2] ESqr, [3..5] BSqr, [6..8] EDotJ, [9..15] T00, TXX, TYY, TZZ, ELECTRIC, MAGNETIC, SOURCE
+ * (volume sums, as the reference returns them). */
+int glasma_bulk(glasma_lattice* h, double out[16]);
+/* Observables::GaussLaw::UpdateViolation (S/OBSERVABLES/GaussLawViolation.cpp:16-124).
+ * sync_first != 0 first syncs the ghosts of JpStat, JmStat, U and E (as the per-z form does).
+ * zprofile (may be NULL): Nz doubles, sum_{x,y,a} G^2 / (Nx Ny) per slice. */
+int glasma_gauss(glasma_lattice* h, int sync_first, double* max_violation, double* avg_violation, double* zprofile);
+/* Observables::Unitarity::UpdateViolation (S/OBSERVABLES/UnitarityViolation.cpp:13-51). */
+int glasma_unitarity(glasma_lattice* h, double* max_violation, double* avg_violation);
+/* Observables::EnergyMomentumTensor::CreateMap (S/OBSERVABLES/EnergyMomentumTensor.cpp:92-170):
+ * out[z*10 + k], k = T00, TXX, TYY, TZZ, T0X, T0Y, T0Z, TXY, TYZ, TZX (transverse averages). */
+int glasma_emt_map(glasma_lattice* h, double* out);
+
+/* Project every link onto SU(3) (Gram-Schmidt on two rows, third row from their cross product). */
+int glasma_reunitarize(glasma_lattice* h);
+
+/* CoulombGaugeFixing::SetCoulombGauge (S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:32-88) with
+ * the Fourier-accelerated update (S/GAUGETRANSFORMATION/ALGORITHMS/FourierAcceleration.cpp:15-142).
+ * alpha: the reference's alphaStepSize.  Iterates while n < max_iters and the latest maximum
+ * deviation > tol (the reference uses 1e-15).  The gauge transformation G persists in the handle
+ * across calls (identity at creation, reset with glasma_gauge_reset); the gauge-fixed links and
+ * fields are GLASMA_FIELD_UG / GLASMA_FIELD_EG.  log (may be NULL): max_iters x 7 doubles per
+ * iteration: n, max dev, avg dev, max step, avg step, min functional, sum functional / V.
+ * Returns GLASMA_ERR_NUMERICAL when an update leaves unitarity by more than 1e-13 (the reference
+ * exits there). */
+int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double tol, unsigned flags, double* log,
+                       int* iterations);
+/* GaugeTransformation::SetIdentity (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:41-60). */
+int glasma_gauge_reset(glasma_lattice* h);
+
+/* Wait for the handle's stream. */
+int glasma_synchronize(glasma_lattice* h);
+const char* glasma_status_string(int status);
+const char* glasma_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLASMA_GB300_H */

@@ -1,0 +1,86 @@
+"""ctypes binding of libglasma_gb300.so (the C ABI in include/glasma_gb300.h).
+
+The library is the only compute path: if it is missing or cannot be loaded,
+every entry point raises instead of falling back to anything else.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libglasma_gb300.so")
+
+GLASMA_OK = 0
+STATUS_NAMES = {
+    0: "GLASMA_OK", 1: "GLASMA_ERR_INVALID_ARGUMENT", 2: "GLASMA_ERR_BAD_SHAPE", 3: "GLASMA_ERR_OUT_OF_MEMORY",
+    4: "GLASMA_ERR_CUDA", 5: "GLASMA_ERR_NUMERICAL", 6: "GLASMA_ERR_TIMEOUT", 7: "GLASMA_ERR_UNSUPPORTED",
+}
+FP64, FP32 = 0, 1
+FIELDS = {"U": 0, "UOld": 1, "E": 2, "Jp": 3, "Jm": 4, "JpStat": 5, "JmStat": 6, "G": 7, "UG": 8, "EG": 9}
+STEP_SAVE_UOLD = 0x1
+GF_PROJECT_ZERO_MODE = 0x1
+
+# (name, restype, argtypes) for every symbol declared in include/glasma_gb300.h
+_H = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+SIGNATURES = [
+    ("glasma_create", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_int,
+                                                                                  ctypes.POINTER(ctypes.c_void_p)]),
+    ("glasma_destroy", ctypes.c_int, [_H]),
+    ("glasma_set_stream", ctypes.c_int, [_H, ctypes.c_void_p]),
+    ("glasma_set_scale", ctypes.c_int, [_H, ctypes.c_double]),
+    ("glasma_get_shape", ctypes.c_int, [_H, _I, _I, _I, _I]),
+    ("glasma_field_doubles", ctypes.c_longlong, [_H, ctypes.c_int]),
+    ("glasma_upload", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p]),
+    ("glasma_download", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p]),
+    ("glasma_upload_device", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p]),
+    ("glasma_download_device", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p]),
+    ("glasma_step", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_uint]),
+    ("glasma_step_profiled", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_uint, _D]),
+    ("glasma_update_efield", ctypes.c_int, [_H, ctypes.c_double]),
+    ("glasma_update_jstat", ctypes.c_int, [_H, ctypes.c_double]),
+    ("glasma_update_links", ctypes.c_int, [_H, ctypes.c_double]),
+    ("glasma_save_old_link", ctypes.c_int, [_H]),
+    ("glasma_update_j", ctypes.c_int, [_H, ctypes.c_double]),
+    ("glasma_bulk", ctypes.c_int, [_H, _D]),
+    ("glasma_gauss", ctypes.c_int, [_H, ctypes.c_int, _D, _D, _D]),
+    ("glasma_unitarity", ctypes.c_int, [_H, _D, _D]),
+    ("glasma_emt_map", ctypes.c_int, [_H, _D]),
+    ("glasma_reunitarize", ctypes.c_int, [_H]),
+    ("glasma_coulomb_fix", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
+    ("glasma_gauge_reset", ctypes.c_int, [_H]),
+    ("glasma_synchronize", ctypes.c_int, [_H]),
+    ("glasma_status_string", ctypes.c_char_p, [ctypes.c_int]),
+    ("glasma_last_error", ctypes.c_char_p, []),
+]
+
+_lib = None
+
+
+class GlasmaError(RuntimeError):
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+
+
+def load(path=LIB_PATH):
+    """Load (once) and return the CDLL with argtypes set.  Raises if the library is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libglasma_gb300.so is not built (%s); run soerenpragya3dglasma_gb300.build.build()" % path)
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status):
+    if status != GLASMA_OK:
+        msg = _lib.glasma_last_error().decode(errors="replace") if _lib is not None else ""
+        raise GlasmaError(status, msg)
+    return status

@@ -1,0 +1,32 @@
+// gaugefix.h -- internal interface of the Coulomb gauge fixer (gaugefix.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "lattice.cuh"
+
+namespace glasma {
+
+struct GaugeFixState;  // FFT plan, work arrays; owned by the lattice handle
+
+struct GaugeFixArgs {
+  Geometry g;
+  int precision;
+  double a_scale;
+  cudaStream_t stream;
+  void* U;
+  void* E;
+  void* G;
+  void* UG;
+  void* EG;
+  double* scratch;
+  size_t scratch_doubles;
+};
+
+int gaugefix_run(GaugeFixState** state, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
+                 double* log, int* iterations, std::string* err);
+void gaugefix_destroy(GaugeFixState* state);
+
+}  // namespace glasma

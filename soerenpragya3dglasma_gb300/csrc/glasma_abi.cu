@@ -1,0 +1,617 @@
+// glasma_abi.cu -- the C ABI (include/glasma_gb300.h): handle, device memory, host copies
+// and the orchestration of the kernels for each reference entry point.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/glasma_gb300.h"
+#include "gaugefix.h"
+#include "lattice.cuh"
+
+using glasma::cx;
+using glasma::FieldPtrs;
+using glasma::Geometry;
+
+struct glasma_lattice {
+  Geometry g;
+  int precision;
+  int reunit_every;
+  long long steps_done;
+  double a_scale;
+  int device;
+  cudaStream_t own_stream;
+  cudaStream_t stream;
+  size_t real_bytes;  // 8 or 4
+  void* f[10];        // device SoA fields, indexed by glasma_field (G, UG, EG allocated lazily)
+  double* staging;    // device AoS staging buffer for host copies
+  size_t staging_bytes;
+  double* scratch;    // reduction partials and results
+  size_t scratch_doubles;
+  glasma::GaugeFixState* gf;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(GLASMA_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define GLASMA_CUDA(call, where)                 \
+  do {                                            \
+    cudaError_t _e = (call);                      \
+    if (_e != cudaSuccess) return cuda_fail(_e, where); \
+  } while (0)
+
+#define GLASMA_CHECK_HANDLE(h)                                                  \
+  do {                                                                          \
+    if (!(h)) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null lattice handle");  \
+    cudaError_t _d = cudaSetDevice((h)->device);                                \
+    if (_d != cudaSuccess) return cuda_fail(_d, "cudaSetDevice");               \
+  } while (0)
+
+// Components per site on the device side, and doubles per site in the host layout.
+int field_components(int field) {  // number of SoA component arrays (complex ones count once)
+  switch (field) {
+    case GLASMA_FIELD_U:
+    case GLASMA_FIELD_UOLD:
+    case GLASMA_FIELD_UG: return 27;
+    case GLASMA_FIELD_G: return 9;
+    case GLASMA_FIELD_E:
+    case GLASMA_FIELD_EG: return 24;
+    default: return 8;
+  }
+}
+bool field_is_complex(int field) {
+  return field == GLASMA_FIELD_U || field == GLASMA_FIELD_UOLD || field == GLASMA_FIELD_UG || field == GLASMA_FIELD_G;
+}
+int host_doubles_per_site(int field) { return field_components(field) * (field_is_complex(field) ? 2 : 1); }
+
+size_t field_bytes(const glasma_lattice* h, int field) {
+  return (size_t)h->g.S * (size_t)host_doubles_per_site(field) * h->real_bytes;
+}
+
+template <typename T>
+FieldPtrs<T> ptrs(glasma_lattice* h) {
+  FieldPtrs<T> p;
+  p.U = static_cast<cx<T>*>(h->f[GLASMA_FIELD_U]);
+  p.UOld = static_cast<cx<T>*>(h->f[GLASMA_FIELD_UOLD]);
+  p.E = static_cast<T*>(h->f[GLASMA_FIELD_E]);
+  p.Jp = static_cast<T*>(h->f[GLASMA_FIELD_JP]);
+  p.Jm = static_cast<T*>(h->f[GLASMA_FIELD_JM]);
+  p.JpStat = static_cast<T*>(h->f[GLASMA_FIELD_JPSTAT]);
+  p.JmStat = static_cast<T*>(h->f[GLASMA_FIELD_JMSTAT]);
+  return p;
+}
+
+// identity links / zero fields, ghost slices included
+template <typename T>
+__global__ void init_identity_kernel(cx<T>* U, long long S, int nmat) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = S * 9 * nmat;
+  if (i >= n) return;
+  const long long comp = i / S;
+  const int k = (int)(comp % 9);
+  cx<T> v;
+  v.re = (k == 0 || k == 4 || k == 8) ? T(1) : T(0);
+  v.im = T(0);
+  U[i] = v;
+}
+
+int ensure_field(glasma_lattice* h, int field) {
+  if (h->f[field]) return GLASMA_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, field_bytes(h, field));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GLASMA_ERR_OUT_OF_MEMORY, std::string("cudaMalloc field: ") + cudaGetErrorString(e));
+  }
+  h->f[field] = p;
+  if (field_is_complex(field)) {
+    const int nmat = field_components(field) / 9;
+    const long long n = h->g.S * 9 * nmat;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (h->precision == GLASMA_FP64)
+      init_identity_kernel<double><<<grid, 256, 0, h->stream>>>(static_cast<cx<double>*>(p), h->g.S, nmat);
+    else
+      init_identity_kernel<float><<<grid, 256, 0, h->stream>>>(static_cast<cx<float>*>(p), h->g.S, nmat);
+    GLASMA_CUDA(cudaGetLastError(), "init identity");
+  } else {
+    GLASMA_CUDA(cudaMemsetAsync(p, 0, field_bytes(h, field), h->stream), "cudaMemsetAsync");
+  }
+  return GLASMA_OK;
+}
+
+int ensure_staging(glasma_lattice* h, size_t bytes) {
+  if (h->staging_bytes >= bytes) return GLASMA_OK;
+  if (h->staging) {
+    cudaStreamSynchronize(h->stream);
+    cudaFree(h->staging);
+    h->staging = nullptr;
+    h->staging_bytes = 0;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GLASMA_ERR_OUT_OF_MEMORY, std::string("cudaMalloc staging: ") + cudaGetErrorString(e));
+  }
+  h->staging = static_cast<double*>(p);
+  h->staging_bytes = bytes;
+  return GLASMA_OK;
+}
+
+int ensure_scratch(glasma_lattice* h) {
+  const size_t need = (size_t)glasma::observable_scratch_doubles(h->g) + (size_t)h->g.nz * 16 + 64;
+  if (h->scratch_doubles >= need) return GLASMA_OK;
+  if (h->scratch) {
+    cudaStreamSynchronize(h->stream);
+    cudaFree(h->scratch);
+    h->scratch = nullptr;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, need * sizeof(double));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GLASMA_ERR_OUT_OF_MEMORY, std::string("cudaMalloc scratch: ") + cudaGetErrorString(e));
+  }
+  h->scratch = static_cast<double*>(p);
+  h->scratch_doubles = need;
+  return GLASMA_OK;
+}
+
+bool valid_field(int field) { return field >= GLASMA_FIELD_U && field <= GLASMA_FIELD_EG; }
+
+int sync_field_ghosts(glasma_lattice* h, int field) {
+  cudaError_t e;
+  const int comps = field_components(field);
+  if (h->precision == GLASMA_FP64) {
+    if (field_is_complex(field))
+      e = glasma::launch_sync_ghosts<cx<double>>(h->g, static_cast<cx<double>*>(h->f[field]), comps, h->stream);
+    else
+      e = glasma::launch_sync_ghosts<double>(h->g, static_cast<double*>(h->f[field]), comps, h->stream);
+  } else {
+    if (field_is_complex(field))
+      e = glasma::launch_sync_ghosts<cx<float>>(h->g, static_cast<cx<float>*>(h->f[field]), comps, h->stream);
+    else
+      e = glasma::launch_sync_ghosts<float>(h->g, static_cast<float*>(h->f[field]), comps, h->stream);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "ghost sync");
+  return GLASMA_OK;
+}
+
+int copy_results_to_host(glasma_lattice* h, const double* dev, double* host, size_t n) {
+  GLASMA_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "result copy");
+  GLASMA_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  return GLASMA_OK;
+}
+
+// When `ev` is non-null it holds 3 events per step (before K1, between K1 and K2, after K2),
+// recorded on the handle's stream.
+template <typename T>
+int step_impl(glasma_lattice* h, double dt, int nsteps, unsigned flags, cudaEvent_t* ev = nullptr) {
+  FieldPtrs<T> p = ptrs<T>(h);
+  // UpdateElectricFields starts with U->SynchronizeGhostCells() (S/DYNAMICS/SUNcDynamics.cpp:151);
+  // the fused kernels keep every ghost slice in sync after that.
+  cudaError_t e = glasma::launch_sync_ghosts<cx<T>>(h->g, p.U, 27, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ghost sync U");
+  for (int n = 0; n < nsteps; n++) {
+    if (ev) cudaEventRecord(ev[3 * n], h->stream);
+    e = glasma::launch_efield_jstat<T>(h->g, p, dt, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "efield_jstat");
+    if (ev) cudaEventRecord(ev[3 * n + 1], h->stream);
+    const bool save = (flags & GLASMA_STEP_SAVE_UOLD) && (n == nsteps - 1);
+    e = glasma::launch_links_j<T>(h->g, p, dt, save, true, true, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "links_j");
+    if (ev) cudaEventRecord(ev[3 * n + 2], h->stream);
+    h->steps_done++;
+    if (h->reunit_every > 0 && h->steps_done % h->reunit_every == 0) {
+      e = glasma::launch_reunitarize<T>(h->g, p.U, h->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "reunitarize");
+    }
+  }
+  return GLASMA_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+const char* glasma_last_error(void) { return g_last_error.c_str(); }
+
+const char* glasma_status_string(int status) {
+  switch (status) {
+    case GLASMA_OK: return "ok";
+    case GLASMA_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GLASMA_ERR_BAD_SHAPE: return "bad lattice shape";
+    case GLASMA_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case GLASMA_ERR_CUDA: return "CUDA error";
+    case GLASMA_ERR_NUMERICAL: return "numerical guard fired";
+    case GLASMA_ERR_TIMEOUT: return "device wait timed out";
+    case GLASMA_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int glasma_create(int nx, int ny, int nz, double ax, double ay, double az, int precision, int reunitarize_every,
+                  glasma_lattice** out) {
+  if (!out) return fail(GLASMA_ERR_INVALID_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (nx < 2 || ny < 2 || nz < 2) return fail(GLASMA_ERR_BAD_SHAPE, "each extent must be >= 2");
+  if ((long long)nx * ny * (nz + 2) > (1LL << 40)) return fail(GLASMA_ERR_BAD_SHAPE, "lattice too large");
+  if (!(ax > 0) || !(ay > 0) || !(az > 0)) return fail(GLASMA_ERR_BAD_SHAPE, "spacings must be positive");
+  if (precision != GLASMA_FP64 && precision != GLASMA_FP32) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (reunitarize_every < 0) return fail(GLASMA_ERR_INVALID_ARGUMENT, "reunitarize_every < 0");
+  glasma_lattice* h = new glasma_lattice;
+  std::memset(h, 0, sizeof(*h));
+  h->g.nx = nx;
+  h->g.ny = ny;
+  h->g.nz = nz;
+  h->g.plane = (long long)nx * ny;
+  h->g.S = h->g.plane * (nz + 2);
+  h->g.vol = h->g.plane * nz;
+  h->g.a[0] = ax;
+  h->g.a[1] = ay;
+  h->g.a[2] = az;
+  h->precision = precision;
+  h->reunit_every = precision == GLASMA_FP32 ? reunitarize_every : 0;
+  h->a_scale = 1.0;
+  h->real_bytes = precision == GLASMA_FP64 ? 8 : 4;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(e, "create");
+  }
+  h->stream = h->own_stream;
+  for (int f = GLASMA_FIELD_U; f <= GLASMA_FIELD_JMSTAT; f++) {
+    int st = ensure_field(h, f);
+    if (st != GLASMA_OK) {
+      glasma_destroy(h);
+      return st;
+    }
+  }
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    glasma_destroy(h);
+    return cuda_fail(e, "create sync");
+  }
+  *out = h;
+  return GLASMA_OK;
+}
+
+int glasma_destroy(glasma_lattice* h) {
+  if (!h) return GLASMA_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (int i = 0; i < 10; i++)
+    if (h->f[i]) cudaFree(h->f[i]);
+  if (h->staging) cudaFree(h->staging);
+  if (h->scratch) cudaFree(h->scratch);
+  glasma::gaugefix_destroy(h->gf);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return GLASMA_OK;
+}
+
+int glasma_set_stream(glasma_lattice* h, void* stream) {
+  GLASMA_CHECK_HANDLE(h);
+  GLASMA_CUDA(cudaStreamSynchronize(h->stream), "sync old stream");
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+  return GLASMA_OK;
+}
+
+int glasma_set_scale(glasma_lattice* h, double a_scale) {
+  if (!h) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null lattice handle");
+  if (!(a_scale > 0)) return fail(GLASMA_ERR_INVALID_ARGUMENT, "a_scale must be positive");
+  h->a_scale = a_scale;
+  return GLASMA_OK;
+}
+
+int glasma_get_shape(const glasma_lattice* h, int* nx, int* ny, int* nz, int* precision) {
+  if (!h) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null lattice handle");
+  if (nx) *nx = h->g.nx;
+  if (ny) *ny = h->g.ny;
+  if (nz) *nz = h->g.nz;
+  if (precision) *precision = h->precision;
+  return GLASMA_OK;
+}
+
+long long glasma_field_doubles(const glasma_lattice* h, int field) {
+  if (!h || !valid_field(field)) return -1;
+  return h->g.S * host_doubles_per_site(field);
+}
+
+static int upload_common(glasma_lattice* h, int field, const double* src, cudaMemcpyKind kind) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!valid_field(field)) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown field");
+  if (!src) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null source");
+  int st = ensure_field(h, field);
+  if (st) return st;
+  const int P = host_doubles_per_site(field);
+  const size_t bytes = (size_t)h->g.S * P * sizeof(double);
+  st = ensure_staging(h, bytes);
+  if (st) return st;
+  GLASMA_CUDA(cudaMemcpyAsync(h->staging, src, bytes, kind, h->stream), "upload copy");
+  cudaError_t e = h->precision == GLASMA_FP64
+                      ? glasma::launch_aos_to_soa<double>(h->staging, static_cast<double*>(h->f[field]), h->g.S, P, h->stream)
+                      : glasma::launch_aos_to_soa<float>(h->staging, static_cast<float*>(h->f[field]), h->g.S, P, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "aos_to_soa");
+  return GLASMA_OK;
+}
+
+static int download_common(glasma_lattice* h, int field, double* dst, cudaMemcpyKind kind) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!valid_field(field)) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown field");
+  if (!dst) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null destination");
+  int st = ensure_field(h, field);
+  if (st) return st;
+  const int P = host_doubles_per_site(field);
+  const size_t bytes = (size_t)h->g.S * P * sizeof(double);
+  st = ensure_staging(h, bytes);
+  if (st) return st;
+  cudaError_t e = h->precision == GLASMA_FP64
+                      ? glasma::launch_soa_to_aos<double>(static_cast<const double*>(h->f[field]), h->staging, h->g.S, P, h->stream)
+                      : glasma::launch_soa_to_aos<float>(static_cast<const float*>(h->f[field]), h->staging, h->g.S, P, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "soa_to_aos");
+  GLASMA_CUDA(cudaMemcpyAsync(dst, h->staging, bytes, kind, h->stream), "download copy");
+  GLASMA_CUDA(cudaStreamSynchronize(h->stream), "download sync");
+  return GLASMA_OK;
+}
+
+int glasma_upload(glasma_lattice* h, int field, const double* host) {
+  return upload_common(h, field, host, cudaMemcpyHostToDevice);
+}
+int glasma_download(glasma_lattice* h, int field, double* host) {
+  return download_common(h, field, host, cudaMemcpyDeviceToHost);
+}
+int glasma_upload_device(glasma_lattice* h, int field, const double* dev) {
+  return upload_common(h, field, dev, cudaMemcpyDeviceToDevice);
+}
+int glasma_download_device(glasma_lattice* h, int field, double* dev) {
+  return download_common(h, field, dev, cudaMemcpyDeviceToDevice);
+}
+
+int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags) {
+  GLASMA_CHECK_HANDLE(h);
+  if (nsteps < 0) return fail(GLASMA_ERR_INVALID_ARGUMENT, "nsteps < 0");
+  if (flags & ~GLASMA_STEP_SAVE_UOLD) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown step flag");
+  if (nsteps == 0) return GLASMA_OK;
+  return h->precision == GLASMA_FP64 ? step_impl<double>(h, dt, nsteps, flags) : step_impl<float>(h, dt, nsteps, flags);
+}
+
+int glasma_step_profiled(glasma_lattice* h, double dt, int nsteps, unsigned flags, double* kernel_ms) {
+  GLASMA_CHECK_HANDLE(h);
+  if (nsteps <= 0 || !kernel_ms) return fail(GLASMA_ERR_INVALID_ARGUMENT, "nsteps <= 0 or null kernel_ms");
+  if (flags & ~GLASMA_STEP_SAVE_UOLD) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown step flag");
+  std::vector<cudaEvent_t> ev((size_t)nsteps * 3);
+  for (auto& x : ev) GLASMA_CUDA(cudaEventCreate(&x), "cudaEventCreate");
+  int st = h->precision == GLASMA_FP64 ? step_impl<double>(h, dt, nsteps, flags, ev.data())
+                                       : step_impl<float>(h, dt, nsteps, flags, ev.data());
+  if (st == GLASMA_OK) {
+    cudaError_t e = cudaEventSynchronize(ev.back());
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaEventSynchronize");
+  }
+  kernel_ms[0] = kernel_ms[1] = 0.0;
+  if (st == GLASMA_OK) {
+    for (int n = 0; n < nsteps; n++) {
+      float a = 0.f, b = 0.f;
+      cudaEventElapsedTime(&a, ev[3 * n], ev[3 * n + 1]);
+      cudaEventElapsedTime(&b, ev[3 * n + 1], ev[3 * n + 2]);
+      kernel_ms[0] += a;
+      kernel_ms[1] += b;
+    }
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  return st;
+}
+
+#define GLASMA_DISPATCH(h, call_double, call_float) \
+  ((h)->precision == GLASMA_FP64 ? (call_double) : (call_float))
+
+int glasma_update_efield(glasma_lattice* h, double dt) {
+  GLASMA_CHECK_HANDLE(h);
+  int st = sync_field_ghosts(h, GLASMA_FIELD_U);
+  if (st) return st;
+  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_efield_only<double>(h->g, ptrs<double>(h), dt, h->stream),
+                                  glasma::launch_efield_only<float>(h->g, ptrs<float>(h), dt, h->stream));
+  return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "update_efield");
+}
+
+int glasma_update_jstat(glasma_lattice* h, double dt) {
+  GLASMA_CHECK_HANDLE(h);
+  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_jstat_only<double>(h->g, ptrs<double>(h), dt, h->stream),
+                                  glasma::launch_jstat_only<float>(h->g, ptrs<float>(h), dt, h->stream));
+  return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "update_jstat");
+}
+
+int glasma_update_links(glasma_lattice* h, double dt_arg) {
+  GLASMA_CHECK_HANDLE(h);
+  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_links_only<double>(h->g, ptrs<double>(h), dt_arg, h->stream),
+                                  glasma::launch_links_only<float>(h->g, ptrs<float>(h), dt_arg, h->stream));
+  return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "update_links");
+}
+
+int glasma_save_old_link(glasma_lattice* h) {
+  GLASMA_CHECK_HANDLE(h);
+  int st = sync_field_ghosts(h, GLASMA_FIELD_U);
+  if (st) return st;
+  cudaError_t e = GLASMA_DISPATCH(
+      h,
+      glasma::launch_copy_links<double>(h->g, static_cast<const cx<double>*>(h->f[GLASMA_FIELD_U]),
+                                        static_cast<cx<double>*>(h->f[GLASMA_FIELD_UOLD]), h->stream),
+      glasma::launch_copy_links<float>(h->g, static_cast<const cx<float>*>(h->f[GLASMA_FIELD_U]),
+                                       static_cast<cx<float>*>(h->f[GLASMA_FIELD_UOLD]), h->stream));
+  return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "save_old_link");
+}
+
+int glasma_update_j(glasma_lattice* h, double dt) {
+  GLASMA_CHECK_HANDLE(h);
+  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_j_only<double>(h->g, ptrs<double>(h), dt, h->stream),
+                                  glasma::launch_j_only<float>(h->g, ptrs<float>(h), dt, h->stream));
+  return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "update_j");
+}
+
+int glasma_bulk(glasma_lattice* h, double out[16]) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!out) return fail(GLASMA_ERR_INVALID_ARGUMENT, "out is null");
+  int st = ensure_scratch(h);
+  if (st) return st;
+  double* res = h->scratch + h->scratch_doubles - 32;
+  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_bulk<double>(h->g, ptrs<double>(h), h->scratch, res, h->stream),
+                                  glasma::launch_bulk<float>(h->g, ptrs<float>(h), h->scratch, res, h->stream));
+  if (e != cudaSuccess) return cuda_fail(e, "bulk");
+  double r[7];
+  st = copy_results_to_host(h, res, r, 7);
+  if (st) return st;
+  // Observables::Bulk constants and accessors (S/OBSERVABLES/BulkObservables.cpp:22-62)
+  const double a3 = h->g.a[0] * h->g.a[1] * h->g.a[2];
+  double cB[3], cE[3], cS[3];
+  for (int mu = 0; mu < 3; mu++) {
+    const double q = h->g.a[mu] * h->a_scale * h->a_scale / a3;
+    cB[mu] = q * q;
+    cE[mu] = q * q;
+    cS[mu] = h->g.a[mu] * h->a_scale / (a3 * a3);
+  }
+  const double ES[3] = {r[3], r[4], r[5]}, BS[3] = {r[0], r[1], r[2]}, ED[3] = {0.0, 0.0, r[6]};
+  for (int i = 0; i < 3; i++) {
+    out[i] = ES[i];
+    out[3 + i] = BS[i];
+    out[6 + i] = ED[i];
+  }
+  const double e0 = cE[0] * ES[0], e1 = cE[1] * ES[1], e2 = cE[2] * ES[2];
+  const double b0 = cB[0] * BS[0], b1 = cB[1] * BS[1], b2 = cB[2] * BS[2];
+  out[9] = 0.5 * (e0 + e1 + e2 + b0 + b1 + b2);
+  out[10] = 0.5 * ((e1 + e2 + b1 + b2) - (e0 + b0));
+  out[11] = 0.5 * ((e0 + e2 + b0 + b2) - (e1 + b1));
+  out[12] = 0.5 * ((e0 + e1 + b0 + b1) - (e2 + b2));
+  out[13] = 0.5 * (e0 + e1 + e2);
+  out[14] = 0.5 * (b0 + b1 + b2);
+  out[15] = cS[0] * ED[0] + cS[1] * ED[1] + cS[2] * ED[2];
+  return GLASMA_OK;
+}
+
+int glasma_gauss(glasma_lattice* h, int sync_first, double* max_violation, double* avg_violation, double* zprofile) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!max_violation || !avg_violation) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null output");
+  int st = ensure_scratch(h);
+  if (st) return st;
+  if (sync_first) {
+    const int fs[4] = {GLASMA_FIELD_JPSTAT, GLASMA_FIELD_JMSTAT, GLASMA_FIELD_U, GLASMA_FIELD_E};
+    for (int f : fs)
+      if ((st = sync_field_ghosts(h, f))) return st;
+  }
+  double* res = h->scratch + h->scratch_doubles - 32;
+  double* prof = zprofile ? h->scratch + h->scratch_doubles - 64 - (size_t)h->g.nz : nullptr;
+  cudaError_t e = GLASMA_DISPATCH(
+      h, glasma::launch_gauss<double>(h->g, ptrs<double>(h), h->a_scale, h->scratch, res, prof, h->stream),
+      glasma::launch_gauss<float>(h->g, ptrs<float>(h), h->a_scale, h->scratch, res, prof, h->stream));
+  if (e != cudaSuccess) return cuda_fail(e, "gauss");
+  double r[2];
+  if ((st = copy_results_to_host(h, res, r, 2))) return st;
+  if (zprofile && (st = copy_results_to_host(h, prof, zprofile, (size_t)h->g.nz))) return st;
+  *max_violation = r[1];
+  *avg_violation = std::sqrt(r[0] / (8.0 * (double)h->g.vol));
+  return GLASMA_OK;
+}
+
+int glasma_unitarity(glasma_lattice* h, double* max_violation, double* avg_violation) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!max_violation || !avg_violation) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null output");
+  int st = ensure_scratch(h);
+  if (st) return st;
+  double* res = h->scratch + h->scratch_doubles - 32;
+  cudaError_t e = GLASMA_DISPATCH(
+      h,
+      glasma::launch_unitarity<double>(h->g, static_cast<const cx<double>*>(h->f[GLASMA_FIELD_U]), h->scratch, res, h->stream),
+      glasma::launch_unitarity<float>(h->g, static_cast<const cx<float>*>(h->f[GLASMA_FIELD_U]), h->scratch, res, h->stream));
+  if (e != cudaSuccess) return cuda_fail(e, "unitarity");
+  double r[2];
+  if ((st = copy_results_to_host(h, res, r, 2))) return st;
+  *max_violation = r[1];
+  *avg_violation = std::sqrt(r[0] / (3.0 * (double)h->g.vol));
+  return GLASMA_OK;
+}
+
+int glasma_emt_map(glasma_lattice* h, double* out) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!out) return fail(GLASMA_ERR_INVALID_ARGUMENT, "out is null");
+  int st = ensure_scratch(h);
+  if (st) return st;
+  // CreateMap syncs the ghosts of UOld and U inside its site loop (S/OBSERVABLES/EnergyMomentumTensor.cpp:132-133)
+  if ((st = sync_field_ghosts(h, GLASMA_FIELD_UOLD))) return st;
+  if ((st = sync_field_ghosts(h, GLASMA_FIELD_U))) return st;
+  const long long nres = (long long)h->g.nz * 10;
+  double* res = h->scratch + h->scratch_doubles - 64 - (size_t)h->g.nz * 11;
+  cudaError_t e = GLASMA_DISPATCH(
+      h, glasma::launch_emt_map<double>(h->g, ptrs<double>(h), h->a_scale, h->scratch, res, h->stream),
+      glasma::launch_emt_map<float>(h->g, ptrs<float>(h), h->a_scale, h->scratch, res, h->stream));
+  if (e != cudaSuccess) return cuda_fail(e, "emt_map");
+  return copy_results_to_host(h, res, out, (size_t)nres);
+}
+
+int glasma_reunitarize(glasma_lattice* h) {
+  GLASMA_CHECK_HANDLE(h);
+  cudaError_t e = GLASMA_DISPATCH(
+      h, glasma::launch_reunitarize<double>(h->g, static_cast<cx<double>*>(h->f[GLASMA_FIELD_U]), h->stream),
+      glasma::launch_reunitarize<float>(h->g, static_cast<cx<float>*>(h->f[GLASMA_FIELD_U]), h->stream));
+  return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "reunitarize");
+}
+
+int glasma_gauge_reset(glasma_lattice* h) {
+  GLASMA_CHECK_HANDLE(h);
+  if (h->f[GLASMA_FIELD_G]) {
+    cudaFree(h->f[GLASMA_FIELD_G]);
+    h->f[GLASMA_FIELD_G] = nullptr;
+  }
+  return ensure_field(h, GLASMA_FIELD_G);
+}
+
+int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double tol, unsigned flags, double* log,
+                       int* iterations) {
+  GLASMA_CHECK_HANDLE(h);
+  if (max_iters < 0) return fail(GLASMA_ERR_INVALID_ARGUMENT, "max_iters < 0");
+  if (flags & ~GLASMA_GF_PROJECT_ZERO_MODE) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown gauge-fixing flag");
+  int st;
+  for (int f : {GLASMA_FIELD_G, GLASMA_FIELD_UG, GLASMA_FIELD_EG})
+    if ((st = ensure_field(h, f))) return st;
+  if ((st = ensure_scratch(h))) return st;
+  glasma::GaugeFixArgs a;
+  a.g = h->g;
+  a.precision = h->precision;
+  a.a_scale = h->a_scale;
+  a.stream = h->stream;
+  a.U = h->f[GLASMA_FIELD_U];
+  a.E = h->f[GLASMA_FIELD_E];
+  a.G = h->f[GLASMA_FIELD_G];
+  a.UG = h->f[GLASMA_FIELD_UG];
+  a.EG = h->f[GLASMA_FIELD_EG];
+  a.scratch = h->scratch;
+  a.scratch_doubles = h->scratch_doubles;
+  std::string err;
+  int n = 0;
+  st = glasma::gaugefix_run(&h->gf, a, alpha, max_iters, tol, flags, log, &n, &err);
+  if (iterations) *iterations = n;
+  if (st != GLASMA_OK) return fail(st, err);
+  return GLASMA_OK;
+}
+
+int glasma_synchronize(glasma_lattice* h) {
+  GLASMA_CHECK_HANDLE(h);
+  GLASMA_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  GLASMA_CUDA(cudaGetLastError(), "pending error");
+  return GLASMA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+// lattice.cuh -- device data layout of one lattice and the internal launch API.
+//
+// HBM layout (structure of arrays, one array per matrix element / colour):
+//   site   s = x + Nx*(y + Ny*(z+1)), x,y periodic, z in [-1, Nz]; the slices
+//          z=-1 and z=Nz are the reference's open-boundary ghost slices
+//          (S/SUNcIndexing.cpp:82, S/LATTICE/GaugeLinks.cpp:27-36, 59-66)
+//   links  U[(mu*9 + k)*S + s]  complex (k = i + 3*j, the reference's element order)
+//   E      E[(mu*8 + a)*S + s]
+//   J      J[a*S + s]           (Jp, Jm, JpStat, JmStat)
+//   G      G[k*S + s]           complex
+// S = Nx*Ny*(Nz+2).  Consecutive x are consecutive addresses, so a warp that
+// walks x reads 32 consecutive elements of every component array.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "su3.cuh"
+
+namespace glasma {
+
+struct Geometry {
+  int nx, ny, nz;
+  long long plane;  // nx*ny
+  long long S;      // plane*(nz+2), sites including ghost slices
+  long long vol;    // plane*nz, interior sites
+  double a[3];
+};
+
+template <typename T>
+struct FieldPtrs {
+  cx<T>* U;
+  cx<T>* UOld;
+  T* E;
+  T* Jp;
+  T* Jm;
+  T* JpStat;
+  T* JmStat;
+};
+
+__device__ __forceinline__ long long site_index(const Geometry& g, int x, int y, int z) {
+  return (long long)x + (long long)g.nx * ((long long)y + (long long)g.ny * (long long)(z + 1));
+}
+
+template <typename T>
+__device__ __forceinline__ void load_link(const cx<T>* __restrict__ U, long long S, int mu, long long s, Mat<T>& m) {
+  const cx<T>* p = U + (long long)(mu * 9) * S + s;
+#pragma unroll
+  for (int k = 0; k < 9; k++) m.e[k] = p[(long long)k * S];
+}
+template <typename T>
+__device__ __forceinline__ void store_link(cx<T>* __restrict__ U, long long S, int mu, long long s, const Mat<T>& m) {
+  cx<T>* p = U + (long long)(mu * 9) * S + s;
+#pragma unroll
+  for (int k = 0; k < 9; k++) p[(long long)k * S] = m.e[k];
+}
+template <typename T>
+__device__ __forceinline__ void load_alg(const T* __restrict__ F, long long S, long long base, long long s, Alg<T>& v) {
+  const T* p = F + base * S + s;
+#pragma unroll
+  for (int a = 0; a < 8; a++) v.a[a] = p[(long long)a * S];
+}
+template <typename T>
+__device__ __forceinline__ void store_alg(T* __restrict__ F, long long S, long long base, long long s, const Alg<T>& v) {
+  T* p = F + base * S + s;
+#pragma unroll
+  for (int a = 0; a < 8; a++) p[(long long)a * S] = v.a[a];
+}
+
+// ---- launch API shared between translation units (host side) ------------------
+// All launches go to `stream`.  Return cudaGetLastError() of the launch.
+template <typename T>
+cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second_half,
+                           cudaStream_t stream);
+template <typename T>
+cudaError_t launch_sync_ghosts(const Geometry& g, T* base, int components, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_reunitarize(const Geometry& g, cx<T>* U, cudaStream_t stream);
+
+// Sub-step kernels with the reference's exact sub-step boundaries.
+template <typename T>
+cudaError_t launch_efield_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_jstat_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_j_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_links_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_copy_links(const Geometry& g, const cx<T>* src, cx<T>* dst, cudaStream_t stream);
+
+// AoS (reference host layout, double) <-> SoA (device, T).  `aos` is device memory.
+template <typename T>
+cudaError_t launch_aos_to_soa(const double* aos, T* soa, long long S, int per_site, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_soa_to_aos(const T* soa, double* aos, long long S, int per_site, cudaStream_t stream);
+
+// Observables.  `partials` is device scratch of at least observable_scratch_doubles(g) doubles.
+long long observable_scratch_doubles(const Geometry& g);
+template <typename T>
+cudaError_t launch_bulk(const Geometry& g, FieldPtrs<T> f, double* partials, double* result7, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_gauss(const Geometry& g, FieldPtrs<T> f, double a_scale, double* partials, double* result2,
+                         double* zprofile, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_unitarity(const Geometry& g, const cx<T>* U, double* partials, double* result2, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_emt_map(const Geometry& g, FieldPtrs<T> f, double a_scale, double* partials, double* result,
+                           cudaStream_t stream);
+
+}  // namespace glasma

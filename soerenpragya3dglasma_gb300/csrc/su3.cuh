@@ -1,0 +1,390 @@
+// su3.cuh -- SU(3) group and algebra arithmetic for the device kernels.
+//
+// Conventions follow the reference (S/ = the reference's SourceCode directory):
+//   * matrix element (i,j) is stored at index i+3*j (S/SUNc/SU3/GroupOperations.cpp:13-15);
+//   * generators t^a = lambda^a/2 with the standard Gell-Mann matrices, and
+//     t^a alpha^a as in S/SUNc/SU3/AlgebraOperations.cpp:31-45;
+//   * ReTrIGen(V)_a = Re tr(i t^a V) (S/SUNc/SU3/GroupOperations.cpp:93-103);
+//   * adjoint actions V (t.e) V^dagger and V^dagger (t.e) V, the SU(3) forms of
+//     the reference's AdjointMultiplication / InverseAdjointMultiplication
+//     (only the SU(2) forms exist in the reference, S/SUNc/SU2/AlgebraOperations.cpp:110-124).
+// exp(i c t^a alpha^a) uses the Cayley-Hamilton closed form of Morningstar and
+// Peardon, Phys. Rev. D 69 (2004) 054501, in place of the reference's
+// eigen-decomposition (S/SUNc/SU3/AlgebraOperations.cpp:48-89).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace glasma {
+
+template <typename T>
+struct alignas(2 * sizeof(T)) cx {
+  T re, im;
+};
+
+template <typename T>
+__device__ __forceinline__ cx<T> mk(T r, T i) {
+  cx<T> c;
+  c.re = r;
+  c.im = i;
+  return c;
+}
+
+template <typename T>
+struct Mat {
+  cx<T> e[9];  // e[i + 3*j]
+};
+
+template <typename T>
+struct Alg {
+  T a[8];
+};
+
+template <typename T>
+struct Consts;
+template <>
+struct Consts<double> {
+  static __device__ __forceinline__ double inv_sqrt3() { return 0.57735026918962576450914878050195745564760175127013; }
+  static __device__ __forceinline__ double inv_sqrt2() { return 0.70710678118654752440084436210484903928483593768847; }
+};
+template <>
+struct Consts<float> {
+  static __device__ __forceinline__ float inv_sqrt3() { return 0.577350269189625764509f; }
+  static __device__ __forceinline__ float inv_sqrt2() { return 0.707106781186547524401f; }
+};
+
+// acc += a*b (complex)
+template <typename T>
+__device__ __forceinline__ void cfma(cx<T>& acc, const cx<T>& a, const cx<T>& b) {
+  acc.re = fma(a.re, b.re, acc.re);
+  acc.re = fma(-a.im, b.im, acc.re);
+  acc.im = fma(a.re, b.im, acc.im);
+  acc.im = fma(a.im, b.re, acc.im);
+}
+// acc += a*conj(b)
+template <typename T>
+__device__ __forceinline__ void cfma_nc(cx<T>& acc, const cx<T>& a, const cx<T>& b) {
+  acc.re = fma(a.re, b.re, acc.re);
+  acc.re = fma(a.im, b.im, acc.re);
+  acc.im = fma(-a.re, b.im, acc.im);
+  acc.im = fma(a.im, b.re, acc.im);
+}
+// acc += conj(a)*b
+template <typename T>
+__device__ __forceinline__ void cfma_cn(cx<T>& acc, const cx<T>& a, const cx<T>& b) {
+  acc.re = fma(a.re, b.re, acc.re);
+  acc.re = fma(a.im, b.im, acc.re);
+  acc.im = fma(a.re, b.im, acc.im);
+  acc.im = fma(-a.im, b.re, acc.im);
+}
+// acc += conj(a)*conj(b)
+template <typename T>
+__device__ __forceinline__ void cfma_cc(cx<T>& acc, const cx<T>& a, const cx<T>& b) {
+  acc.re = fma(a.re, b.re, acc.re);
+  acc.re = fma(-a.im, b.im, acc.re);
+  acc.im = fma(-a.re, b.im, acc.im);
+  acc.im = fma(-a.im, b.re, acc.im);
+}
+
+// C = A B
+template <typename T>
+__device__ __forceinline__ void mul_nn(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) cfma(acc, A.e[i + 3 * k], B.e[k + 3 * j]);
+      C.e[i + 3 * j] = acc;
+    }
+}
+// C = A B^dagger
+template <typename T>
+__device__ __forceinline__ void mul_nd(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) cfma_nc(acc, A.e[i + 3 * k], B.e[j + 3 * k]);
+      C.e[i + 3 * j] = acc;
+    }
+}
+// C = A^dagger B
+template <typename T>
+__device__ __forceinline__ void mul_dn(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) cfma_cn(acc, A.e[k + 3 * i], B.e[k + 3 * j]);
+      C.e[i + 3 * j] = acc;
+    }
+}
+// C = A^dagger B^dagger
+template <typename T>
+__device__ __forceinline__ void mul_dd(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) cfma_cc(acc, A.e[k + 3 * i], B.e[j + 3 * k]);
+      C.e[i + 3 * j] = acc;
+    }
+}
+// C += s * A B^dagger
+template <typename T>
+__device__ __forceinline__ void add_mul_nd(const Mat<T>& A, const Mat<T>& B, T s, Mat<T>& C) {
+  Mat<T> t;
+  mul_nd(A, B, t);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    C.e[k].re = fma(s, t.e[k].re, C.e[k].re);
+    C.e[k].im = fma(s, t.e[k].im, C.e[k].im);
+  }
+}
+// C += s * A B
+template <typename T>
+__device__ __forceinline__ void add_mul_nn(const Mat<T>& A, const Mat<T>& B, T s, Mat<T>& C) {
+  Mat<T> t;
+  mul_nn(A, B, t);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    C.e[k].re = fma(s, t.e[k].re, C.e[k].re);
+    C.e[k].im = fma(s, t.e[k].im, C.e[k].im);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void set_zero(Mat<T>& A) {
+#pragma unroll
+  for (int k = 0; k < 9; k++) A.e[k] = mk<T>(0, 0);
+}
+
+// out_a = c * Re tr(i t^a V)
+template <typename T>
+__device__ __forceinline__ void retr_itg(const Mat<T>& V, T c, Alg<T>& out) {
+  const T h = T(-0.5) * c;
+  out.a[0] = h * (V.e[3].im + V.e[1].im);
+  out.a[1] = h * (V.e[3].re - V.e[1].re);
+  out.a[2] = h * (V.e[0].im - V.e[4].im);
+  out.a[3] = h * (V.e[6].im + V.e[2].im);
+  out.a[4] = h * (V.e[6].re - V.e[2].re);
+  out.a[5] = h * (V.e[7].im + V.e[5].im);
+  out.a[6] = h * (V.e[7].re - V.e[5].re);
+  out.a[7] = h * (V.e[0].im + V.e[4].im - T(2) * V.e[8].im) * Consts<T>::inv_sqrt3();
+}
+
+// M = t^a al^a (Hermitian, traceless)
+template <typename T>
+__device__ __forceinline__ void herm_from_alg(const Alg<T>& al, Mat<T>& M) {
+  const T s8 = al.a[7] * Consts<T>::inv_sqrt3();
+  M.e[0] = mk<T>(T(0.5) * (al.a[2] + s8), 0);
+  M.e[4] = mk<T>(T(-0.5) * (al.a[2] - s8), 0);
+  M.e[8] = mk<T>(-s8, 0);
+  M.e[1] = mk<T>(T(0.5) * al.a[0], T(0.5) * al.a[1]);   // (1,0)
+  M.e[2] = mk<T>(T(0.5) * al.a[3], T(0.5) * al.a[4]);   // (2,0)
+  M.e[5] = mk<T>(T(0.5) * al.a[5], T(0.5) * al.a[6]);   // (2,1)
+  M.e[3] = mk<T>(M.e[1].re, -M.e[1].im);                // (0,1)
+  M.e[6] = mk<T>(M.e[2].re, -M.e[2].im);                // (0,2)
+  M.e[7] = mk<T>(M.e[5].re, -M.e[5].im);                // (1,2)
+}
+
+// out_a = 2 tr(t^a W) for Hermitian W (only the upper triangle and the real diagonal are read)
+template <typename T>
+__device__ __forceinline__ void alg_from_herm(const Mat<T>& W, Alg<T>& out) {
+  out.a[0] = T(2) * W.e[3].re;
+  out.a[1] = T(-2) * W.e[3].im;
+  out.a[2] = W.e[0].re - W.e[4].re;
+  out.a[3] = T(2) * W.e[6].re;
+  out.a[4] = T(-2) * W.e[6].im;
+  out.a[5] = T(2) * W.e[7].re;
+  out.a[6] = T(-2) * W.e[7].im;
+  out.a[7] = (W.e[0].re + W.e[4].re - T(2) * W.e[8].re) * Consts<T>::inv_sqrt3();
+}
+
+// out = V (t.e) V^dagger  (AdjointMultiplication)
+template <typename T>
+__device__ __forceinline__ void adj_mul(const Mat<T>& V, const Alg<T>& e, Alg<T>& out) {
+  Mat<T> M, W, R;
+  herm_from_alg(e, M);
+  mul_nn(V, M, W);
+  mul_nd(W, V, R);
+  alg_from_herm(R, out);
+}
+// out = V^dagger (t.e) V  (InverseAdjointMultiplication)
+template <typename T>
+__device__ __forceinline__ void inv_adj_mul(const Mat<T>& V, const Alg<T>& e, Alg<T>& out) {
+  Mat<T> M, W, R;
+  herm_from_alg(e, M);
+  mul_dn(V, M, W);
+  mul_nn(W, V, R);
+  alg_from_herm(R, out);
+}
+
+template <typename T>
+struct Trig;
+template <>
+struct Trig<double> {
+  static __device__ __forceinline__ void sincos_(double x, double* s, double* c) { sincos(x, s, c); }
+  static __device__ __forceinline__ double acos_(double x) { return acos(x); }
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  static __device__ __forceinline__ double taylor_c1() { return 1e-6; }
+};
+template <>
+struct Trig<float> {
+  static __device__ __forceinline__ void sincos_(float x, float* s, float* c) { sincosf(x, s, c); }
+  static __device__ __forceinline__ float acos_(float x) { return acosf(x); }
+  static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  static __device__ __forceinline__ float taylor_c1() { return 1e-3f; }
+};
+
+// X = exp(i c t^a al^a), Cayley-Hamilton form exp(iQ) = f0 + f1 Q + f2 Q^2.
+template <typename T>
+__device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
+  Alg<T> sc;
+#pragma unroll
+  for (int a = 0; a < 8; a++) sc.a[a] = c * al.a[a];
+  Mat<T> Q, Q2;
+  herm_from_alg(sc, Q);
+  mul_nn(Q, Q, Q2);
+  const T c1 = T(0.5) * (Q2.e[0].re + Q2.e[4].re + Q2.e[8].re);
+  // det Q = Q00 (Q11 Q22 - |Q12|^2) - ... ; real for Hermitian Q.  Expanded in the
+  // Gell-Mann components for brevity: det Q = tr(Q^3)/3.
+  T c0 = (Q2.e[0].re * Q.e[0].re + Q2.e[4].re * Q.e[4].re + Q2.e[8].re * Q.e[8].re);
+  // tr(Q2 Q) = sum_ij Q2_ij Q_ji; add off-diagonal terms (both triangles)
+  c0 += T(2) * (Q2.e[3].re * Q.e[1].re - Q2.e[3].im * Q.e[1].im);  // (0,1)*(1,0) + (1,0)*(0,1)
+  c0 += T(2) * (Q2.e[6].re * Q.e[2].re - Q2.e[6].im * Q.e[2].im);  // (0,2)*(2,0) + (2,0)*(0,2)
+  c0 += T(2) * (Q2.e[7].re * Q.e[5].re - Q2.e[7].im * Q.e[5].im);  // (1,2)*(2,1) + (2,1)*(1,2)
+  c0 *= T(1) / T(3);
+  cx<T> f0, f1, f2;
+  if (c1 < Trig<T>::taylor_c1()) {
+    f0 = mk<T>(T(1) - c0 * c0 / T(720), -c0 / T(6) + c1 * c0 / T(120));
+    f1 = mk<T>(c0 / T(24) - c0 * c1 / T(360), T(1) - c1 / T(6) + c1 * c1 / T(120));
+    f2 = mk<T>(T(-0.5) + c1 / T(24) - c1 * c1 / T(720), c0 / T(120));
+  } else {
+    const bool neg = c0 < T(0);
+    const T ac0 = neg ? -c0 : c0;
+    const T s3 = Trig<T>::sqrt_(c1 * (T(1) / T(3)));
+    const T c0max = T(2) * s3 * s3 * s3;
+    T r = ac0 / c0max;
+    r = r > T(1) ? T(1) : r;
+    const T theta = Trig<T>::acos_(r);
+    T st, ct;
+    Trig<T>::sincos_(theta * (T(1) / T(3)), &st, &ct);
+    const T u = s3 * ct;
+    const T w = Trig<T>::sqrt_(c1) * st;
+    const T u2 = u * u, w2 = w * w;
+    T sw, cw;
+    Trig<T>::sincos_(w, &sw, &cw);
+    T xi0;
+    if (w < T(0.05)) {
+      xi0 = T(1) - w2 / T(6) * (T(1) - w2 / T(20) * (T(1) - w2 / T(42) * (T(1) - w2 / T(72))));
+    } else {
+      xi0 = sw / w;
+    }
+    T s2u, c2u, su, cu;
+    Trig<T>::sincos_(T(2) * u, &s2u, &c2u);
+    Trig<T>::sincos_(u, &su, &cu);
+    // e^{-iu} = (cu, -su)
+    // h0 = (u^2-w^2) e^{2iu} + e^{-iu} (8u^2 cos w + 2iu(3u^2+w^2) xi0)
+    const T a0r = T(8) * u2 * cw, a0i = T(2) * u * (T(3) * u2 + w2) * xi0;
+    const T h0r = (u2 - w2) * c2u + (cu * a0r + su * a0i);
+    const T h0i = (u2 - w2) * s2u + (cu * a0i - su * a0r);
+    // h1 = 2u e^{2iu} - e^{-iu} (2u cos w - i(3u^2-w^2) xi0)
+    const T a1r = T(2) * u * cw, a1i = -(T(3) * u2 - w2) * xi0;
+    const T h1r = T(2) * u * c2u - (cu * a1r + su * a1i);
+    const T h1i = T(2) * u * s2u - (cu * a1i - su * a1r);
+    // h2 = e^{2iu} - e^{-iu} (cos w + 3iu xi0)
+    const T a2r = cw, a2i = T(3) * u * xi0;
+    const T h2r = c2u - (cu * a2r + su * a2i);
+    const T h2i = s2u - (cu * a2i - su * a2r);
+    const T den = T(1) / (T(9) * u2 - w2);
+    f0 = mk<T>(h0r * den, h0i * den);
+    f1 = mk<T>(h1r * den, h1i * den);
+    f2 = mk<T>(h2r * den, h2i * den);
+    if (neg) {
+      f0.im = -f0.im;
+      f1.re = -f1.re;
+      f2.im = -f2.im;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    cx<T> v = mk<T>(0, 0);
+    cfma(v, f1, Q.e[k]);
+    cfma(v, f2, Q2.e[k]);
+    X.e[k] = v;
+  }
+  X.e[0].re += f0.re;
+  X.e[0].im += f0.im;
+  X.e[4].re += f0.re;
+  X.e[4].im += f0.im;
+  X.e[8].re += f0.re;
+  X.e[8].im += f0.im;
+}
+
+// ||V V^dagger - 1||_F  (S/SUNc/SU3/GroupOperations.cpp:337-349)
+template <typename T>
+__device__ __forceinline__ T unitarity_norm(const Mat<T>& V) {
+  Mat<T> C;
+  mul_nd(V, V, C);
+  T n = 0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const T d = C.e[k].re - ((k % 4 == 0) ? T(1) : T(0));
+    n += d * d + C.e[k].im * C.e[k].im;
+  }
+  return sqrt(n);
+}
+
+// Project onto SU(3): Gram-Schmidt on the first two rows, third row = conj(row0 x row1).
+template <typename T>
+__device__ __forceinline__ void reunitarize(Mat<T>& V) {
+  // row r element j is e[r + 3*j]
+  T n0 = 0;
+#pragma unroll
+  for (int j = 0; j < 3; j++) n0 += V.e[3 * j].re * V.e[3 * j].re + V.e[3 * j].im * V.e[3 * j].im;
+  const T i0 = T(1) / sqrt(n0);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    V.e[3 * j].re *= i0;
+    V.e[3 * j].im *= i0;
+  }
+  cx<T> p = mk<T>(0, 0);  // <row0, row1> = sum conj(r0) r1
+#pragma unroll
+  for (int j = 0; j < 3; j++) cfma_cn(p, V.e[3 * j], V.e[1 + 3 * j]);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    // r1 -= p r0
+    const cx<T> r0 = V.e[3 * j];
+    V.e[1 + 3 * j].re -= p.re * r0.re - p.im * r0.im;
+    V.e[1 + 3 * j].im -= p.re * r0.im + p.im * r0.re;
+  }
+  T n1 = 0;
+#pragma unroll
+  for (int j = 0; j < 3; j++) n1 += V.e[1 + 3 * j].re * V.e[1 + 3 * j].re + V.e[1 + 3 * j].im * V.e[1 + 3 * j].im;
+  const T i1 = T(1) / sqrt(n1);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    V.e[1 + 3 * j].re *= i1;
+    V.e[1 + 3 * j].im *= i1;
+  }
+  // r2_j = conj(r0_k r1_l - r0_l r1_k), (j,k,l) cyclic
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int k = (j + 1) % 3, l = (j + 2) % 3;
+    const cx<T> a = V.e[3 * k], b = V.e[1 + 3 * l], c = V.e[3 * l], d = V.e[1 + 3 * k];
+    const T re = (a.re * b.re - a.im * b.im) - (c.re * d.re - c.im * d.im);
+    const T im = (a.re * b.im + a.im * b.re) - (c.re * d.im + c.im * d.re);
+    V.e[2 + 3 * j] = mk<T>(re, -im);
+  }
+}
+
+}  // namespace glasma

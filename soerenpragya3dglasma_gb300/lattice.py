@@ -1,0 +1,197 @@
+"""Host-side handle of one GPU-resident lattice, over the C ABI.
+
+Fields cross the boundary as numpy arrays in the reference's host layout, FP64,
+ghost slices included (site s = x + Nx*(y + Ny*(z+1)), z in [-1, Nz];
+S/SUNcIndexing.cpp:82 with S/ the reference's SourceCode directory):
+
+    U, UOld, UG   complex128 (Nz+2, Ny, Nx, 3, 3, 3)   [z+1, y, x, mu, j, i]
+    E, EG         float64    (Nz+2, Ny, Nx, 3, 8)
+    Jp, Jm, JpStat, JmStat   float64 (Nz+2, Ny, Nx, 8)
+    G             complex128 (Nz+2, Ny, Nx, 3, 3)      [z+1, y, x, j, i]
+
+Any C-contiguous array (or a pinned torch CPU tensor exposing the same bytes)
+with that many doubles is accepted.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_SHAPES = {
+    "U": lambda N: (N[2] + 2, N[1], N[0], 3, 3, 3),
+    "UOld": lambda N: (N[2] + 2, N[1], N[0], 3, 3, 3),
+    "UG": lambda N: (N[2] + 2, N[1], N[0], 3, 3, 3),
+    "G": lambda N: (N[2] + 2, N[1], N[0], 3, 3),
+    "E": lambda N: (N[2] + 2, N[1], N[0], 3, 8),
+    "EG": lambda N: (N[2] + 2, N[1], N[0], 3, 8),
+    "Jp": lambda N: (N[2] + 2, N[1], N[0], 8),
+    "Jm": lambda N: (N[2] + 2, N[1], N[0], 8),
+    "JpStat": lambda N: (N[2] + 2, N[1], N[0], 8),
+    "JmStat": lambda N: (N[2] + 2, N[1], N[0], 8),
+}
+_COMPLEX = {"U", "UOld", "UG", "G"}
+
+DYNAMICAL_FIELDS = ("U", "UOld", "E", "Jp", "Jm", "JpStat", "JmStat")
+
+
+def field_shape(name, N):
+    return _SHAPES[name](N)
+
+
+def empty_field(name, N):
+    return np.zeros(field_shape(name, N), dtype=np.complex128 if name in _COMPLEX else np.float64)
+
+
+def _address(arr, n_doubles):
+    """Host address of a C-contiguous buffer holding n_doubles doubles (numpy array or torch CPU tensor)."""
+    if isinstance(arr, np.ndarray):
+        if not arr.flags["C_CONTIGUOUS"]:
+            raise ValueError("field array must be C-contiguous")
+        if arr.nbytes != 8 * n_doubles:
+            raise ValueError("field array has %d bytes, expected %d" % (arr.nbytes, 8 * n_doubles))
+        return arr.ctypes.data
+    # torch tensor
+    if not arr.is_contiguous():
+        raise ValueError("field tensor must be contiguous")
+    if arr.numel() * arr.element_size() != 8 * n_doubles:
+        raise ValueError("field tensor has the wrong number of bytes")
+    return arr.data_ptr()
+
+
+class Lattice:
+    """One lattice resident in GPU memory (the reference's global field singletons,
+    S/LATTICE/SUNcVariables.cpp:4-90, become one handle)."""
+
+    def __init__(self, N, a=(1.0, 1.0, 1.0), precision="fp64", reunitarize_every=0, stream=None):
+        self.lib = _lib.load()
+        self.N = tuple(int(n) for n in N)
+        self.a = tuple(float(x) for x in a)
+        self.precision = precision
+        prec = {"fp64": _lib.FP64, "fp32": _lib.FP32}[precision]
+        h = ctypes.c_void_p()
+        check(self.lib.glasma_create(self.N[0], self.N[1], self.N[2], self.a[0], self.a[1], self.a[2], prec,
+                                     int(reunitarize_every), ctypes.byref(h)))
+        self.h = h
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.glasma_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- plumbing
+    def set_stream(self, stream):
+        """stream: a torch.cuda.Stream, an integer cudaStream_t, or None for the handle's own stream."""
+        ptr = getattr(stream, "cuda_stream", stream)
+        check(self.lib.glasma_set_stream(self.h, ctypes.c_void_p(ptr) if ptr else None))
+
+    def set_scale(self, a_scale):
+        check(self.lib.glasma_set_scale(self.h, float(a_scale)))
+
+    def synchronize(self):
+        check(self.lib.glasma_synchronize(self.h))
+
+    def field_doubles(self, name):
+        return self.lib.glasma_field_doubles(self.h, _lib.FIELDS[name])
+
+    # -- field transfer
+    def upload(self, name, arr):
+        check(self.lib.glasma_upload(self.h, _lib.FIELDS[name], _address(arr, self.field_doubles(name))))
+
+    def download(self, name, out=None):
+        if out is None:
+            out = empty_field(name, self.N)
+        check(self.lib.glasma_download(self.h, _lib.FIELDS[name], _address(out, self.field_doubles(name))))
+        return out
+
+    def upload_device(self, name, dev_ptr):
+        check(self.lib.glasma_upload_device(self.h, _lib.FIELDS[name], ctypes.c_void_p(int(dev_ptr))))
+
+    def download_device(self, name, dev_ptr):
+        check(self.lib.glasma_download_device(self.h, _lib.FIELDS[name], ctypes.c_void_p(int(dev_ptr))))
+
+    def upload_fields(self, fields):
+        for k, v in fields.items():
+            self.upload(k, v)
+
+    def download_fields(self, names=DYNAMICAL_FIELDS):
+        return {k: self.download(k) for k in names}
+
+    # -- dynamics (Dynamics::SUNc, S/DYNAMICS/SUNcDynamics.cpp)
+    def step(self, dt, nsteps=1, save_uold=True):
+        check(self.lib.glasma_step(self.h, float(dt), int(nsteps), _lib.STEP_SAVE_UOLD if save_uold else 0))
+
+    def step_profiled(self, dt, nsteps=1, save_uold=False):
+        """Like step(); returns the summed CUDA-event milliseconds of (efield_jstat, links_j)."""
+        ms = np.zeros(2)
+        check(self.lib.glasma_step_profiled(self.h, float(dt), int(nsteps), _lib.STEP_SAVE_UOLD if save_uold else 0,
+                                            ms.ctypes.data_as(_lib._D)))
+        return ms
+
+    def update_efield(self, dt):
+        check(self.lib.glasma_update_efield(self.h, float(dt)))
+
+    def update_jstat(self, dt):
+        check(self.lib.glasma_update_jstat(self.h, float(dt)))
+
+    def update_links(self, dt_arg):
+        check(self.lib.glasma_update_links(self.h, float(dt_arg)))
+
+    def save_old_link(self):
+        check(self.lib.glasma_save_old_link(self.h))
+
+    def update_j(self, dt):
+        check(self.lib.glasma_update_j(self.h, float(dt)))
+
+    def reunitarize(self):
+        check(self.lib.glasma_reunitarize(self.h))
+
+    # -- observables (S/OBSERVABLES)
+    def bulk(self):
+        out = np.zeros(16)
+        check(self.lib.glasma_bulk(self.h, out.ctypes.data_as(_lib._D)))
+        return out
+
+    def gauss(self, sync_first=False, profile=False):
+        mx, avg = ctypes.c_double(), ctypes.c_double()
+        zp = np.zeros(self.N[2]) if profile else None
+        check(self.lib.glasma_gauss(self.h, int(sync_first), ctypes.byref(mx), ctypes.byref(avg),
+                                    zp.ctypes.data_as(_lib._D) if profile else None))
+        return (mx.value, avg.value, zp) if profile else (mx.value, avg.value)
+
+    def unitarity(self):
+        mx, avg = ctypes.c_double(), ctypes.c_double()
+        check(self.lib.glasma_unitarity(self.h, ctypes.byref(mx), ctypes.byref(avg)))
+        return mx.value, avg.value
+
+    def emt_map(self):
+        out = np.zeros((self.N[2], 10))
+        check(self.lib.glasma_emt_map(self.h, out.ctypes.data_as(_lib._D)))
+        return out
+
+    # -- Coulomb gauge fixing (S/GAUGETRANSFORMATION)
+    def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False):
+        log = np.zeros((max(int(max_iters), 1), 7))
+        n = ctypes.c_int()
+        check(self.lib.glasma_coulomb_fix(self.h, float(alpha), int(max_iters), float(tol),
+                                          _lib.GF_PROJECT_ZERO_MODE if project_zero_mode else 0,
+                                          log.ctypes.data_as(_lib._D), ctypes.byref(n)))
+        return log[: n.value]
+
+    def gauge_reset(self):
+        check(self.lib.glasma_gauge_reset(self.h))

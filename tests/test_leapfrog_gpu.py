@@ -1,0 +1,164 @@
+"""Parity of the CUDA leapfrog and observables (through the C ABI) with the oracle and with
+golden vectors from the reference's own code.  Bar: FP64 relative 1e-10 or better on fields and
+observables; FP32 compared against FP64 with the tolerances stated per test."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from soerenpragya3dglasma_gb300 import Lattice, build
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = O.FIELD_NAMES
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    build.build()
+
+
+def _load(golden_dir, name):
+    return dict(np.load(os.path.join(golden_dir, name)))
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def _gpu(fields, N, a, precision="fp64", **kw):
+    lat = Lattice(N, a, precision=precision, **kw)
+    lat.upload_fields(fields)
+    return lat
+
+
+def test_upload_download_roundtrip_is_bit_exact():
+    N = (5, 3, 4)
+    f = O.random_fields(N, 3, sync=False)
+    f["G"] = O.identity_gauge(N) * (1 + 0.5j)
+    with Lattice(N) as lat:
+        for k, v in f.items():
+            lat.upload(k, v)
+        for k, v in f.items():
+            assert np.array_equal(lat.download(k), v), k
+
+
+@pytest.mark.parametrize("tag,nsteps", [("s1", 1), ("s10", 10)])
+def test_leapfrog_matches_reference_golden(golden_dir, tag, nsteps):
+    g = _load(golden_dir, "leapfrog_random.npz")
+    N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
+    init = {k: g["init_" + k] for k in FIELDS}
+    with _gpu(init, N, a) as lat:
+        lat.step(dt, nsteps)
+        out = lat.download_fields()
+        for k in FIELDS:
+            assert _rel(out[k], g[tag + "_" + k]) < 1e-12, k
+        assert np.allclose(lat.bulk(), g[tag + "_bulk"], rtol=1e-12, atol=1e-12)
+        assert np.allclose(lat.gauss(), g[tag + "_gauss"], rtol=1e-12)
+        mx, avg, prof = lat.gauss(sync_first=True, profile=True)
+        assert np.allclose(prof, g[tag + "_gauss_profile"], rtol=1e-13, atol=1e-14)
+        assert np.allclose(lat.emt_map(), g[tag + "_emt"], rtol=1e-12, atol=1e-13)
+        assert lat.unitarity()[0] < 1e-12
+
+
+@pytest.mark.parametrize("N,a,dt,seed", [((6, 5, 8), (1.0, 1.0, 1.0), 0.125, 11),
+                                         ((8, 8, 16), (1.0, 1.1, 0.5), 0.05, 12),
+                                         ((3, 7, 2), (1.0, 1.0, 1.0), 0.1, 13)])
+def test_leapfrog_matches_oracle(oracle, N, a, dt, seed):
+    f = O.random_fields(N, seed)
+    ref = O.copy_fields(f)
+    oracle.update(ref, N, a, dt, 5)
+    with _gpu(f, N, a) as lat:
+        lat.step(dt, 5)
+        out = lat.download_fields()
+    for k in FIELDS:
+        assert _rel(out[k], ref[k]) < 1e-12, k
+
+
+def test_unsynced_ghosts_are_read_as_the_reference_reads_them(oracle):
+    """Uploaded ghost slices that are out of date: the reference syncs U at the start of the
+    electric update but reads the current ghosts of Jp/Jm as they stand."""
+    N, a, dt = (4, 4, 6), (1.0, 1.0, 1.0), 0.1
+    f = O.random_fields(N, 21, sync=False)
+    ref = O.copy_fields(f)
+    oracle.update(ref, N, a, dt, 2)
+    with _gpu(f, N, a) as lat:
+        lat.step(dt, 2)
+        out = lat.download_fields()
+    for k in FIELDS:
+        assert _rel(out[k], ref[k]) < 1e-12, k
+
+
+def test_substeps_match_oracle(oracle):
+    N, a, dt = (6, 4, 8), (1.0, 0.8, 1.2), 0.1
+    f = O.random_fields(N, 31)
+    ref = O.copy_fields(f)
+    lib = oracle.lib
+    with _gpu(f, N, a) as lat:
+        # Dynamics::SUNc::Update spelled out sub-step by sub-step
+        lat.update_efield(dt)
+        lat.update_jstat(dt)
+        lat.update_links(0.5 * dt)
+        lat.save_old_link()
+        lat.update_j(dt)
+        lat.update_links(0.5 * dt)
+        out = lat.download_fields()
+    oracle.update(ref, N, a, dt, 1)
+    for k in FIELDS:
+        assert _rel(out[k], ref[k]) < 1e-12, k
+
+
+def test_mv_collision_matches_reference_golden(golden_dir):
+    g = _load(golden_dir, "mv_collision.npz")
+    N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
+    init = {k: g["init_" + k] for k in FIELDS}
+    with _gpu(init, N, a) as lat:
+        assert np.allclose(lat.bulk(), g["t0_bulk"], rtol=1e-12, atol=1e-14)
+        assert np.allclose(lat.gauss(), g["t0_gauss"], rtol=1e-10, atol=1e-16)
+        lat.step(dt, int(g["cfg_steps"]))
+        assert np.allclose(lat.bulk(), g["t8_bulk"], rtol=1e-11, atol=1e-11)
+        assert np.allclose(lat.gauss(), g["t8_gauss"], rtol=1e-10, atol=1e-15)
+        assert np.allclose(lat.emt_map(), g["t8_emt"], rtol=1e-10, atol=1e-14)
+
+
+def test_observables_match_oracle_on_larger_lattice(oracle):
+    N, a = (16, 12, 20), (1.0, 1.0, 0.8)
+    f = O.random_fields(N, 41, link_amp=0.2)
+    with _gpu(f, N, a) as lat:
+        assert np.allclose(lat.bulk(), oracle.bulk(f, N, a), rtol=1e-12, atol=1e-10)
+        gm = lat.gauss(profile=True)
+        om = oracle.gauss(f, N, a, profile=True)
+        assert np.allclose(gm[:2], om[:2], rtol=1e-12)
+        assert np.allclose(gm[2], om[2], rtol=1e-12)
+        assert np.allclose(lat.emt_map(), oracle.emt_map(f, N, a), rtol=1e-11, atol=1e-13)
+        assert np.allclose(lat.unitarity(), oracle.unitarity(f, N), rtol=1e-3, atol=1e-15)
+
+
+def test_fp32_tracks_fp64(oracle):
+    """FP32 storage and arithmetic, FP64 reductions: energy within 1e-6 relative after 20 steps of
+    a smooth random field, fields within FP32 rounding growth."""
+    N, a, dt = (12, 12, 16), (1.0, 1.0, 1.0), 0.1
+    f = O.random_fields(N, 51, link_amp=0.15, e_amp=0.1, j_amp=0.02)
+    ref = O.copy_fields(f)
+    oracle.update(ref, N, a, dt, 20)
+    with _gpu(f, N, a, precision="fp32", reunitarize_every=16) as lat:
+        lat.step(dt, 20)
+        e32 = lat.bulk()
+        out = lat.download_fields()
+        umax, _ = lat.unitarity()
+    e64 = oracle.bulk(ref, N, a)
+    assert abs(e32[9] - e64[9]) / abs(e64[9]) < 1e-6
+    assert _rel(out["U"], ref["U"]) < 1e-5
+    assert _rel(out["E"], ref["E"]) < 1e-4
+    assert umax < 1e-5
+
+
+def test_fp32_reunitarize_restores_unitarity():
+    N = (4, 4, 4)
+    f = O.random_fields(N, 61)
+    f["U"] = f["U"] * (1 + 1e-3)
+    with _gpu(f, N, (1.0, 1.0, 1.0), precision="fp32") as lat:
+        assert lat.unitarity()[0] > 1e-3
+        lat.reunitarize()
+        assert lat.unitarity()[0] < 1e-6
