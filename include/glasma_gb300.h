@@ -143,6 +143,13 @@ int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double to
 /* GaugeTransformation::SetIdentity (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:41-60). */
 int glasma_gauge_reset(glasma_lattice* h);
 
+/* The batched 3D FFT used by the gauge fixer, exposed for testing: 8 colour planes of complex
+ * doubles, X[a][z][y][x] (8*Nx*Ny*Nz complex values, interleaved re/im), unnormalised,
+ * exponent sign -1 (inverse = 0) or +1 (inverse = 1), the convention of FFTW's
+ * fftw_plan_many_dft as S/FFT/FFT3D.cpp:126-138 uses it.  `in` and `out` may be host or device
+ * pointers. */
+int glasma_fft3d(glasma_lattice* h, const double* in, double* out, int inverse);
+
 /* Wait for the handle's stream. */
 int glasma_synchronize(glasma_lattice* h);
 const char* glasma_status_string(int status);

@@ -1,18 +1,526 @@
-// gaugefix.cu -- placeholder until the Fourier-accelerated gauge fixer lands.
+// gaugefix.cu -- Fourier-accelerated Coulomb gauge fixing with a hand-written batched 3D FFT.
+//
+// Follows CoulombGaugeFixing::SetCoulombGauge (S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:32-88)
+// and FourierAccelerationAlgorithm::UpdateGaugeTransformation
+// (S/GAUGETRANSFORMATION/ALGORITHMS/FourierAcceleration.cpp:15-142), per iteration:
+//   deviation   w(x) = sum_mu c_mu (UG_mu(x) + UG_mu^d(x-mu)), Delta^a = ReTr(i t^a w)
+//               (S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41); z term only if Nz > 1
+//   FFT         8 colours, unnormalised, forward sign -1 (FFTW semantics of S/FFT/FFT3D.cpp:126-138)
+//   accelerate  Delta(p) <- Delta(p) / (p^2 V) for p^2 > 0; the p = 0 mode is left as it is
+//               (optionally projected out: GLASMA_GF_PROJECT_ZERO_MODE)
+//   inverse FFT
+//   update      wt = exp(-i alpha t.Re Delta), guard ||wt wt^d - 1|| <= 1e-13, G <- wt^d G
+//   transform   UG_mu(x) = G(x) U_mu(x) G^d(x+mu), reading the ghost G(x,y,Nz) before the ghost
+//               sync, as GaugeTransformLinks does (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:111-124)
+// The ghost slices of UG are never written (the reference's gauge-fixed container keeps the
+// identity it was created with), so the backward z link at z = 0 is the identity.
+//
+// All arithmetic is FP64; G / UG / EG are stored in the handle's precision.
+//
+// FFT: the 3D transform is three passes of batched 1D transforms along x, y and z over the
+// colour-major array X[a][z][y][x] (complex double).  A block stages a tile of lines in shared
+// memory (consecutive lines for the x pass; for the y and z passes a tile of consecutive x, so
+// every global access is a contiguous run), transforms it there and writes it back in place:
+// radix-2 decimation in time for power-of-two lengths, a direct DFT otherwise.
+#include <map>
+#include <vector>
+
 #include "../../include/glasma_gb300.h"
 #include "gaugefix.h"
+#include "reduce.cuh"
 
 namespace glasma {
 
-struct GaugeFixState {};
+namespace {
 
-int gaugefix_run(GaugeFixState**, const GaugeFixArgs&, double, int, double, unsigned, double*, int* iterations,
-                 std::string* err) {
-  if (iterations) *iterations = 0;
-  *err = "Coulomb gauge fixing not built yet";
-  return GLASMA_ERR_UNSUPPORTED;
+constexpr int kGfThreads = red::kThreads;
+constexpr int kGfBlocks = 1216;
+constexpr int kFftThreads = 256;
+constexpr int kFftMaxTile = 4096;  // complex doubles staged per block (64 KB)
+
+inline unsigned blocks_for(long long n, int threads, int cap) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  return (unsigned)(b < cap ? b : cap);
 }
 
-void gaugefix_destroy(GaugeFixState* state) { delete state; }
+template <typename T>
+__device__ __forceinline__ void ld_d(const cx<T>* __restrict__ U, long long S, long long comp0, long long s, Mat<double>& m) {
+  const cx<T>* p = U + comp0 * S + s;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const cx<T> v = p[(long long)k * S];
+    m.e[k] = mk<double>((double)v.re, (double)v.im);
+  }
+}
+template <typename T>
+__device__ __forceinline__ void st_d(cx<T>* __restrict__ U, long long S, long long comp0, long long s, const Mat<double>& m) {
+  cx<T>* p = U + comp0 * S + s;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    cx<T> v;
+    v.re = (T)m.e[k].re;
+    v.im = (T)m.e[k].im;
+    p[(long long)k * S] = v;
+  }
+}
+
+__device__ __forceinline__ long long nbr(const Geometry& g, int x, int y, int z, int dx, int dy, int dz) {
+  int xx = x + dx, yy = y + dy;
+  xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
+  yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
+  return site_index(g, xx, yy, z + dz);
+}
+
+// ---- deviation: X = Delta (imaginary part 0); partials {max|Delta|, sum Delta^2, min ReTr w, sum ReTr w}
+template <typename T>
+__global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const cx<T>* UG, double c0, double c1,
+                                                               double c2, double2* X, double* partials) {
+  double v[4] = {0.0, 0.0, 1.0e300, 0.0};
+  const int op[4] = {1, 0, 2, 0};
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long r = idx / g.nx;
+    const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+    const long long s = idx + g.plane;
+    const double c[3] = {c0, c1, c2};
+    const long long back[3] = {nbr(g, x, y, z, -1, 0, 0), nbr(g, x, y, z, 0, -1, 0), s - g.plane};
+    Mat<double> w;
+    set_zero(w);
+    for (int mu = 0; mu < 3; mu++) {
+      if (c[mu] == 0.0) continue;
+      Mat<double> u, d;
+      ld_d(UG, g.S, mu * 9, s, u);
+      ld_d(UG, g.S, mu * 9, back[mu], d);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          const int k = i + 3 * j, kt = j + 3 * i;
+          w.e[k].re += c[mu] * (u.e[k].re + d.e[kt].re);
+          w.e[k].im += c[mu] * (u.e[k].im - d.e[kt].im);
+        }
+    }
+    Alg<double> dev;
+    retr_itg(w, 1.0, dev);
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      v[0] = fmax(v[0], fabs(dev.a[a]));
+      v[1] += dev.a[a] * dev.a[a];
+      X[(long long)a * g.vol + idx] = make_double2(dev.a[a], 0.0);
+    }
+    const double lf = w.e[0].re + w.e[4].re + w.e[8].re;
+    v[2] = fmin(v[2], lf);
+    v[3] += lf;
+  }
+  red::block_reduce_store<4>(v, op, partials + (long long)blockIdx.x * 4);
+}
+
+// ---- momentum-space acceleration
+__global__ void accelerate_kernel(int nx, int ny, int nz, double ax, double ay, double az, double2* X, int project_zero) {
+  const long long V = (long long)nx * ny * nz;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 8 * V) return;
+  const long long site = i % V;
+  const long long r = site / nx;
+  const int px = (int)(site - r * nx), pz = (int)(r / ny), py = (int)(r - (long long)pz * ny);
+  const double p2 = (2.0 - 2.0 * cospi(2.0 * px / (double)nx)) / (ax * ax) +
+                    (2.0 - 2.0 * cospi(2.0 * py / (double)ny)) / (ay * ay) +
+                    (2.0 - 2.0 * cospi(2.0 * pz / (double)nz)) / (az * az);
+  if (p2 > 0.0) {
+    const double f = 1.0 / ((double)V * p2);
+    double2 v = X[i];
+    v.x *= f;
+    v.y *= f;
+    X[i] = v;
+  } else if (project_zero) {
+    X[i] = make_double2(0.0, 0.0);
+  }
+}
+
+// ---- update of G; partials {max step, sum step^2, guard count}
+template <typename T>
+__global__ void __launch_bounds__(kGfThreads) update_kernel(Geometry g, const double2* X, cx<T>* G, double alpha,
+                                                            double* partials) {
+  double v[3] = {0.0, 0.0, 0.0};
+  const int op[3] = {1, 0, 0};
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
+       idx += (long long)gridDim.x * blockDim.x) {
+    Alg<double> upd;
+#pragma unroll
+    for (int a = 0; a < 8; a++) upd.a[a] = X[(long long)a * g.vol + idx].x;
+    Mat<double> wt, gm, gn;
+    expi(-alpha, upd, wt);
+    if (unitarity_norm(wt) > 1e-13) v[2] += 1.0;
+    const double sr = 3.0 - wt.e[0].re - wt.e[4].re - wt.e[8].re, si = -(wt.e[0].im + wt.e[4].im + wt.e[8].im);
+    const double step = sqrt(sr * sr + si * si);
+    v[0] = fmax(v[0], step);
+    v[1] += step * step;
+    const long long s = idx + g.plane;
+    ld_d(G, g.S, 0, s, gm);
+    mul_dn(wt, gm, gn);
+    st_d(G, g.S, 0, s, gn);
+  }
+  red::block_reduce_store<3>(v, op, partials + (long long)blockIdx.x * 3);
+}
+
+// ---- UG_mu(x) = G(x) U_mu(x) G^d(x+mu), interior sites
+template <typename T>
+__global__ void __launch_bounds__(128) transform_links_kernel(Geometry g, const cx<T>* U, const cx<T>* G, cx<T>* UG) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.vol) return;
+  const long long r = idx / g.nx;
+  const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+  const long long s = idx + g.plane;
+  const long long fwd[3] = {nbr(g, x, y, z, 1, 0, 0), nbr(g, x, y, z, 0, 1, 0), s + g.plane};
+  Mat<double> gx, u, gy, t, o;
+  ld_d(G, g.S, 0, s, gx);
+  for (int mu = 0; mu < 3; mu++) {
+    ld_d(U, g.S, mu * 9, s, u);
+    ld_d(G, g.S, 0, fwd[mu], gy);
+    mul_nn(gx, u, t);
+    mul_nd(t, gy, o);
+    st_d(UG, g.S, mu * 9, s, o);
+  }
+}
+
+// ---- EG_mu(x) = G(x) E_mu(x) G^d(x)
+template <typename T>
+__global__ void __launch_bounds__(128) transform_efield_kernel(Geometry g, const T* E, const cx<T>* G, T* EG) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.vol) return;
+  const long long s = idx + g.plane;
+  Mat<double> gx;
+  ld_d(G, g.S, 0, s, gx);
+  for (int mu = 0; mu < 3; mu++) {
+    Alg<double> e, o;
+#pragma unroll
+    for (int a = 0; a < 8; a++) e.a[a] = (double)E[(long long)(mu * 8 + a) * g.S + s];
+    adj_mul(gx, e, o);
+#pragma unroll
+    for (int a = 0; a < 8; a++) EG[(long long)(mu * 8 + a) * g.S + s] = (T)o.a[a];
+  }
+}
+
+// ---- FFT
+__global__ void twiddle_kernel(double2* tw, int n, int count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  double s, c;
+  sincospi(-2.0 * (double)k / (double)n, &s, &c);
+  tw[k] = make_double2(c, s);
+}
+
+// Element (line l, k) of a batch of 1D transforms of length n, stride st:
+//   st == 1 : l*n + k
+//   st  > 1 : o*st*n + i + k*st  with l = (o, i), i in [0, st)
+// A block owns `tw_lines` lines: consecutive l for st == 1, consecutive i for st > 1.
+__device__ __forceinline__ long long fft_addr(long long tile, int t, int k, int n, long long st, int tile_lines) {
+  if (st == 1) return (tile * tile_lines + t) * (long long)n + k;
+  const long long tiles_per_block = st / tile_lines;
+  const long long o = tile / tiles_per_block;
+  const long long i = (tile - o * tiles_per_block) * tile_lines + t;
+  return o * st * n + i + (long long)k * st;
+}
+
+__global__ void __launch_bounds__(kFftThreads) fft_pow2_kernel(double2* X, int n, int logn, long long st, int tile_lines,
+                                                               const double2* __restrict__ tw, int inverse) {
+  extern __shared__ double2 sm[];
+  const long long tile = blockIdx.x;
+  const int total = tile_lines * n;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int t, k;
+    if (st == 1) {
+      t = idx / n;
+      k = idx - t * n;
+    } else {
+      t = idx % tile_lines;
+      k = idx / tile_lines;
+    }
+    const int rk = (int)(__brev((unsigned)k) >> (32 - logn));
+    sm[t * n + rk] = X[fft_addr(tile, t, k, n, st, tile_lines)];
+  }
+  __syncthreads();
+  const int halfn = n >> 1;
+  for (int s = 1; s <= logn; s++) {
+    const int half = 1 << (s - 1);
+    for (int j = threadIdx.x; j < tile_lines * halfn; j += blockDim.x) {
+      const int t = j / halfn, b = j - t * halfn;
+      const int grp = b >> (s - 1), pos = b & (half - 1);
+      const int i0 = t * n + (grp << s) + pos, i1 = i0 + half;
+      double2 w = tw[pos << (logn - s)];
+      if (inverse) w.y = -w.y;
+      const double2 a = sm[i0], c = sm[i1];
+      const double tr = w.x * c.x - w.y * c.y, ti = w.x * c.y + w.y * c.x;
+      sm[i0] = make_double2(a.x + tr, a.y + ti);
+      sm[i1] = make_double2(a.x - tr, a.y - ti);
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int t, k;
+    if (st == 1) {
+      t = idx / n;
+      k = idx - t * n;
+    } else {
+      t = idx % tile_lines;
+      k = idx / tile_lines;
+    }
+    X[fft_addr(tile, t, k, n, st, tile_lines)] = sm[t * n + k];
+  }
+}
+
+// Direct DFT for lengths that are not powers of two; tw holds exp(-2 pi i k / n), k < n.
+__global__ void __launch_bounds__(kFftThreads) dft_kernel(double2* X, int n, long long st, int tile_lines,
+                                                          const double2* __restrict__ tw, int inverse) {
+  extern __shared__ double2 sm[];
+  const long long tile = blockIdx.x;
+  const int total = tile_lines * n;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int t = st == 1 ? idx / n : idx % tile_lines;
+    const int k = st == 1 ? idx - t * n : idx / tile_lines;
+    sm[t * n + k] = X[fft_addr(tile, t, k, n, st, tile_lines)];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int t = st == 1 ? idx / n : idx % tile_lines;
+    const int k = st == 1 ? idx - t * n : idx / tile_lines;
+    double re = 0.0, im = 0.0;
+    for (int j = 0; j < n; j++) {
+      double2 w = tw[(int)(((long long)j * k) % n)];
+      if (inverse) w.y = -w.y;
+      const double2 a = sm[t * n + j];
+      re += a.x * w.x - a.y * w.y;
+      im += a.x * w.y + a.y * w.x;
+    }
+    X[fft_addr(tile, t, k, n, st, tile_lines)] = make_double2(re, im);
+  }
+}
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+int ilog2(int n) {
+  int l = 0;
+  while ((1 << l) < n) l++;
+  return l;
+}
+
+}  // namespace
+
+struct GaugeFixState {
+  Geometry g;
+  int precision = -1;
+  double2* X = nullptr;
+  std::map<int, double2*> twiddles;
+  std::vector<double> host_results;
+};
+
+namespace {
+
+int tile_lines_for(int n, long long st, long long nlines_total) {
+  int cap = kFftMaxTile / n;
+  if (cap < 1) cap = 1;
+  if (cap > 16) cap = 16;
+  if (st == 1) {
+    int t = 1;
+    while (t * 2 <= cap && nlines_total % (t * 2) == 0) t *= 2;
+    return t;
+  }
+  int t = 1;
+  while (t * 2 <= cap && st % (t * 2) == 0) t *= 2;
+  return t;
+}
+
+cudaError_t fft_axis(GaugeFixState* s, int n, long long st, long long total, int inverse, cudaStream_t stream) {
+  const double2* tw = s->twiddles.at(n);
+  const long long nlines = total / n;
+  const int tl = tile_lines_for(n, st, nlines);
+  const long long tiles = nlines / tl;
+  const size_t smem = (size_t)tl * n * sizeof(double2);
+  if (is_pow2(n)) {
+    if (n == 1) return cudaSuccess;
+    cudaFuncSetAttribute(fft_pow2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kFftMaxTile * 16 > smem ? kFftMaxTile * 16 : smem));
+    fft_pow2_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(s->X, n, ilog2(n), st, tl, tw, inverse);
+  } else {
+    cudaFuncSetAttribute(dft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+    dft_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(s->X, n, st, tl, tw, inverse);
+  }
+  return cudaGetLastError();
+}
+
+// 3D transform of the 8 colour planes of X
+cudaError_t fft3d(GaugeFixState* s, int inverse, cudaStream_t stream) {
+  const Geometry& g = s->g;
+  const long long total = 8 * g.vol;
+  cudaError_t e = fft_axis(s, g.nx, 1, total, inverse, stream);
+  if (e == cudaSuccess) e = fft_axis(s, g.ny, g.nx, total, inverse, stream);
+  if (e == cudaSuccess) e = fft_axis(s, g.nz, g.plane, total, inverse, stream);
+  return e;
+}
+
+int prepare(GaugeFixState** ps, const GaugeFixArgs& a, std::string* err) {
+  GaugeFixState* s = *ps;
+  if (s && (s->g.nx != a.g.nx || s->g.ny != a.g.ny || s->g.nz != a.g.nz)) {
+    gaugefix_destroy(s);
+    s = nullptr;
+  }
+  if (!s) {
+    s = new GaugeFixState;
+    s->g = a.g;
+    s->precision = a.precision;
+    *ps = s;
+    cudaError_t e = cudaMalloc(&s->X, sizeof(double2) * 8 * a.g.vol);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      *err = std::string("cudaMalloc FFT array: ") + cudaGetErrorString(e);
+      return GLASMA_ERR_OUT_OF_MEMORY;
+    }
+    const int ns[3] = {a.g.nx, a.g.ny, a.g.nz};
+    for (int n : ns) {
+      if (s->twiddles.count(n)) continue;
+      const int count = is_pow2(n) ? (n / 2 > 0 ? n / 2 : 1) : n;
+      double2* tw = nullptr;
+      e = cudaMalloc(&tw, sizeof(double2) * count);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        *err = "cudaMalloc twiddles";
+        return GLASMA_ERR_OUT_OF_MEMORY;
+      }
+      twiddle_kernel<<<(count + 255) / 256, 256, 0, a.stream>>>(tw, n, count);
+      s->twiddles[n] = tw;
+    }
+  }
+  return GLASMA_OK;
+}
+
+template <typename T>
+int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
+             double* log, int* iterations, std::string* err) {
+  const Geometry& g = a.g;
+  cudaStream_t st = a.stream;
+  const cx<T>* U = static_cast<const cx<T>*>(a.U);
+  const T* E = static_cast<const T*>(a.E);
+  cx<T>* G = static_cast<cx<T>*>(a.G);
+  cx<T>* UG = static_cast<cx<T>*>(a.UG);
+  T* EG = static_cast<T*>(a.EG);
+  auto cuda_err = [&](cudaError_t e, const char* where) {
+    *err = std::string(where) + ": " + cudaGetErrorString(e);
+    return GLASMA_ERR_CUDA;
+  };
+  cudaError_t e;
+  // CopyFields (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:93-97): interior slices only
+  for (int c = 0; c < 27; c++) {
+    e = cudaMemcpyAsync(UG + (long long)c * g.S + g.plane, U + (long long)c * g.S + g.plane, sizeof(cx<T>) * g.vol,
+                        cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_err(e, "copy U");
+  }
+  for (int c = 0; c < 24; c++) {
+    e = cudaMemcpyAsync(EG + (long long)c * g.S + g.plane, E + (long long)c * g.S + g.plane, sizeof(T) * g.vol,
+                        cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_err(e, "copy E");
+  }
+  const unsigned tb = (unsigned)((g.vol + 127) / 128);
+  auto transform_links = [&]() {
+    transform_links_kernel<T><<<tb, 128, 0, st>>>(g, U, G, UG);
+    cudaError_t e2 = cudaGetLastError();
+    if (e2 == cudaSuccess) e2 = launch_sync_ghosts<cx<T>>(g, G, 9, st);
+    return e2;
+  };
+  if ((e = transform_links()) != cudaSuccess) return cuda_err(e, "transform links");
+
+  const double cw[3] = {(a.a_scale / g.a[0]) * (a.a_scale / g.a[0]), (a.a_scale / g.a[1]) * (a.a_scale / g.a[1]),
+                        g.nz > 1 ? (a.a_scale / g.a[2]) * (a.a_scale / g.a[2]) : 0.0};
+  const unsigned nb = blocks_for(g.vol, kGfThreads, kGfBlocks);
+  double* part_dev = a.scratch;                 // nb * 4
+  double* part_upd = a.scratch + (size_t)nb * 4;  // nb * 3
+  double* res = a.scratch + (size_t)nb * 7;     // 8 results
+  double h[8];
+  double gmax = 1.0;
+  int n = 0;
+  int status = GLASMA_OK;
+  const double minf0 = 2.0 * 3 * (1.0 / (g.a[0] * g.a[0]) + 1.0 / (g.a[1] * g.a[1]) + 1.0 / (g.a[2] * g.a[2]));
+  while (n < max_iters && gmax > tol) {
+    deviation_kernel<T><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], s->X, part_dev);
+    red::finish_kernel<4><<<1, red::kThreads, 0, st>>>(part_dev, (int)nb, 1 | (0 << 2) | (2 << 4) | (0 << 6), res);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "deviation");
+    if ((e = fft3d(s, 0, st)) != cudaSuccess) return cuda_err(e, "fft forward");
+    const long long tot = 8 * g.vol;
+    accelerate_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2], s->X,
+                                                                     (flags & GLASMA_GF_PROJECT_ZERO_MODE) ? 1 : 0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
+    if ((e = fft3d(s, 1, st)) != cudaSuccess) return cuda_err(e, "fft backward");
+    update_kernel<T><<<nb, kGfThreads, 0, st>>>(g, s->X, G, alpha, part_upd);
+    red::finish_kernel<3><<<1, red::kThreads, 0, st>>>(part_upd, (int)nb, 1 | (0 << 2) | (0 << 4), res + 4);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "update");
+    if ((e = transform_links()) != cudaSuccess) return cuda_err(e, "transform links");
+    if ((e = cudaMemcpyAsync(h, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+      return cuda_err(e, "monitor copy");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e, "monitor sync");
+    const double V = (double)g.vol;
+    gmax = h[0];
+    if (log) {
+      double* o = log + 7 * (size_t)n;
+      o[0] = n;
+      o[1] = h[0];
+      o[2] = sqrt(h[1] / (8.0 * V));
+      o[3] = h[4];
+      o[4] = sqrt(h[5] / (8.0 * V));
+      o[5] = h[2] < minf0 ? h[2] : minf0;
+      o[6] = h[3] / V;
+    }
+    n++;
+    if (h[6] > 0.0) {
+      *err = "gauge update left SU(3) by more than 1e-13 (the reference exits here)";
+      status = GLASMA_ERR_NUMERICAL;
+      break;
+    }
+  }
+  *iterations = n;
+  if (status != GLASMA_OK) return status;
+  if ((e = transform_links()) != cudaSuccess) return cuda_err(e, "transform links");
+  transform_efield_kernel<T><<<tb, 128, 0, st>>>(g, E, G, EG);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "transform E");
+  if ((e = launch_sync_ghosts<cx<T>>(g, G, 9, st)) != cudaSuccess) return cuda_err(e, "sync G");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e, "final sync");
+  return GLASMA_OK;
+}
+
+}  // namespace
+
+int gaugefix_run(GaugeFixState** state, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
+                 double* log, int* iterations, std::string* err) {
+  *iterations = 0;
+  int st = prepare(state, a, err);
+  if (st != GLASMA_OK) return st;
+  if (a.scratch_doubles < (size_t)kGfBlocks * 7 + 16) {
+    *err = "scratch too small";
+    return GLASMA_ERR_INVALID_ARGUMENT;
+  }
+  return a.precision == GLASMA_FP64 ? run_impl<double>(*state, a, alpha, max_iters, tol, flags, log, iterations, err)
+                                    : run_impl<float>(*state, a, alpha, max_iters, tol, flags, log, iterations, err);
+}
+
+void gaugefix_destroy(GaugeFixState* s) {
+  if (!s) return;
+  if (s->X) cudaFree(s->X);
+  for (auto& kv : s->twiddles) cudaFree(kv.second);
+  delete s;
+}
+
+// Exposed for the FFT test entry point: forward or backward 3D transform of 8 colour planes.
+int gaugefix_fft_test(GaugeFixState** state, const GaugeFixArgs& a, const double2* in, double2* out, int inverse,
+                      std::string* err) {
+  int st = prepare(state, a, err);
+  if (st != GLASMA_OK) return st;
+  const size_t bytes = sizeof(double2) * 8 * a.g.vol;
+  cudaError_t e = cudaMemcpyAsync((*state)->X, in, bytes, cudaMemcpyDefault, a.stream);
+  if (e == cudaSuccess) e = fft3d(*state, inverse, a.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, (*state)->X, bytes, cudaMemcpyDefault, a.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(a.stream);
+  if (e != cudaSuccess) {
+    *err = cudaGetErrorString(e);
+    return GLASMA_ERR_CUDA;
+  }
+  return GLASMA_OK;
+}
 
 }  // namespace glasma

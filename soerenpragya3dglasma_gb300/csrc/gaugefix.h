@@ -28,5 +28,9 @@ struct GaugeFixArgs {
 int gaugefix_run(GaugeFixState** state, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
                  double* log, int* iterations, std::string* err);
 void gaugefix_destroy(GaugeFixState* state);
+// 3D transform (unnormalised, sign -1 forward / +1 inverse) of 8 colour planes X[a][z][y][x];
+// `in` / `out` may be host or device memory.
+int gaugefix_fft_test(GaugeFixState** state, const GaugeFixArgs& a, const double2* in, double2* out, int inverse,
+                      std::string* err);
 
 }  // namespace glasma

@@ -607,6 +607,24 @@ int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double to
   return GLASMA_OK;
 }
 
+int glasma_fft3d(glasma_lattice* h, const double* in, double* out, int inverse) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!in || !out) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null buffer");
+  int st = ensure_scratch(h);
+  if (st) return st;
+  glasma::GaugeFixArgs a = {};
+  a.g = h->g;
+  a.precision = h->precision;
+  a.a_scale = h->a_scale;
+  a.stream = h->stream;
+  a.scratch = h->scratch;
+  a.scratch_doubles = h->scratch_doubles;
+  std::string err;
+  st = glasma::gaugefix_fft_test(&h->gf, a, reinterpret_cast<const double2*>(in), reinterpret_cast<double2*>(out),
+                                 inverse ? 1 : 0, &err);
+  return st == GLASMA_OK ? GLASMA_OK : fail(st, err);
+}
+
 int glasma_synchronize(glasma_lattice* h) {
   GLASMA_CHECK_HANDLE(h);
   GLASMA_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");

@@ -193,5 +193,13 @@ class Lattice:
                                           log.ctypes.data_as(_lib._D), ctypes.byref(n)))
         return log[: n.value]
 
+    def fft3d(self, X, inverse=False):
+        """Batched 3D FFT of 8 colour planes: X complex128 of shape (8, Nz, Ny, Nx)."""
+        X = np.ascontiguousarray(X, dtype=np.complex128)
+        assert X.shape == (8, self.N[2], self.N[1], self.N[0])
+        out = np.empty_like(X)
+        check(self.lib.glasma_fft3d(self.h, X.ctypes.data, out.ctypes.data, int(inverse)))
+        return out
+
     def gauge_reset(self):
         check(self.lib.glasma_gauge_reset(self.h))

@@ -114,7 +114,8 @@ def test_mv_collision_matches_reference_golden(golden_dir):
     N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
     init = {k: g["init_" + k] for k in FIELDS}
     with _gpu(init, N, a) as lat:
-        assert np.allclose(lat.bulk(), g["t0_bulk"], rtol=1e-12, atol=1e-14)
+        # B^2 sums 4*(3 - ReTr P) with P ~ 1: absolute rounding ~ V * 12 * eps
+        assert np.allclose(lat.bulk(), g["t0_bulk"], rtol=1e-12, atol=1e-11)
         assert np.allclose(lat.gauss(), g["t0_gauss"], rtol=1e-10, atol=1e-16)
         lat.step(dt, int(g["cfg_steps"]))
         assert np.allclose(lat.bulk(), g["t8_bulk"], rtol=1e-11, atol=1e-11)

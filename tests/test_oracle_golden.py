@@ -67,7 +67,7 @@ def test_mv_collision_evolution_matches_reference(oracle, golden_dir):
     g = _load(golden_dir, "mv_collision.npz")
     N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
     f = {k: g["init_" + k].copy() for k in FIELDS}
-    assert np.allclose(oracle.bulk(f, N, a), g["t0_bulk"], rtol=1e-12, atol=1e-14)
+    assert np.allclose(oracle.bulk(f, N, a), g["t0_bulk"], rtol=1e-12, atol=1e-11)
     oracle.update(f, N, a, dt, int(g["cfg_steps"]))
     # B^2 sums 4*(3 - Re tr P) over sites with P ~ 1: absolute rounding ~ V * 12 * eps
     assert np.allclose(oracle.bulk(f, N, a), g["t8_bulk"], rtol=1e-11, atol=1e-11)
