@@ -151,7 +151,8 @@ __global__ void __launch_bounds__(kGfThreads) update_kernel(Geometry g, const do
     for (int a = 0; a < 8; a++) upd.a[a] = X[(long long)a * g.vol + idx].x;
     Mat<double> wt, gm, gn;
     expi(-alpha, upd, wt);
-    if (unitarity_norm(wt) > 1e-13) v[2] += 1.0;
+    // the reference's guard (CoulombGaugeDeviation.cpp:57-68); written so that a NaN also trips it
+    if (!(unitarity_norm(wt) <= 1e-13)) v[2] += 1.0;
     const double sr = 3.0 - wt.e[0].re - wt.e[4].re - wt.e[8].re, si = -(wt.e[0].im + wt.e[4].im + wt.e[8].im);
     const double step = sqrt(sr * sr + si * si);
     v[0] = fmax(v[0], step);

@@ -96,10 +96,17 @@ def test_zero_mode_projection_converges():
 
 
 def test_unitarity_guard_returns_status_instead_of_exiting():
+    """A corrupted link (NaN) trips the update guard; the call returns GLASMA_ERR_NUMERICAL where
+    the reference would exit, and the handle stays usable."""
     N = (6, 6, 8)
-    f = O.random_fields(N, 77, link_amp=0.6)
+    f = O.random_fields(N, 77, link_amp=0.2)
+    bad = f["U"].copy()
+    bad[3, 2, 1, 0, 0, 0] = np.nan
     with Lattice(N) as lat:
-        lat.upload("U", f["U"])
+        lat.upload("U", bad)
         with pytest.raises(GlasmaError) as ei:
-            lat.coulomb_fix(40.0, 50)
+            lat.coulomb_fix(0.5, 5)
         assert ei.value.status == 5
+        lat.upload("U", f["U"])
+        lat.gauge_reset()
+        assert len(lat.coulomb_fix(0.5, 2)) == 2
