@@ -285,30 +285,7 @@ def run_ours(args):
         lat.upload_device("UOld", inputs["U"].data_ptr())
         return lat
 
-    # ---- FP64, resident fields
-    lat = make_lattice("fp64")
-    lat.step(DT, args.warmup, save_uold=False)
-    torch.cuda.synchronize()
-    barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        kernel_ms = lat.step_profiled(DT, args.steps, save_uold=False)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    ms_total = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms_step = ms_total / args.steps
-    value = world * vol / (ms_step * 1e-3)
-    e64 = lat.bulk()
-
     peak, peak_kind = hbm_peak()
-    k_ms = {"efield_jstat": kernel_ms[0] / args.steps, "links_j": kernel_ms[1] / args.steps}
-    dom = max(k_ms, key=k_ms.get)
     traffic = ncu_traffic()
 
     def roofline(name, prec, ms):
@@ -319,61 +296,93 @@ def run_ours(args):
                 "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr,
                 "algorithmic_bytes_per_launch": alg, "launch_ms": ms}
 
-    rl = roofline(dom, "fp64", k_ms[dom])
+    def max_over_ranks(x):
+        if world > 1:
+            t = torch.tensor([x], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
 
-    # ---- FP32 on the same inputs
-    lat32 = make_lattice("fp32")
-    lat32.step(DT, args.warmup, save_uold=False)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    kms32 = lat32.step_profiled(DT, args.steps, save_uold=False)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms32 = e0.elapsed_time(e1) / args.steps
-    e32 = lat32.bulk()
-    k32 = {"efield_jstat": kms32[0] / args.steps, "links_j": kms32[1] / args.steps}
-    dom32 = max(k32, key=k32.get)
-    fp32 = {"value": world * vol / (ms32 * 1e-3), "ms_per_step": ms32,
-            "step_hbm_frac": STEP_BYTES["fp32"] * vol / (ms32 * 1e-3) / 1e9 / peak,
-            "energy_rel_err_vs_fp64": abs(e32[9] - e64[9]) / abs(e64[9]),
-            "steps_compared": args.warmup + args.steps,
-            "roofline": roofline(dom32, "fp32", k32[dom32])}
-    del lat32
+    def timed_run(precision, sampler=None):
+        lat = make_lattice(precision)
+        lat.step(DT, args.warmup, save_uold=False)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if sampler is not None:
+            sampler.__enter__()
+        e0.record(stream)
+        kms = lat.step_profiled(DT, args.steps, save_uold=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if sampler is not None:
+            sampler.__exit__(None, None, None)
+        barrier()
+        ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
+        kern = {"efield_jstat": kms[0] / args.steps, "links_j": kms[1] / args.steps}
+        return lat, ms, kern
 
-    # ---- e2e through the C ABI with pinned host buffers
-    host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in inputs.items()}
-    for k in host:
-        host[k].copy_(inputs[k])
-    e2e_steps = max(1, min(args.steps, 5))
-    h2d = sum(host[k].numel() * host[k].element_size() for k in INPUT_FIELDS)
-    lat.upload("U", host["U"])
-    torch.cuda.synchronize()
-    barrier()
-    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a0.record(stream)
-    for _ in range(e2e_steps):
-        for k in INPUT_FIELDS:
-            lat.upload(k, host[k])
-        lat.step(DT, 1, save_uold=False)
-        lat.bulk()  # device -> host read of the step's energy (7 doubles), synchronises
-    a1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = a0.elapsed_time(a1) / e2e_steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    run64 = args.only in ("both", "fp64")
+    run32 = args.only in ("both", "fp32")
+    clk = ClockSampler(local)
+    lat = None
+    value = ms_step = rl = k_ms = e64 = None
+    if run64:
+        # ---- FP64, resident fields (the headline)
+        lat, ms_step, k_ms = timed_run("fp64", clk)
+        value = world * vol / (ms_step * 1e-3)
+        e64 = lat.bulk()
+        dom = max(k_ms, key=k_ms.get)
+        rl = roofline(dom, "fp64", k_ms[dom])
+
+    fp32 = None
+    if run32:
+        # ---- FP32 on the same inputs
+        lat32, ms32, k32 = timed_run("fp32", None if run64 else clk)
+        e32 = lat32.bulk()
+        dom32 = max(k32, key=k32.get)
+        fp32 = {"value": world * vol / (ms32 * 1e-3), "ms_per_step": ms32,
+                "step_hbm_frac": STEP_BYTES["fp32"] * vol / (ms32 * 1e-3) / 1e9 / peak,
+                "energy_rel_err_vs_fp64": (abs(e32[9] - e64[9]) / abs(e64[9])) if e64 is not None else None,
+                "steps_compared": args.warmup + args.steps,
+                "kernel_ms": k32,
+                "roofline": roofline(dom32, "fp32", k32[dom32])}
+        del lat32
+
+    e2e = None
+    if lat is not None and not args.no_e2e:
+        # ---- e2e through the C ABI with pinned host buffers
+        host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in inputs.items()}
+        for k in host:
+            host[k].copy_(inputs[k])
+        e2e_steps = max(1, min(args.steps, 5))
+        h2d = sum(host[k].numel() * host[k].element_size() for k in INPUT_FIELDS)
+        lat.upload("U", host["U"])
+        torch.cuda.synchronize()
+        barrier()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(e2e_steps):
+            for k in INPUT_FIELDS:
+                lat.upload(k, host[k])
+            lat.step(DT, 1, save_uold=False)
+            lat.bulk()  # device -> host read of the step's energy (7 doubles); synchronises
+        a1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = max_over_ranks(a0.elapsed_time(a1)) / e2e_steps
+        e2e = {"value": world * vol / (e2e_ms * 1e-3), "unit": "site-updates/s", "ms_per_step": e2e_ms,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 7 * 8, "steps": e2e_steps,
+               "per_step": "upload U,E,Jp,Jm,JpStat,JmStat from pinned host (reference layout) + 1 step + bulk read"}
 
     # ---- CPU baseline (rank 0 at N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        nz_slab = 64
+        nz_slab = min(64, N[2])
         hs = host_slab(inputs, nz_slab)
         rate, n, secs, threads = time_oracle(hs, (N[0], N[1], nz_slab), os.cpu_count(), 10.0, 50)
         cpu = {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
-               "sample": "%d leapfrog steps of a 128x128x%d slab of the workload in %.1f s, oracle "
-                         "restatement, %d threads" % (n, nz_slab, secs, threads)}
+               "sample": "%d leapfrog steps of a %dx%dx%d slab of the workload in %.1f s, oracle "
+                         "restatement, %d threads" % (n, N[0], N[1], nz_slab, secs, threads)}
     del lat
     if world > 1:
         dist.destroy_process_group()
@@ -392,15 +401,14 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded SU(3) links exp(i 0.3 t.r), E ~ N(0,0.01), J ~ N(0,4e-4); workload shapes)",
-        "config": {"workload": "glasma leapfrog 128x128x512 FP64 (plain method, production size)",
+        "config": {"workload": "glasma leapfrog %dx%dx%d FP64 (plain method, production size)" % N,
                    "lattice": list(N), "dt": DT, "a": list(A_WORK), "parallelism": "replicas" if world > 1 else "1 GPU",
                    "l2": "inputs larger than L2 (%.1f GB of FP64 state)" % (STEP_BYTES["fp64"] / 2 * vol / 1e9)},
-        "step_hbm_frac": STEP_BYTES["fp64"] * vol / (ms_step * 1e-3) / 1e9 / peak,
+        "step_hbm_frac": (STEP_BYTES["fp64"] * vol / (ms_step * 1e-3) / 1e9 / peak) if ms_step else None,
         "roofline": rl,
         "kernel_ms": k_ms,
         "fp32": fp32,
-        "e2e": {"value": world * vol / (e2e_ms * 1e-3), "unit": "site-updates/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 7 * 8, "steps": e2e_steps},
+        "e2e": e2e,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": 2 * args.steps,
@@ -415,9 +423,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--only", default="both", choices=["both", "fp64", "fp32"],
+                    help="which precisions to run (profiling runs); the JSON line needs both")
+    ap.add_argument("--lattice", default=None, help="Nx,Ny,Nz instead of the workload's (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.lattice:
+        global N_WORK
+        N_WORK = tuple(int(v) for v in args.lattice.split(","))
     if args.impl == "reference":
         run_reference(args)
     else:
