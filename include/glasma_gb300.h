@@ -150,6 +150,24 @@ int glasma_gauge_reset(glasma_lattice* h);
  * pointers. */
 int glasma_fft3d(glasma_lattice* h, const double* in, double* out, int inverse);
 
+/* Gauss-law violation with no device allocation.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc -- code running while another framework captures a
+ * CUDA graph on the stream, memory owned by a pool or arena that forbids outside allocations,
+ * real-time loops that must not allocate or synchronise -- and that already hold the fields in
+ * device memory.  Same result as glasma_gauss (sync_first = 0) without a lattice handle.
+ * Inputs: FP64 device buffers in the library's device layout (S = nx*ny*(nz+2) sites, site
+ * s = x + nx*(y + ny*(z+1)), ghost slices included): U[(mu*9 + k)*S + s] complex (k = i + 3*j),
+ * E[(mu*8 + a)*S + s], JpStat[a*S + s], JmStat[a*S + s].  Output: result (device, 2 doubles) =
+ * {max |G^a|, sqrt(sum G^2 / (8 V))}; zprofile (device, nz doubles, may be NULL).  Work is issued
+ * on `stream` (a cudaStream_t, NULL = default stream); the caller synchronises.
+ * Scratch is one fixed 512 KiB __device__ array per device, held until the process exits, which
+ * limits nz to 992 (larger nz returns GLASMA_ERR_BAD_SHAPE).  The first call on a device looks up
+ * that array's address; make it before any stream capture.  All calls on a device share the
+ * array: calls that overlap on the GPU race and must be ordered by the caller. */
+int glasma_gauss_noalloc(const double* U, const double* E, const double* JpStat, const double* JmStat, int nx, int ny,
+                         int nz, double ax, double ay, double az, double a_scale, double* result, double* zprofile,
+                         void* stream);
+
 /* Wait for the handle's stream. */
 int glasma_synchronize(glasma_lattice* h);
 const char* glasma_status_string(int status);

@@ -50,6 +50,8 @@ SIGNATURES = [
     ("glasma_coulomb_fix", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
     ("glasma_gauge_reset", ctypes.c_int, [_H]),
     ("glasma_fft3d", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    ("glasma_gauss_noalloc", ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("glasma_synchronize", ctypes.c_int, [_H]),
     ("glasma_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("glasma_last_error", ctypes.c_char_p, []),
