@@ -34,8 +34,21 @@ def _deps():
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
+STAMP = LIB + ".flags"
+
+
+def _extra_flags():
+    """Extra nvcc flags for tuning sweeps, e.g. GLASMA_NVCC_EXTRA="-DGLASMA_FP32_MIN_BLOCKS=4"."""
+    return os.environ.get("GLASMA_NVCC_EXTRA", "").split()
+
+
 def needs_build():
     if not os.path.exists(LIB):
+        return True
+    try:
+        if open(STAMP).read() != " ".join(_extra_flags()):
+            return True
+    except OSError:
         return True
     t = os.path.getmtime(LIB)
     return any(os.path.getmtime(d) > t for d in _deps())
@@ -47,7 +60,7 @@ def build(force=False, verbose=False, ptxas_verbose=False):
     nvcc = _nvcc()
     objdir = os.path.join(os.path.dirname(HERE), "_build", "obj")
     os.makedirs(objdir, exist_ok=True)
-    extra = ["-Xptxas", "-v"] if ptxas_verbose else []
+    extra = (["-Xptxas", "-v"] if ptxas_verbose else []) + _extra_flags()
 
     def compile_one(src):
         obj = os.path.join(objdir, os.path.basename(src) + ".o")
@@ -67,6 +80,8 @@ def build(force=False, verbose=False, ptxas_verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr[-4000:])
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(" ".join(_extra_flags()))
     return LIB
 
 

@@ -42,30 +42,34 @@ __device__ __forceinline__ long long site_index(const Geometry& g, int x, int y,
   return (long long)x + (long long)g.nx * ((long long)y + (long long)g.ny * (long long)(z + 1));
 }
 
-template <typename T>
-__device__ __forceinline__ void load_link(const cx<T>* __restrict__ U, long long S, int mu, long long s, Mat<T>& m) {
-  const cx<T>* p = U + (long long)(mu * 9) * S + s;
+// Component offsets are computed in the index type I: 32-bit when 27*S < 2^31 (every lattice up to
+// 256x256x1200), 64-bit otherwise; fewer registers and integer instructions in the 32-bit case.
+template <typename T, typename I>
+__device__ __forceinline__ void load_link(const cx<T>* __restrict__ U, I S, int mu, I s, Mat<T>& m) {
+  const cx<T>* p = U + ((I)(mu * 9) * S + s);
 #pragma unroll
-  for (int k = 0; k < 9; k++) m.e[k] = p[(long long)k * S];
+  for (int k = 0; k < 9; k++) m.e[k] = p[(I)k * S];
 }
-template <typename T>
-__device__ __forceinline__ void store_link(cx<T>* __restrict__ U, long long S, int mu, long long s, const Mat<T>& m) {
-  cx<T>* p = U + (long long)(mu * 9) * S + s;
+template <typename T, typename I>
+__device__ __forceinline__ void store_link(cx<T>* __restrict__ U, I S, int mu, I s, const Mat<T>& m) {
+  cx<T>* p = U + ((I)(mu * 9) * S + s);
 #pragma unroll
-  for (int k = 0; k < 9; k++) p[(long long)k * S] = m.e[k];
+  for (int k = 0; k < 9; k++) p[(I)k * S] = m.e[k];
 }
-template <typename T>
-__device__ __forceinline__ void load_alg(const T* __restrict__ F, long long S, long long base, long long s, Alg<T>& v) {
-  const T* p = F + base * S + s;
+template <typename T, typename I>
+__device__ __forceinline__ void load_alg(const T* __restrict__ F, I S, int base, I s, Alg<T>& v) {
+  const T* p = F + ((I)base * S + s);
 #pragma unroll
-  for (int a = 0; a < 8; a++) v.a[a] = p[(long long)a * S];
+  for (int a = 0; a < 8; a++) v.a[a] = p[(I)a * S];
 }
-template <typename T>
-__device__ __forceinline__ void store_alg(T* __restrict__ F, long long S, long long base, long long s, const Alg<T>& v) {
-  T* p = F + base * S + s;
+template <typename T, typename I>
+__device__ __forceinline__ void store_alg(T* __restrict__ F, I S, int base, I s, const Alg<T>& v) {
+  T* p = F + ((I)base * S + s);
 #pragma unroll
-  for (int a = 0; a < 8; a++) p[(long long)a * S] = v.a[a];
+  for (int a = 0; a < 8; a++) p[(I)a * S] = v.a[a];
 }
+
+inline bool use_32bit_index(const Geometry& g) { return g.S * 27 < (1LL << 31) - 1; }
 
 // ---- launch API shared between translation units (host side) ------------------
 // All launches go to `stream`.  Return cudaGetLastError() of the launch.

@@ -25,25 +25,45 @@ namespace {
 
 constexpr int kThreads = 128;
 
-__device__ __forceinline__ long long nb(const Geometry& g, int x, int y, int z, int dx, int dy, int dz) {
+// Blocks per SM the register allocation must leave room for (the register cap is 64K / (128 * n)),
+// chosen by measurement on GB300; overridable at build time for tuning sweeps.
+#ifndef GLASMA_FP64_MIN_BLOCKS
+#define GLASMA_FP64_MIN_BLOCKS 2
+#endif
+#ifndef GLASMA_FP32_MIN_BLOCKS
+#define GLASMA_FP32_MIN_BLOCKS 3
+#endif
+template <typename T>
+struct Occupancy;
+template <>
+struct Occupancy<double> {
+  static constexpr int kMinBlocks = GLASMA_FP64_MIN_BLOCKS;
+};
+template <>
+struct Occupancy<float> {
+  static constexpr int kMinBlocks = GLASMA_FP32_MIN_BLOCKS;
+};
+
+template <typename I>
+__device__ __forceinline__ I nb(const Geometry& g, int x, int y, int z, int dx, int dy, int dz) {
   int xx = x + dx, yy = y + dy;
   xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
   yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
-  return site_index(g, xx, yy, z + dz);
+  return (I)xx + (I)g.nx * ((I)yy + (I)g.ny * (I)(z + dz + 1));
 }
 
-__device__ __forceinline__ void decode(const Geometry& g, long long idx, int& x, int& y, int& z) {
-  const long long r = idx / g.nx;
-  x = (int)(idx - r * g.nx);
-  z = (int)(r / g.ny);
-  y = (int)(r - (long long)z * g.ny);
+template <typename I>
+__device__ __forceinline__ void decode(const Geometry& g, I idx, int& x, int& y, int& z) {
+  const I r = idx / (I)g.nx;
+  x = (int)(idx - r * (I)g.nx);
+  z = (int)(r / (I)g.ny);
+  y = (int)(r - (I)z * (I)g.ny);
 }
 
 // Staples of link mu at x in the (mu,nu) plane, weighted by c, added to acc.
-template <typename T>
-__device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, long long S, int mu, int nu, long long s,
-                                            long long s_pmu, long long s_pnu, long long s_pmu_mnu, long long s_mnu, T c,
-                                            Mat<T>& acc) {
+template <typename T, typename I>
+__device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, I S, int mu, int nu, I s, I s_pmu, I s_pnu,
+                                            I s_pmu_mnu, I s_mnu, T c, Mat<T>& acc) {
   Mat<T> a, b, t;
   load_link(U, S, nu, s_pmu, a);
   load_link(U, S, mu, s_pnu, b);
@@ -66,33 +86,34 @@ struct EParams {
   int do_e, do_jstat;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) efield_jstat_kernel(Geometry g, FieldPtrs<T> f, EParams<T> p) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.vol) return;
+template <typename T, typename I>
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
+    efield_jstat_kernel(Geometry g, FieldPtrs<T> f, EParams<T> p) {
+  const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+  if (idx >= (I)g.vol) return;
   int x, y, z;
-  decode(g, idx, x, y, z);
-  const long long S = g.S;
-  const long long s = idx + g.plane;
+  decode<I>(g, idx, x, y, z);
+  const I S = (I)g.S, plane = (I)g.plane;
+  const I s = idx + plane;
   const bool lo = (z == 0), hi = (z == g.nz - 1);
-  const long long sg = lo ? s - g.plane : (hi ? s + g.plane : -1);
+  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
   if (p.do_e) {
-    const long long sxp = nb(g, x, y, z, 1, 0, 0), sxm = nb(g, x, y, z, -1, 0, 0);
-    const long long syp = nb(g, x, y, z, 0, 1, 0), sym = nb(g, x, y, z, 0, -1, 0);
-    const long long szp = s + g.plane, szm = s - g.plane;
+    const I sxp = nb<I>(g, x, y, z, 1, 0, 0), sxm = nb<I>(g, x, y, z, -1, 0, 0);
+    const I syp = nb<I>(g, x, y, z, 0, 1, 0), sym = nb<I>(g, x, y, z, 0, -1, 0);
+    const I szp = s + plane, szm = s - plane;
 #pragma unroll 1
     for (int mu = 0; mu < 3; mu++) {
       Mat<T> acc;
       set_zero(acc);
       if (mu == 0) {
-        add_staples(f.U, S, 0, 1, s, sxp, syp, nb(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc);
-        add_staples(f.U, S, 0, 2, s, sxp, szp, nb(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc);
+        add_staples(f.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc);
+        add_staples(f.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc);
       } else if (mu == 1) {
-        add_staples(f.U, S, 1, 0, s, syp, sxp, nb(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc);
-        add_staples(f.U, S, 1, 2, s, syp, szp, nb(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc);
+        add_staples(f.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc);
+        add_staples(f.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc);
       } else {
-        add_staples(f.U, S, 2, 0, s, szp, sxp, nb(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc);
-        add_staples(f.U, S, 2, 1, s, szp, syp, nb(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc);
+        add_staples(f.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc);
+        add_staples(f.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc);
       }
       Mat<T> u, P;
       load_link(f.U, S, mu, s, u);
@@ -114,7 +135,7 @@ __global__ void __launch_bounds__(kThreads) efield_jstat_kernel(Geometry g, Fiel
     }
   }
   if (p.do_jstat) {
-    const long long szm = s - g.plane;
+    const I szm = s - plane;
     Mat<T> uzm;
     load_link(f.U, S, 2, szm, uzm);
     Alg<T> down, jc, st;
@@ -144,15 +165,16 @@ struct LParams {
   int save_uold, do_j, do_second;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) links_j_kernel(Geometry g, FieldPtrs<T> f, LParams<T> p) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.vol) return;
-  const long long S = g.S;
-  const long long s = idx + g.plane;
-  const int z = (int)(idx / g.plane);
+template <typename T, typename I>
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
+    links_j_kernel(Geometry g, FieldPtrs<T> f, LParams<T> p) {
+  const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+  if (idx >= (I)g.vol) return;
+  const I S = (I)g.S, plane = (I)g.plane;
+  const I s = idx + plane;
+  const int z = (int)(idx / plane);
   const bool lo = (z == 0), hi = (z == g.nz - 1);
-  const long long sg = lo ? s - g.plane : (hi ? s + g.plane : -1);
+  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
 #pragma unroll 1
   for (int mu = 0; mu < 3; mu++) {
     Alg<T> e;
@@ -167,7 +189,7 @@ __global__ void __launch_bounds__(kThreads) links_j_kernel(Geometry g, FieldPtrs
     }
     if (mu == 2 && p.do_j) {
       Alg<T> up, st, j;
-      const long long szp = s + g.plane;
+      const I szp = s + plane;
       load_alg(f.JpStat, S, 0, szp, st);
       adj_mul(uh, st, up);
       load_alg(f.JpStat, S, 0, s, st);
@@ -196,18 +218,18 @@ __global__ void __launch_bounds__(kThreads) links_j_kernel(Geometry g, FieldPtrs
 }
 
 // UpdateJ alone (S/DYNAMICS/SUNcDynamics.cpp:238-269) with the links as they stand.
-template <typename T>
+template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads) j_only_kernel(Geometry g, FieldPtrs<T> f, T cj) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.vol) return;
-  const long long S = g.S;
-  const long long s = idx + g.plane;
-  const int z = (int)(idx / g.plane);
-  const long long sg = (z == 0) ? s - g.plane : (z == g.nz - 1 ? s + g.plane : -1);
+  const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+  if (idx >= (I)g.vol) return;
+  const I S = (I)g.S, plane = (I)g.plane;
+  const I s = idx + plane;
+  const int z = (int)(idx / plane);
+  const I sg = (z == 0) ? s - plane : (z == g.nz - 1 ? s + plane : (I)-1);
   Mat<T> uz;
   load_link(f.U, S, 2, s, uz);
   Alg<T> up, st, j;
-  load_alg(f.JpStat, S, 0, s + g.plane, st);
+  load_alg(f.JpStat, S, 0, s + plane, st);
   adj_mul(uz, st, up);
   load_alg(f.JpStat, S, 0, s, st);
   load_alg(f.Jp, S, 0, s, j);
@@ -215,7 +237,7 @@ __global__ void __launch_bounds__(kThreads) j_only_kernel(Geometry g, FieldPtrs<
   for (int a = 0; a < 8; a++) j.a[a] += -cj * (up.a[a] - st.a[a]);
   store_alg(f.Jp, S, 0, s, j);
   if (sg >= 0) store_alg(f.Jp, S, 0, sg, j);
-  load_alg(f.JmStat, S, 0, s + g.plane, st);
+  load_alg(f.JmStat, S, 0, s + plane, st);
   adj_mul(uz, st, up);
   load_alg(f.JmStat, S, 0, s, st);
   load_alg(f.Jm, S, 0, s, j);
@@ -244,9 +266,9 @@ __global__ void reunitarize_kernel(Geometry g, cx<T>* U) {
   const int mu = (int)(i / g.S);
   const long long s = i - (long long)mu * g.S;
   Mat<T> u;
-  load_link(U, g.S, mu, s, u);
+  load_link<T, long long>(U, g.S, mu, s, u);
   reunitarize(u);
-  store_link(U, g.S, mu, s, u);
+  store_link<T, long long>(U, g.S, mu, s, u);
 }
 
 template <typename E>
@@ -256,6 +278,15 @@ __global__ void copy_kernel(const E* __restrict__ src, E* __restrict__ dst, long
 }
 
 inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+template <typename T>
+cudaError_t launch_efield_kernel(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, cudaStream_t stream) {
+  if (use_32bit_index(g))
+    efield_jstat_kernel<T, int><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+  else
+    efield_jstat_kernel<T, long long><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+  return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -273,8 +304,7 @@ cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, cu
   p.cj = (T)(dt / g.a[2]);
   p.do_e = 1;
   p.do_jstat = 1;
-  efield_jstat_kernel<T><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
-  return cudaGetLastError();
+  return launch_efield_kernel<T>(g, f, p, stream);
 }
 
 template <typename T>
@@ -291,8 +321,7 @@ cudaError_t launch_efield_only(const Geometry& g, FieldPtrs<T> f, double dt, cud
   p.cj = (T)(dt / g.a[2]);
   p.do_e = 1;
   p.do_jstat = 0;
-  efield_jstat_kernel<T><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
-  return cudaGetLastError();
+  return launch_efield_kernel<T>(g, f, p, stream);
 }
 
 template <typename T>
@@ -301,8 +330,7 @@ cudaError_t launch_jstat_only(const Geometry& g, FieldPtrs<T> f, double dt, cuda
   p.cj = (T)(dt / g.a[2]);
   p.do_e = 0;
   p.do_jstat = 1;
-  efield_jstat_kernel<T><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
-  return cudaGetLastError();
+  return launch_efield_kernel<T>(g, f, p, stream);
 }
 
 template <typename T>
@@ -315,7 +343,10 @@ cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool sa
   p.save_uold = save_uold ? 1 : 0;
   p.do_j = do_j ? 1 : 0;
   p.do_second = do_second ? 1 : 0;
-  links_j_kernel<T><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+  if (use_32bit_index(g))
+    links_j_kernel<T, int><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+  else
+    links_j_kernel<T, long long><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
   return cudaGetLastError();
 }
 
@@ -327,7 +358,10 @@ cudaError_t launch_links_only(const Geometry& g, FieldPtrs<T> f, double dt, cuda
 
 template <typename T>
 cudaError_t launch_j_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream) {
-  j_only_kernel<T><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, (T)(dt / g.a[2]));
+  if (use_32bit_index(g))
+    j_only_kernel<T, int><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, (T)(dt / g.a[2]));
+  else
+    j_only_kernel<T, long long><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, (T)(dt / g.a[2]));
   return cudaGetLastError();
 }
 

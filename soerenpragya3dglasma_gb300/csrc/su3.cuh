@@ -344,46 +344,77 @@ __device__ __forceinline__ T unitarity_norm(const Mat<T>& V) {
   return sqrt(n);
 }
 
-// Project onto SU(3): Gram-Schmidt on the first two rows, third row = conj(row0 x row1).
+// Project onto SU(3) without rotating it: two Newton steps U <- (U + U^{-dagger})/2 towards the
+// unitary polar factor (the unitary matrix closest in Frobenius norm), then the phase of the
+// determinant is divided out, det^(-1/3).  FP64 arithmetic for either storage type.  (A Gram-Schmidt
+// projection would turn the accumulated non-unitary part into a small rotation of the link, which
+// shows up as a systematic shift of the plaquette energy.)
 template <typename T>
 __device__ __forceinline__ void reunitarize(Mat<T>& V) {
-  // row r element j is e[r + 3*j]
-  T n0 = 0;
+  Mat<double> U;
 #pragma unroll
-  for (int j = 0; j < 3; j++) n0 += V.e[3 * j].re * V.e[3 * j].re + V.e[3 * j].im * V.e[3 * j].im;
-  const T i0 = T(1) / sqrt(n0);
+  for (int k = 0; k < 9; k++) U.e[k] = mk<double>((double)V.e[k].re, (double)V.e[k].im);
+#pragma unroll 1
+  for (int it = 0; it < 2; it++) {
+    Mat<double> C;  // signed cofactors C(i,j)
 #pragma unroll
-  for (int j = 0; j < 3; j++) {
-    V.e[3 * j].re *= i0;
-    V.e[3 * j].im *= i0;
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        cx<double> c = mk<double>(0, 0);
+        cfma(c, U.e[i1 + 3 * j1], U.e[i2 + 3 * j2]);
+        const cx<double> m = mk<double>(-U.e[i1 + 3 * j2].re, -U.e[i1 + 3 * j2].im);
+        cfma(c, m, U.e[i2 + 3 * j1]);
+        C.e[i + 3 * j] = c;
+      }
+    cx<double> det = mk<double>(0, 0);
+#pragma unroll
+    for (int j = 0; j < 3; j++) cfma(det, U.e[3 * j], C.e[3 * j]);
+    // U^{-dagger}(i,j) = conj(C(i,j)) / conj(det) = conj(C(i,j)) * det / |det|^2
+    const double n2 = det.re * det.re + det.im * det.im;
+    const cx<double> f = mk<double>(det.re / n2, det.im / n2);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      cx<double> w = mk<double>(0, 0);
+      cfma(w, mk<double>(C.e[k].re, -C.e[k].im), f);
+      U.e[k].re = 0.5 * (U.e[k].re + w.re);
+      U.e[k].im = 0.5 * (U.e[k].im + w.im);
+    }
   }
-  cx<T> p = mk<T>(0, 0);  // <row0, row1> = sum conj(r0) r1
-#pragma unroll
-  for (int j = 0; j < 3; j++) cfma_cn(p, V.e[3 * j], V.e[1 + 3 * j]);
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    // r1 -= p r0
-    const cx<T> r0 = V.e[3 * j];
-    V.e[1 + 3 * j].re -= p.re * r0.re - p.im * r0.im;
-    V.e[1 + 3 * j].im -= p.re * r0.im + p.im * r0.re;
+  // remove the determinant's phase
+  cx<double> det = mk<double>(0, 0);
+  {
+    const cx<double> c0 = [&] {
+      cx<double> c = mk<double>(0, 0);
+      cfma(c, U.e[4], U.e[8]);
+      cfma(c, mk<double>(-U.e[7].re, -U.e[7].im), U.e[5]);
+      return c;
+    }();
+    const cx<double> c1 = [&] {
+      cx<double> c = mk<double>(0, 0);
+      cfma(c, U.e[5], U.e[6]);
+      cfma(c, mk<double>(-U.e[8].re, -U.e[8].im), U.e[3]);
+      return c;
+    }();
+    const cx<double> c2 = [&] {
+      cx<double> c = mk<double>(0, 0);
+      cfma(c, U.e[3], U.e[7]);
+      cfma(c, mk<double>(-U.e[6].re, -U.e[6].im), U.e[4]);
+      return c;
+    }();
+    cfma(det, U.e[0], c0);
+    cfma(det, U.e[1], c1);
+    cfma(det, U.e[2], c2);
   }
-  T n1 = 0;
+  double sp, cp;
+  sincos(-atan2(det.im, det.re) / 3.0, &sp, &cp);
+  const cx<double> ph = mk<double>(cp, sp);
 #pragma unroll
-  for (int j = 0; j < 3; j++) n1 += V.e[1 + 3 * j].re * V.e[1 + 3 * j].re + V.e[1 + 3 * j].im * V.e[1 + 3 * j].im;
-  const T i1 = T(1) / sqrt(n1);
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    V.e[1 + 3 * j].re *= i1;
-    V.e[1 + 3 * j].im *= i1;
-  }
-  // r2_j = conj(r0_k r1_l - r0_l r1_k), (j,k,l) cyclic
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    const int k = (j + 1) % 3, l = (j + 2) % 3;
-    const cx<T> a = V.e[3 * k], b = V.e[1 + 3 * l], c = V.e[3 * l], d = V.e[1 + 3 * k];
-    const T re = (a.re * b.re - a.im * b.im) - (c.re * d.re - c.im * d.im);
-    const T im = (a.re * b.im + a.im * b.re) - (c.re * d.im + c.im * d.re);
-    V.e[2 + 3 * j] = mk<T>(re, -im);
+  for (int k = 0; k < 9; k++) {
+    cx<double> w = mk<double>(0, 0);
+    cfma(w, U.e[k], ph);
+    V.e[k] = mk<T>((T)w.re, (T)w.im);
   }
 }
 
