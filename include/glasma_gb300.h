@@ -125,6 +125,10 @@ int glasma_unitarity(glasma_lattice* h, double* max_violation, double* avg_viola
 /* Observables::EnergyMomentumTensor::CreateMap (S/OBSERVABLES/EnergyMomentumTensor.cpp:92-170):
  * out[z*10 + k], k = T00, TXX, TYY, TZZ, T0X, T0Y, T0Z, TXY, TYZ, TZX (transverse averages). */
 int glasma_emt_map(glasma_lattice* h, double* out);
+/* Pressure anisotropy of the slices z in [z_begin, z_end): P_L = mean TZZ, P_T = mean (TXX+TYY)/2
+ * from the CreateMap columns (S/OBSERVABLES/EnergyMomentumTensor.cpp:140-142), ratio = P_L / P_T.
+ * No reference function computes it; it is the late-time objective of the adjoint configuration. */
+int glasma_pressure_anisotropy(glasma_lattice* h, int z_begin, int z_end, double* ratio, double* p_l, double* p_t);
 
 /* Project every link onto SU(3) (Gram-Schmidt on two rows, third row from their cross product). */
 int glasma_reunitarize(glasma_lattice* h);
@@ -142,6 +146,17 @@ int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double to
                        int* iterations);
 /* GaugeTransformation::SetIdentity (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:41-60). */
 int glasma_gauge_reset(glasma_lattice* h);
+
+/* Seeded synthetic fields generated on the device (benchmarks, demos): links exp(i link_amp t.r),
+ * E = e_amp r, the four currents j_amp r, r ~ N(0,1) from a counter-based generator (SplitMix64 +
+ * Box-Muller), ghost slices synced.  Same seed, same fields.  No reference counterpart. */
+int glasma_fill_synthetic(glasma_lattice* h, unsigned long long seed, double link_amp, double e_amp, double j_amp);
+
+/* Autotuner: times the electric-field kernel (computing, storing nothing) for each block tile
+ * shape tile_x x (128/tile_x) sites of a z slice and keeps the fastest for this lattice;
+ * *tile_x (may be NULL) receives it.  glasma_set_tile sets it by hand (tile_x divides 128). */
+int glasma_autotune(glasma_lattice* h, double dt, int* tile_x);
+int glasma_set_tile(glasma_lattice* h, int tile_x);
 
 /* The batched 3D FFT used by the gauge fixer, exposed for testing: 8 colour planes of complex
  * doubles, X[a][z][y][x] (8*Nx*Ny*Nz complex values, interleaved re/im), unnormalised,
@@ -167,6 +182,27 @@ int glasma_fft3d(glasma_lattice* h, const double* in, double* out, int inverse);
 int glasma_gauss_noalloc(const double* U, const double* E, const double* JpStat, const double* JmStat, int nx, int ny,
                          int nz, double ax, double ay, double az, double a_scale, double* result, double* zprofile,
                          void* stream);
+
+/* ---- Batches of independent events (lattices of uneven sizes) advanced together.
+ * No reference counterpart: the reference runs one event per process (seeds are farmed out as
+ * separate jobs).  Each event is an ordinary lattice handle (glasma_batch_event gives it, for
+ * uploads, downloads and observables); a batch step is one persistent launch per leapfrog kernel
+ * over all events' tiles, bit-identical to stepping each event alone.  use_graph != 0 replays
+ * blocks of steps (reunitarize_every steps, or 16) from a CUDA graph captured on first use.
+ * extents / spacings: 3 values per event. */
+typedef struct glasma_batch glasma_batch;
+int glasma_batch_create(int n_events, const int* extents, const double* spacings, int precision, int reunitarize_every,
+                        glasma_batch** out);
+int glasma_batch_destroy(glasma_batch* b);
+int glasma_batch_set_stream(glasma_batch* b, void* cuda_stream);
+int glasma_batch_event(glasma_batch* b, int event, glasma_lattice** out);
+/* Autotunes the electric-field tile once per distinct lattice shape; tiles (may be NULL): n_events ints. */
+int glasma_batch_autotune(glasma_batch* b, double dt, int* tiles);
+int glasma_batch_step(glasma_batch* b, double dt, int nsteps, int use_graph);
+/* Per-event T00 (volume sum, FP64 reductions), n_events doubles. */
+int glasma_batch_energy(glasma_batch* b, double* t00);
+int glasma_batch_synchronize(glasma_batch* b);
+const char* glasma_batch_last_error(void);
 
 /* Wait for the handle's stream. */
 int glasma_synchronize(glasma_lattice* h);

@@ -9,6 +9,7 @@ fixing as hand-written sm_103a kernels behind a C ABI (include/glasma_gb300.h).
 Observables::Bulk, ...) over the same handle.
 """
 from ._lib import GlasmaError, load  # noqa: F401
+from .batch import Batch  # noqa: F401
 from .lattice import DYNAMICAL_FIELDS, Lattice, empty_field, field_shape  # noqa: F401
 
-__all__ = ["Lattice", "GlasmaError", "load", "field_shape", "empty_field", "DYNAMICAL_FIELDS"]
+__all__ = ["Lattice", "Batch", "GlasmaError", "load", "field_shape", "empty_field", "DYNAMICAL_FIELDS"]

@@ -46,12 +46,27 @@ SIGNATURES = [
     ("glasma_gauss", ctypes.c_int, [_H, ctypes.c_int, _D, _D, _D]),
     ("glasma_unitarity", ctypes.c_int, [_H, _D, _D]),
     ("glasma_emt_map", ctypes.c_int, [_H, _D]),
+    ("glasma_pressure_anisotropy", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _D, _D, _D]),
     ("glasma_reunitarize", ctypes.c_int, [_H]),
     ("glasma_coulomb_fix", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
     ("glasma_gauge_reset", ctypes.c_int, [_H]),
+    ("glasma_fill_synthetic", ctypes.c_int, [_H, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_double]),
+    ("glasma_autotune", ctypes.c_int, [_H, ctypes.c_double, _I]),
+    ("glasma_set_tile", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_fft3d", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("glasma_gauss_noalloc", ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("glasma_batch_create", ctypes.c_int, [ctypes.c_int, _I, _D, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    ("glasma_batch_destroy", ctypes.c_int, [_H]),
+    ("glasma_batch_set_stream", ctypes.c_int, [_H, ctypes.c_void_p]),
+    ("glasma_batch_event", ctypes.c_int, [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    ("glasma_batch_autotune", ctypes.c_int, [_H, ctypes.c_double, _I]),
+    ("glasma_batch_step", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int]),
+    ("glasma_batch_energy", ctypes.c_int, [_H, _D]),
+    ("glasma_batch_synchronize", ctypes.c_int, [_H]),
+    ("glasma_batch_last_error", ctypes.c_char_p, []),
     ("glasma_synchronize", ctypes.c_int, [_H]),
     ("glasma_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("glasma_last_error", ctypes.c_char_p, []),

@@ -1,0 +1,83 @@
+"""Batches of independent events (lattices of uneven sizes) advanced together on one GPU."""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .lattice import Lattice
+
+
+class _EventView(Lattice):
+    """A Lattice over an event handle owned by its batch (not destroyed on close)."""
+
+    def __init__(self, lib, handle, N, a, precision):
+        self.lib = lib
+        self.h = handle
+        self.N = tuple(N)
+        self.a = tuple(a)
+        self.precision = precision
+
+    def close(self):
+        self.h = None
+
+
+def _bcheck(lib, st):
+    if st != 0:
+        raise _lib.GlasmaError(st, lib.glasma_batch_last_error().decode(errors="replace") or
+                               lib.glasma_last_error().decode(errors="replace"))
+
+
+class Batch:
+    def __init__(self, extents, spacings=None, precision="fp32", reunitarize_every=16, stream=None):
+        self.lib = _lib.load()
+        n = len(extents)
+        spacings = spacings or [(1.0, 1.0, 1.0)] * n
+        ext = (ctypes.c_int * (3 * n))(*[int(v) for e in extents for v in e])
+        sp = (ctypes.c_double * (3 * n))(*[float(v) for a in spacings for v in a])
+        prec = {"fp64": _lib.FP64, "fp32": _lib.FP32}[precision]
+        b = ctypes.c_void_p()
+        _bcheck(self.lib, self.lib.glasma_batch_create(n, ext, sp, prec, int(reunitarize_every), ctypes.byref(b)))
+        self.b = b
+        self.events = []
+        for i in range(n):
+            h = ctypes.c_void_p()
+            _bcheck(self.lib, self.lib.glasma_batch_event(self.b, i, ctypes.byref(h)))
+            self.events.append(_EventView(self.lib, h, extents[i], spacings[i], precision))
+        if stream is not None:
+            ptr = getattr(stream, "cuda_stream", stream)
+            _bcheck(self.lib, self.lib.glasma_batch_set_stream(self.b, ctypes.c_void_p(ptr) if ptr else None))
+
+    def autotune(self, dt=0.1):
+        t = (ctypes.c_int * len(self.events))()
+        _bcheck(self.lib, self.lib.glasma_batch_autotune(self.b, float(dt), t))
+        return list(t)
+
+    def step(self, dt, nsteps, use_graph=True):
+        _bcheck(self.lib, self.lib.glasma_batch_step(self.b, float(dt), int(nsteps), int(bool(use_graph))))
+
+    def energy(self):
+        out = np.zeros(len(self.events))
+        _bcheck(self.lib, self.lib.glasma_batch_energy(self.b, out.ctypes.data_as(_lib._D)))
+        return out
+
+    def synchronize(self):
+        _bcheck(self.lib, self.lib.glasma_batch_synchronize(self.b))
+
+    def close(self):
+        if getattr(self, "b", None):
+            for e in self.events:
+                e.close()
+            self.lib.glasma_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -9,30 +9,12 @@
 #include <vector>
 
 #include "../../include/glasma_gb300.h"
-#include "gaugefix.h"
-#include "lattice.cuh"
+#include "handle.h"
 
 using glasma::cx;
 using glasma::FieldPtrs;
 using glasma::Geometry;
 
-struct glasma_lattice {
-  Geometry g;
-  int precision;
-  int reunit_every;
-  long long steps_done;
-  double a_scale;
-  int device;
-  cudaStream_t own_stream;
-  cudaStream_t stream;
-  size_t real_bytes;  // 8 or 4
-  void* f[10];        // device SoA fields, indexed by glasma_field (G, UG, EG allocated lazily)
-  double* staging;    // device AoS staging buffer for host copies
-  size_t staging_bytes;
-  double* scratch;    // reduction partials and results
-  size_t scratch_doubles;
-  glasma::GaugeFixState* gf;
-};
 
 namespace {
 
@@ -207,7 +189,7 @@ int step_impl(glasma_lattice* h, double dt, int nsteps, unsigned flags, cudaEven
   if (e != cudaSuccess) return cuda_fail(e, "ghost sync U");
   for (int n = 0; n < nsteps; n++) {
     if (ev) cudaEventRecord(ev[3 * n], h->stream);
-    e = glasma::launch_efield_jstat<T>(h->g, p, dt, h->stream);
+    e = glasma::launch_efield_jstat<T>(h->g, p, dt, h->tile_x, h->stream);
     if (e != cudaSuccess) return cuda_fail(e, "efield_jstat");
     if (ev) cudaEventRecord(ev[3 * n + 1], h->stream);
     const bool save = (flags & GLASMA_STEP_SAVE_UOLD) && (n == nsteps - 1);
@@ -268,6 +250,7 @@ int glasma_create(int nx, int ny, int nz, double ax, double ay, double az, int p
   h->reunit_every = precision == GLASMA_FP32 ? reunitarize_every : 0;
   h->a_scale = 1.0;
   h->real_bytes = precision == GLASMA_FP64 ? 8 : 4;
+  h->tile_x = glasma::default_tile_x(nx);
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -424,15 +407,15 @@ int glasma_update_efield(glasma_lattice* h, double dt) {
   GLASMA_CHECK_HANDLE(h);
   int st = sync_field_ghosts(h, GLASMA_FIELD_U);
   if (st) return st;
-  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_efield_only<double>(h->g, ptrs<double>(h), dt, h->stream),
-                                  glasma::launch_efield_only<float>(h->g, ptrs<float>(h), dt, h->stream));
+  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_efield_only<double>(h->g, ptrs<double>(h), dt, h->tile_x, h->stream),
+                                  glasma::launch_efield_only<float>(h->g, ptrs<float>(h), dt, h->tile_x, h->stream));
   return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "update_efield");
 }
 
 int glasma_update_jstat(glasma_lattice* h, double dt) {
   GLASMA_CHECK_HANDLE(h);
-  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_jstat_only<double>(h->g, ptrs<double>(h), dt, h->stream),
-                                  glasma::launch_jstat_only<float>(h->g, ptrs<float>(h), dt, h->stream));
+  cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_jstat_only<double>(h->g, ptrs<double>(h), dt, h->tile_x, h->stream),
+                                  glasma::launch_jstat_only<float>(h->g, ptrs<float>(h), dt, h->tile_x, h->stream));
   return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "update_jstat");
 }
 
@@ -561,6 +544,25 @@ int glasma_emt_map(glasma_lattice* h, double* out) {
   return copy_results_to_host(h, res, out, (size_t)nres);
 }
 
+int glasma_pressure_anisotropy(glasma_lattice* h, int z_begin, int z_end, double* ratio, double* p_l, double* p_t) {
+  GLASMA_CHECK_HANDLE(h);
+  if (z_begin < 0 || z_end > h->g.nz || z_begin >= z_end) return fail(GLASMA_ERR_INVALID_ARGUMENT, "bad slice range");
+  std::vector<double> map((size_t)h->g.nz * 10);
+  int st = glasma_emt_map(h, map.data());
+  if (st) return st;
+  double pl = 0.0, pt = 0.0;
+  for (int z = z_begin; z < z_end; z++) {
+    pl += map[(size_t)z * 10 + 3];
+    pt += 0.5 * (map[(size_t)z * 10 + 1] + map[(size_t)z * 10 + 2]);
+  }
+  pl /= (z_end - z_begin);
+  pt /= (z_end - z_begin);
+  if (p_l) *p_l = pl;
+  if (p_t) *p_t = pt;
+  if (ratio) *ratio = pl / pt;
+  return GLASMA_OK;
+}
+
 int glasma_reunitarize(glasma_lattice* h) {
   GLASMA_CHECK_HANDLE(h);
   cudaError_t e = GLASMA_DISPATCH(
@@ -623,6 +625,51 @@ int glasma_fft3d(glasma_lattice* h, const double* in, double* out, int inverse) 
   st = glasma::gaugefix_fft_test(&h->gf, a, reinterpret_cast<const double2*>(in), reinterpret_cast<double2*>(out),
                                  inverse ? 1 : 0, &err);
   return st == GLASMA_OK ? GLASMA_OK : fail(st, err);
+}
+
+int glasma_autotune(glasma_lattice* h, double dt, int* tile_x) {
+  GLASMA_CHECK_HANDLE(h);
+  const int candidates[5] = {128, 64, 32, 16, 8};
+  cudaEvent_t e0, e1;
+  GLASMA_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
+  GLASMA_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+  float best = 1e30f;
+  int best_tx = h->tile_x;
+  for (int tx : candidates) {
+    if (tx > 2 * h->g.nx && tx != glasma::default_tile_x(h->g.nx)) continue;  // mostly idle threads
+    float total = 0.f;
+    for (int rep = 0; rep < 4; rep++) {
+      cudaEventRecord(e0, h->stream);
+      cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_efield_dry<double>(h->g, ptrs<double>(h), dt, tx, h->stream),
+                                      glasma::launch_efield_dry<float>(h->g, ptrs<float>(h), dt, tx, h->stream));
+      cudaEventRecord(e1, h->stream);
+      if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(e, "autotune");
+      }
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) total += ms;  // first run warms caches
+    }
+    if (total < best) {
+      best = total;
+      best_tx = tx;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->tile_x = best_tx;
+  if (tile_x) *tile_x = best_tx;
+  return GLASMA_OK;
+}
+
+int glasma_set_tile(glasma_lattice* h, int tile_x) {
+  if (!h) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null lattice handle");
+  if (tile_x < 1 || tile_x > 128 || 128 % tile_x) return fail(GLASMA_ERR_INVALID_ARGUMENT, "tile_x must divide 128");
+  h->tile_x = tile_x;
+  return GLASMA_OK;
 }
 
 int glasma_synchronize(glasma_lattice* h) {

@@ -1,0 +1,35 @@
+// handle.h -- the lattice handle behind the C ABI (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gaugefix.h"
+#include "lattice.cuh"
+
+struct glasma_lattice {
+  glasma::Geometry g;
+  int precision;
+  int reunit_every;
+  long long steps_done;
+  double a_scale;
+  int device;
+  cudaStream_t own_stream;
+  cudaStream_t stream;
+  size_t real_bytes;  // 8 or 4
+  void* f[10];        // device SoA fields, indexed by glasma_field (G, UG, EG allocated lazily)
+  double* staging;    // device AoS staging buffer for host copies
+  size_t staging_bytes;
+  double* scratch;    // reduction partials and results
+  size_t scratch_doubles;
+  glasma::GaugeFixState* gf;
+  int tile_x;         // K1 tile width along x (autotuned)
+};
+
+namespace glasma {
+// Default K1 tile width: the widest power of two dividing the block that does not exceed Nx.
+inline int default_tile_x(int nx) {
+  int t = 128;
+  while (t > 1 && t > nx) t >>= 1;
+  return t;
+}
+}  // namespace glasma

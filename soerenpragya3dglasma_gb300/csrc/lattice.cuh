@@ -73,8 +73,12 @@ inline bool use_32bit_index(const Geometry& g) { return g.S * 27 < (1LL << 31) -
 
 // ---- launch API shared between translation units (host side) ------------------
 // All launches go to `stream`.  Return cudaGetLastError() of the launch.
+// tile_x: sites along x per K1 block tile (kThreads/tile_x along y); chosen by the autotuner.
 template <typename T>
-cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream);
+// K1 computing everything and storing nothing: timing runs of the autotuner.
+template <typename T>
+cudaError_t launch_efield_dry(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream);
 template <typename T>
 cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second_half,
                            cudaStream_t stream);
@@ -85,9 +89,9 @@ cudaError_t launch_reunitarize(const Geometry& g, cx<T>* U, cudaStream_t stream)
 
 // Sub-step kernels with the reference's exact sub-step boundaries.
 template <typename T>
-cudaError_t launch_efield_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+cudaError_t launch_efield_only(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream);
 template <typename T>
-cudaError_t launch_jstat_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
+cudaError_t launch_jstat_only(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream);
 template <typename T>
 cudaError_t launch_j_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream);
 template <typename T>

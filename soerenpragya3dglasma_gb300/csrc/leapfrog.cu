@@ -17,207 +17,28 @@
 // SUNcDynamics.cpp:181-183) regrouped by linearity of ReTr(i t^a .) and the identity
 // ReTr(i t^a W^dagger) = -ReTr(i t^a W).  Ghost slices are written by the threads that own
 // slice 0 and slice Nz-1, which is the reference's SynchronizeGhostCells after each sub-step.
-#include "lattice.cuh"
+#include "leapfrog_sites.cuh"
 
 namespace glasma {
 
 namespace {
 
-constexpr int kThreads = 128;
-
-// Blocks per SM the register allocation must leave room for (the register cap is 64K / (128 * n)),
-// chosen by measurement on GB300; overridable at build time for tuning sweeps.
-#ifndef GLASMA_FP64_MIN_BLOCKS
-#define GLASMA_FP64_MIN_BLOCKS 2
-#endif
-#ifndef GLASMA_FP32_MIN_BLOCKS
-#define GLASMA_FP32_MIN_BLOCKS 3
-#endif
-template <typename T>
-struct Occupancy;
-template <>
-struct Occupancy<double> {
-  static constexpr int kMinBlocks = GLASMA_FP64_MIN_BLOCKS;
-};
-template <>
-struct Occupancy<float> {
-  static constexpr int kMinBlocks = GLASMA_FP32_MIN_BLOCKS;
-};
-
-template <typename I>
-__device__ __forceinline__ I nb(const Geometry& g, int x, int y, int z, int dx, int dy, int dz) {
-  int xx = x + dx, yy = y + dy;
-  xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
-  yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
-  return (I)xx + (I)g.nx * ((I)yy + (I)g.ny * (I)(z + dz + 1));
-}
-
-template <typename I>
-__device__ __forceinline__ void decode(const Geometry& g, I idx, int& x, int& y, int& z) {
-  const I r = idx / (I)g.nx;
-  x = (int)(idx - r * (I)g.nx);
-  z = (int)(r / (I)g.ny);
-  y = (int)(r - (I)z * (I)g.ny);
-}
-
-// Staples of link mu at x in the (mu,nu) plane, weighted by c, added to acc.
-template <typename T, typename I>
-__device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, I S, int mu, int nu, I s, I s_pmu, I s_pnu,
-                                            I s_pmu_mnu, I s_mnu, T c, Mat<T>& acc) {
-  Mat<T> a, b, t;
-  load_link(U, S, nu, s_pmu, a);
-  load_link(U, S, mu, s_pnu, b);
-  mul_nd(a, b, t);
-  load_link(U, S, nu, s, a);
-  add_mul_nd(t, a, c, acc);
-  load_link(U, S, nu, s_pmu_mnu, a);
-  load_link(U, S, mu, s_mnu, b);
-  mul_dd(a, b, t);
-  load_link(U, S, nu, s_mnu, a);
-  add_mul_nn(t, a, c, acc);
-}
-
-template <typename T>
-struct EParams {
-  T gc[3];    // gamma * cE[mu],   gamma = -2 dt a^3, cE = 1/a_mu^2
-  T cnu[3];   // cE[nu]
-  T jz;       // -(dt/a_z)/sqrt(2)
-  T cj;       // dt/a_z
-  int do_e, do_jstat;
-};
-
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
-    efield_jstat_kernel(Geometry g, FieldPtrs<T> f, EParams<T> p) {
-  const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
-  if (idx >= (I)g.vol) return;
+    efield_jstat_kernel(Geometry g, FieldPtrs<T> f, EParams<T> p, TileMap tm) {
   int x, y, z;
-  decode<I>(g, idx, x, y, z);
-  const I S = (I)g.S, plane = (I)g.plane;
-  const I s = idx + plane;
-  const bool lo = (z == 0), hi = (z == g.nz - 1);
-  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
-  if (p.do_e) {
-    const I sxp = nb<I>(g, x, y, z, 1, 0, 0), sxm = nb<I>(g, x, y, z, -1, 0, 0);
-    const I syp = nb<I>(g, x, y, z, 0, 1, 0), sym = nb<I>(g, x, y, z, 0, -1, 0);
-    const I szp = s + plane, szm = s - plane;
-#pragma unroll 1
-    for (int mu = 0; mu < 3; mu++) {
-      Mat<T> acc;
-      set_zero(acc);
-      if (mu == 0) {
-        add_staples(f.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc);
-        add_staples(f.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc);
-      } else if (mu == 1) {
-        add_staples(f.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc);
-        add_staples(f.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc);
-      } else {
-        add_staples(f.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc);
-        add_staples(f.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc);
-      }
-      Mat<T> u, P;
-      load_link(f.U, S, mu, s, u);
-      mul_nn(u, acc, P);
-      Alg<T> force, e;
-      retr_itg(P, p.gc[mu], force);
-      load_alg(f.E, S, mu * 8, s, e);
-#pragma unroll
-      for (int a = 0; a < 8; a++) e.a[a] += force.a[a];
-      if (mu == 2) {
-        Alg<T> jp, jm;
-        load_alg(f.Jp, S, 0, s, jp);
-        load_alg(f.Jm, S, 0, s, jm);
-#pragma unroll
-        for (int a = 0; a < 8; a++) e.a[a] += p.jz * (jp.a[a] - jm.a[a]);
-      }
-      store_alg(f.E, S, mu * 8, s, e);
-      if (sg >= 0) store_alg(f.E, S, mu * 8, sg, e);
-    }
-  }
-  if (p.do_jstat) {
-    const I szm = s - plane;
-    Mat<T> uzm;
-    load_link(f.U, S, 2, szm, uzm);
-    Alg<T> down, jc, st;
-    load_alg(f.Jp, S, 0, szm, jc);
-    inv_adj_mul(uzm, jc, down);
-    load_alg(f.Jp, S, 0, s, jc);
-    load_alg(f.JpStat, S, 0, s, st);
-#pragma unroll
-    for (int a = 0; a < 8; a++) st.a[a] += -p.cj * (jc.a[a] - down.a[a]);
-    store_alg(f.JpStat, S, 0, s, st);
-    if (sg >= 0) store_alg(f.JpStat, S, 0, sg, st);
-    load_alg(f.Jm, S, 0, szm, jc);
-    inv_adj_mul(uzm, jc, down);
-    load_alg(f.Jm, S, 0, s, jc);
-    load_alg(f.JmStat, S, 0, s, st);
-#pragma unroll
-    for (int a = 0; a < 8; a++) st.a[a] += p.cj * (jc.a[a] - down.a[a]);
-    store_alg(f.JmStat, S, 0, s, st);
-    if (sg >= 0) store_alg(f.JmStat, S, 0, sg, st);
-  }
+  if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
+  efield_site<T, I>(g, f, p, x, y, z);
 }
-
-template <typename T>
-struct LParams {
-  T cU[3];  // -(h) a_mu^2 / a^3 for the half step h
-  T cj;     // dt/a_z
-  int save_uold, do_j, do_second;
-};
 
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
     links_j_kernel(Geometry g, FieldPtrs<T> f, LParams<T> p) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
   if (idx >= (I)g.vol) return;
-  const I S = (I)g.S, plane = (I)g.plane;
-  const I s = idx + plane;
-  const int z = (int)(idx / plane);
-  const bool lo = (z == 0), hi = (z == g.nz - 1);
-  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
-#pragma unroll 1
-  for (int mu = 0; mu < 3; mu++) {
-    Alg<T> e;
-    load_alg(f.E, S, mu * 8, s, e);
-    Mat<T> X, u, uh;
-    expi(p.cU[mu], e, X);
-    load_link(f.U, S, mu, s, u);
-    mul_nn(X, u, uh);
-    if (p.save_uold) {
-      store_link(f.UOld, S, mu, s, uh);
-      if (sg >= 0) store_link(f.UOld, S, mu, sg, uh);
-    }
-    if (mu == 2 && p.do_j) {
-      Alg<T> up, st, j;
-      const I szp = s + plane;
-      load_alg(f.JpStat, S, 0, szp, st);
-      adj_mul(uh, st, up);
-      load_alg(f.JpStat, S, 0, s, st);
-      load_alg(f.Jp, S, 0, s, j);
-#pragma unroll
-      for (int a = 0; a < 8; a++) j.a[a] += -p.cj * (up.a[a] - st.a[a]);
-      store_alg(f.Jp, S, 0, s, j);
-      if (sg >= 0) store_alg(f.Jp, S, 0, sg, j);
-      load_alg(f.JmStat, S, 0, szp, st);
-      adj_mul(uh, st, up);
-      load_alg(f.JmStat, S, 0, s, st);
-      load_alg(f.Jm, S, 0, s, j);
-#pragma unroll
-      for (int a = 0; a < 8; a++) j.a[a] += p.cj * (up.a[a] - st.a[a]);
-      store_alg(f.Jm, S, 0, s, j);
-      if (sg >= 0) store_alg(f.Jm, S, 0, sg, j);
-    }
-    if (p.do_second) {
-      mul_nn(X, uh, u);
-    } else {
-      u = uh;
-    }
-    store_link(f.U, S, mu, s, u);
-    if (sg >= 0) store_link(f.U, S, mu, sg, u);
-  }
+  links_site<T, I>(g, f, p, idx);
 }
 
-// UpdateJ alone (S/DYNAMICS/SUNcDynamics.cpp:238-269) with the links as they stand.
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads) j_only_kernel(Geometry g, FieldPtrs<T> f, T cj) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
@@ -280,57 +101,56 @@ __global__ void copy_kernel(const E* __restrict__ src, E* __restrict__ dst, long
 inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 template <typename T>
-cudaError_t launch_efield_kernel(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, cudaStream_t stream) {
+cudaError_t launch_efield_kernel(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, int tile_x,
+                                 cudaStream_t stream) {
+  if (tile_x <= 0 || tile_x > kThreads || kThreads % tile_x) tile_x = kThreads;
+  const TileMap tm = TileMap::make(g.nx, g.ny, tile_x, kThreads);
+  const unsigned grid = (unsigned)tm.tiles(g.nz);
   if (use_32bit_index(g))
-    efield_jstat_kernel<T, int><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+    efield_jstat_kernel<T, int><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
   else
-    efield_jstat_kernel<T, long long><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+    efield_jstat_kernel<T, long long><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
   return cudaGetLastError();
+}
+
+template <typename T>
+EParams<T> make_eparams(const Geometry& g, double dt, int do_e, int do_jstat, int dry) {
+  EParams<T> p;
+  const double a3 = g.a[0] * g.a[1] * g.a[2];
+  const double gamma = -2.0 * dt * a3;
+  for (int mu = 0; mu < 3; mu++) {
+    const double ce = 1.0 / (g.a[mu] * g.a[mu]);
+    p.gc[mu] = (T)(gamma * ce);
+    p.cnu[mu] = (T)ce;
+  }
+  p.jz = (T)(-(dt / g.a[2]) * 0.70710678118654752440084436210484903928483593768847);
+  p.cj = (T)(dt / g.a[2]);
+  p.do_e = do_e;
+  p.do_jstat = do_jstat;
+  p.dry = dry;
+  return p;
 }
 
 }  // namespace
 
 template <typename T>
-cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream) {
-  EParams<T> p;
-  const double a3 = g.a[0] * g.a[1] * g.a[2];
-  const double gamma = -2.0 * dt * a3;
-  for (int mu = 0; mu < 3; mu++) {
-    const double ce = 1.0 / (g.a[mu] * g.a[mu]);
-    p.gc[mu] = (T)(gamma * ce);
-    p.cnu[mu] = (T)ce;
-  }
-  p.jz = (T)(-(dt / g.a[2]) * 0.70710678118654752440084436210484903928483593768847);
-  p.cj = (T)(dt / g.a[2]);
-  p.do_e = 1;
-  p.do_jstat = 1;
-  return launch_efield_kernel<T>(g, f, p, stream);
+cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream) {
+  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 1, 1, 0), tile_x, stream);
 }
 
 template <typename T>
-cudaError_t launch_efield_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream) {
-  EParams<T> p;
-  const double a3 = g.a[0] * g.a[1] * g.a[2];
-  const double gamma = -2.0 * dt * a3;
-  for (int mu = 0; mu < 3; mu++) {
-    const double ce = 1.0 / (g.a[mu] * g.a[mu]);
-    p.gc[mu] = (T)(gamma * ce);
-    p.cnu[mu] = (T)ce;
-  }
-  p.jz = (T)(-(dt / g.a[2]) * 0.70710678118654752440084436210484903928483593768847);
-  p.cj = (T)(dt / g.a[2]);
-  p.do_e = 1;
-  p.do_jstat = 0;
-  return launch_efield_kernel<T>(g, f, p, stream);
+cudaError_t launch_efield_dry(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream) {
+  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 1, 1, 1), tile_x, stream);
 }
 
 template <typename T>
-cudaError_t launch_jstat_only(const Geometry& g, FieldPtrs<T> f, double dt, cudaStream_t stream) {
-  EParams<T> p = {};
-  p.cj = (T)(dt / g.a[2]);
-  p.do_e = 0;
-  p.do_jstat = 1;
-  return launch_efield_kernel<T>(g, f, p, stream);
+cudaError_t launch_efield_only(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream) {
+  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 1, 0, 0), tile_x, stream);
+}
+
+template <typename T>
+cudaError_t launch_jstat_only(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream) {
+  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 0, 1, 0), tile_x, stream);
 }
 
 template <typename T>
@@ -386,9 +206,10 @@ cudaError_t launch_copy_links(const Geometry& g, const cx<T>* src, cx<T>* dst, c
 }
 
 #define GLASMA_INSTANTIATE(T)                                                                                   \
-  template cudaError_t launch_efield_jstat<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);            \
-  template cudaError_t launch_efield_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);             \
-  template cudaError_t launch_jstat_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);              \
+  template cudaError_t launch_efield_jstat<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);       \
+  template cudaError_t launch_efield_dry<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);         \
+  template cudaError_t launch_efield_only<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);        \
+  template cudaError_t launch_jstat_only<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);         \
   template cudaError_t launch_links_j<T>(const Geometry&, FieldPtrs<T>, double, bool, bool, bool, cudaStream_t); \
   template cudaError_t launch_links_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);              \
   template cudaError_t launch_j_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);                  \

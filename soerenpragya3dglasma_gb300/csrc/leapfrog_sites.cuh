@@ -1,0 +1,233 @@
+// leapfrog_sites.cuh -- per-site bodies of the two leapfrog kernels, shared by the single-lattice
+// launches (leapfrog.cu) and the batched multi-event launches (batch.cu).
+#pragma once
+
+#include "lattice.cuh"
+
+namespace glasma {
+
+
+constexpr int kThreads = 128;
+
+// Blocks per SM the register allocation must leave room for (the register cap is 64K / (128 * n)),
+// chosen by measurement on GB300; overridable at build time for tuning sweeps.
+#ifndef GLASMA_FP64_MIN_BLOCKS
+#define GLASMA_FP64_MIN_BLOCKS 2
+#endif
+#ifndef GLASMA_FP32_MIN_BLOCKS
+#define GLASMA_FP32_MIN_BLOCKS 3
+#endif
+template <typename T>
+struct Occupancy;
+template <>
+struct Occupancy<double> {
+  static constexpr int kMinBlocks = GLASMA_FP64_MIN_BLOCKS;
+};
+template <>
+struct Occupancy<float> {
+  static constexpr int kMinBlocks = GLASMA_FP32_MIN_BLOCKS;
+};
+
+template <typename I>
+__device__ __forceinline__ I nb(const Geometry& g, int x, int y, int z, int dx, int dy, int dz) {
+  int xx = x + dx, yy = y + dy;
+  xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
+  yy = yy < 0 ? yy + g.ny : (yy >= g.ny ? yy - g.ny : yy);
+  return (I)xx + (I)g.nx * ((I)yy + (I)g.ny * (I)(z + dz + 1));
+}
+
+template <typename I>
+__device__ __forceinline__ void decode(const Geometry& g, I idx, int& x, int& y, int& z) {
+  const I r = idx / (I)g.nx;
+  x = (int)(idx - r * (I)g.nx);
+  z = (int)(r / (I)g.ny);
+  y = (int)(r - (I)z * (I)g.ny);
+}
+
+// Staples of link mu at x in the (mu,nu) plane, weighted by c, added to acc.
+template <typename T, typename I>
+__device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, I S, int mu, int nu, I s, I s_pmu, I s_pnu,
+                                            I s_pmu_mnu, I s_mnu, T c, Mat<T>& acc) {
+  Mat<T> a, b, t;
+  load_link(U, S, nu, s_pmu, a);
+  load_link(U, S, mu, s_pnu, b);
+  mul_nd(a, b, t);
+  load_link(U, S, nu, s, a);
+  add_mul_nd(t, a, c, acc);
+  load_link(U, S, nu, s_pmu_mnu, a);
+  load_link(U, S, mu, s_mnu, b);
+  mul_dd(a, b, t);
+  load_link(U, S, nu, s_mnu, a);
+  add_mul_nn(t, a, c, acc);
+}
+
+template <typename T>
+struct EParams {
+  T gc[3];    // gamma * cE[mu],   gamma = -2 dt a^3, cE = 1/a_mu^2
+  T cnu[3];   // cE[nu]
+  T jz;       // -(dt/a_z)/sqrt(2)
+  T cj;       // dt/a_z
+  int do_e, do_jstat;
+  int dry;    // compute, store nothing (autotuner timing runs)
+};
+
+// The electric-field and JStat update of one site (K1's per-site body).
+template <typename T, typename I>
+__device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T>& f, const EParams<T>& p, int x, int y,
+                                            int z) {
+  const I S = (I)g.S, plane = (I)g.plane;
+  const I s = (I)x + (I)g.nx * ((I)y + (I)g.ny * (I)(z + 1));
+  const bool lo = (z == 0), hi = (z == g.nz - 1);
+  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
+  if (p.do_e) {
+    const I sxp = nb<I>(g, x, y, z, 1, 0, 0), sxm = nb<I>(g, x, y, z, -1, 0, 0);
+    const I syp = nb<I>(g, x, y, z, 0, 1, 0), sym = nb<I>(g, x, y, z, 0, -1, 0);
+    const I szp = s + plane, szm = s - plane;
+#pragma unroll 1
+    for (int mu = 0; mu < 3; mu++) {
+      Mat<T> acc;
+      set_zero(acc);
+      if (mu == 0) {
+        add_staples(f.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc);
+        add_staples(f.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc);
+      } else if (mu == 1) {
+        add_staples(f.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc);
+        add_staples(f.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc);
+      } else {
+        add_staples(f.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc);
+        add_staples(f.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc);
+      }
+      Mat<T> u, P;
+      load_link(f.U, S, mu, s, u);
+      mul_nn(u, acc, P);
+      Alg<T> force, e;
+      retr_itg(P, p.gc[mu], force);
+      load_alg(f.E, S, mu * 8, s, e);
+#pragma unroll
+      for (int a = 0; a < 8; a++) e.a[a] += force.a[a];
+      if (mu == 2) {
+        Alg<T> jp, jm;
+        load_alg(f.Jp, S, 0, s, jp);
+        load_alg(f.Jm, S, 0, s, jm);
+#pragma unroll
+        for (int a = 0; a < 8; a++) e.a[a] += p.jz * (jp.a[a] - jm.a[a]);
+      }
+      if (!p.dry) {
+        store_alg(f.E, S, mu * 8, s, e);
+        if (sg >= 0) store_alg(f.E, S, mu * 8, sg, e);
+      }
+    }
+  }
+  if (p.do_jstat) {
+    const I szm = s - plane;
+    Mat<T> uzm;
+    load_link(f.U, S, 2, szm, uzm);
+    Alg<T> down, jc, st;
+    load_alg(f.Jp, S, 0, szm, jc);
+    inv_adj_mul(uzm, jc, down);
+    load_alg(f.Jp, S, 0, s, jc);
+    load_alg(f.JpStat, S, 0, s, st);
+#pragma unroll
+    for (int a = 0; a < 8; a++) st.a[a] += -p.cj * (jc.a[a] - down.a[a]);
+    if (!p.dry) {
+      store_alg(f.JpStat, S, 0, s, st);
+      if (sg >= 0) store_alg(f.JpStat, S, 0, sg, st);
+    }
+    load_alg(f.Jm, S, 0, szm, jc);
+    inv_adj_mul(uzm, jc, down);
+    load_alg(f.Jm, S, 0, s, jc);
+    load_alg(f.JmStat, S, 0, s, st);
+#pragma unroll
+    for (int a = 0; a < 8; a++) st.a[a] += p.cj * (jc.a[a] - down.a[a]);
+    if (!p.dry) {
+      store_alg(f.JmStat, S, 0, s, st);
+      if (sg >= 0) store_alg(f.JmStat, S, 0, sg, st);
+    }
+  }
+}
+
+// Thread-to-site map of K1: a block of kThreads threads covers a tile of tile_x x (kThreads/tile_x)
+// sites of one z slice, so most y-neighbours a block reads are its own sites (L1 hits).
+struct TileMap {
+  int tile_x, tile_y, ntx, nty;
+  __host__ __device__ static TileMap make(int nx, int ny, int tile_x, int threads) {
+    TileMap t;
+    t.tile_x = tile_x;
+    t.tile_y = threads / tile_x;
+    t.ntx = (nx + t.tile_x - 1) / t.tile_x;
+    t.nty = (ny + t.tile_y - 1) / t.tile_y;
+    return t;
+  }
+  __host__ __device__ long long tiles(int nz) const { return (long long)ntx * nty * nz; }
+  // tile index -> site of thread `t` (false when the thread falls outside the lattice)
+  __device__ bool site(long long tile, int t, int nx, int ny, int& x, int& y, int& z) const {
+    const long long per_z = (long long)ntx * nty;
+    z = (int)(tile / per_z);
+    const int r = (int)(tile - (long long)z * per_z);
+    const int by = r / ntx, bx = r - by * ntx;
+    x = bx * tile_x + t % tile_x;
+    y = by * tile_y + t / tile_x;
+    return x < nx && y < ny;
+  }
+};
+
+template <typename T>
+struct LParams {
+  T cU[3];  // -(h) a_mu^2 / a^3 for the half step h
+  T cj;     // dt/a_z
+  int save_uold, do_j, do_second;
+};
+
+// K2's per-site body: links to t+dt (two applications of one exp), UOld, J transport.
+template <typename T, typename I>
+__device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>& f, const LParams<T>& p, I idx) {
+  const I S = (I)g.S, plane = (I)g.plane;
+  const I s = idx + plane;
+  const int z = (int)(idx / plane);
+  const bool lo = (z == 0), hi = (z == g.nz - 1);
+  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
+#pragma unroll 1
+  for (int mu = 0; mu < 3; mu++) {
+    Alg<T> e;
+    load_alg(f.E, S, mu * 8, s, e);
+    Mat<T> X, u, uh;
+    expi(p.cU[mu], e, X);
+    load_link(f.U, S, mu, s, u);
+    mul_nn(X, u, uh);
+    if (p.save_uold) {
+      store_link(f.UOld, S, mu, s, uh);
+      if (sg >= 0) store_link(f.UOld, S, mu, sg, uh);
+    }
+    if (mu == 2 && p.do_j) {
+      Alg<T> up, st, j;
+      const I szp = s + plane;
+      load_alg(f.JpStat, S, 0, szp, st);
+      adj_mul(uh, st, up);
+      load_alg(f.JpStat, S, 0, s, st);
+      load_alg(f.Jp, S, 0, s, j);
+#pragma unroll
+      for (int a = 0; a < 8; a++) j.a[a] += -p.cj * (up.a[a] - st.a[a]);
+      store_alg(f.Jp, S, 0, s, j);
+      if (sg >= 0) store_alg(f.Jp, S, 0, sg, j);
+      load_alg(f.JmStat, S, 0, szp, st);
+      adj_mul(uh, st, up);
+      load_alg(f.JmStat, S, 0, s, st);
+      load_alg(f.Jm, S, 0, s, j);
+#pragma unroll
+      for (int a = 0; a < 8; a++) j.a[a] += p.cj * (up.a[a] - st.a[a]);
+      store_alg(f.Jm, S, 0, s, j);
+      if (sg >= 0) store_alg(f.Jm, S, 0, sg, j);
+    }
+    if (p.do_second) {
+      mul_nn(X, uh, u);
+    } else {
+      u = uh;
+    }
+    store_link(f.U, S, mu, s, u);
+    if (sg >= 0) store_link(f.U, S, mu, sg, u);
+  }
+}
+
+// UpdateJ alone (S/DYNAMICS/SUNcDynamics.cpp:238-269) with the links as they stand.
+
+}  // namespace glasma

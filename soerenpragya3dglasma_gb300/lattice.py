@@ -103,6 +103,19 @@ class Lattice:
     def set_scale(self, a_scale):
         check(self.lib.glasma_set_scale(self.h, float(a_scale)))
 
+    def fill_synthetic(self, seed, link_amp=0.3, e_amp=0.1, j_amp=0.02):
+        """Seeded synthetic fields generated on the device (links exp(i link_amp t.r), Gaussian E, J)."""
+        check(self.lib.glasma_fill_synthetic(self.h, int(seed), float(link_amp), float(e_amp), float(j_amp)))
+
+    def autotune(self, dt=0.1):
+        """Pick the electric-field kernel's block tile for this lattice; returns tile_x."""
+        t = ctypes.c_int()
+        check(self.lib.glasma_autotune(self.h, float(dt), ctypes.byref(t)))
+        return t.value
+
+    def set_tile(self, tile_x):
+        check(self.lib.glasma_set_tile(self.h, int(tile_x)))
+
     def synchronize(self):
         check(self.lib.glasma_synchronize(self.h))
 
@@ -183,6 +196,13 @@ class Lattice:
         out = np.zeros((self.N[2], 10))
         check(self.lib.glasma_emt_map(self.h, out.ctypes.data_as(_lib._D)))
         return out
+
+    def pressure_anisotropy(self, z_begin, z_end):
+        """(P_L/P_T, P_L, P_T) over slices [z_begin, z_end) from the energy-momentum map."""
+        r, pl, pt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(self.lib.glasma_pressure_anisotropy(self.h, int(z_begin), int(z_end), ctypes.byref(r), ctypes.byref(pl),
+                                                  ctypes.byref(pt)))
+        return r.value, pl.value, pt.value
 
     # -- Coulomb gauge fixing (S/GAUGETRANSFORMATION)
     def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False):

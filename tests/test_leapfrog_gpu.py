@@ -163,3 +163,15 @@ def test_fp32_reunitarize_restores_unitarity():
         assert lat.unitarity()[0] > 1e-3
         lat.reunitarize()
         assert lat.unitarity()[0] < 1e-6
+
+
+def test_pressure_anisotropy_from_emt_map(oracle):
+    N, a = (8, 8, 24), (1.0, 1.0, 1.0)
+    f = O.random_fields(N, 91, link_amp=0.25)
+    emt = oracle.emt_map(f, N, a)
+    z0, z1 = 8, 16
+    pl = emt[z0:z1, 3].mean()
+    pt = 0.5 * (emt[z0:z1, 1] + emt[z0:z1, 2]).mean()
+    with _gpu(f, N, a) as lat:
+        r, gl, gt = lat.pressure_anisotropy(z0, z1)
+    assert np.allclose([gl, gt, r], [pl, pt, pl / pt], rtol=1e-11)
