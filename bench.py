@@ -271,11 +271,16 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
 
-    stream = torch.cuda.current_stream(dev)
+    # a stream of our own: the legacy default stream is handle 0, which the C ABI reads as
+    # "the handle's own stream", and the CUDA events below must sit on the launching stream
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     N = N_WORK
     vol = N[0] * N[1] * N[2]
     inputs = device_inputs(torch, N, SEED + rank, dev)
     torch.cuda.synchronize()
+
+    tiles = {}
 
     def make_lattice(precision):
         lat = Lattice(N, A_WORK, precision=precision, reunitarize_every=16 if precision == "fp32" else 0,
@@ -283,6 +288,11 @@ def run_ours(args):
         for k in INPUT_FIELDS:
             lat.upload_device(k, inputs[k].data_ptr())
         lat.upload_device("UOld", inputs["U"].data_ptr())
+        if args.tile:
+            lat.set_tile(args.tile)
+            tiles[precision] = args.tile
+        else:
+            tiles[precision] = lat.autotune(DT)  # untimed: picks the electric-field kernel's block tile
         return lat
 
     peak, peak_kind = hbm_peak()
@@ -412,6 +422,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": 2 * args.steps,
+        "tiles": tiles,
     }
     print(json.dumps(line), flush=True)
 
@@ -437,7 +448,8 @@ def run_batched(args):
 
     build.build()
     torch.cuda.set_device(0)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     shapes = batched_shapes(args.events)
     sites = sum(a * b * c for a, b, c in shapes)
     with Batch(shapes, precision="fp32", reunitarize_every=16, stream=stream) as b:
@@ -497,6 +509,7 @@ def main():
     ap.add_argument("--workload", default="production", choices=["production", "batched"],
                     help="production: the headline 128x128x512 line; batched: 64 uneven events in one launch")
     ap.add_argument("--events", type=int, default=64)
+    ap.add_argument("--tile", type=int, default=0, help="fixed electric-field tile width instead of autotuning")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

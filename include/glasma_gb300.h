@@ -183,6 +183,24 @@ int glasma_gauss_noalloc(const double* U, const double* E, const double* JpStat,
                          int nz, double ax, double ay, double az, double a_scale, double* result, double* zprofile,
                          void* stream);
 
+/* ---- Adjoint leapfrog (FP64 lattices).  No reference counterpart.
+ * Objective on the state after nsteps: L = N(q)/D(q), q = (e0,e1,e2,b0,b1,b2) summed over the slices
+ * z in [z_begin, z_end), e_mu = cE_mu sum E_mu^2, b_i = cB_i sum 4 ReTr(1 - P_jk) with the bulk
+ * observables' constants (S/OBSERVABLES/BulkObservables.cpp:22-97); N = num.q, D = den.q (D = 1 if
+ * den is all zero).  Pressure anisotropy P_L/P_T: num = (1,1,-1,1,1,-1), den = (0,0,1,0,0,1);
+ * energy T00: num = (.5,.5,.5,.5,.5,.5), den = 0.
+ * glasma_objective evaluates L on the current state.  glasma_adjoint runs nsteps forward from the
+ * current state (checkpoints every checkpoint_every steps), evaluates L, and returns dL/d(initial
+ * field) for E and the four currents (host buffers in the reference layout, ghost entries zero; any
+ * may be NULL), with respect to interior values whose ghost slices are copies of the boundary
+ * slices.  Backward pass: time-reversed integration between checkpoints.  The handle is left in
+ * its initial state. */
+int glasma_objective(glasma_lattice* h, int z_begin, int z_end, const double* num, const double* den, double* value);
+int glasma_adjoint(glasma_lattice* h, double dt, int nsteps, int checkpoint_every, int z_begin, int z_end,
+                   const double* num, const double* den, double* objective, double* grad_E, double* grad_Jp,
+                   double* grad_Jm, double* grad_JpStat, double* grad_JmStat);
+const char* glasma_adjoint_last_error(void);
+
 /* ---- Batches of independent events (lattices of uneven sizes) advanced together.
  * No reference counterpart: the reference runs one event per process (seeds are farmed out as
  * separate jobs).  Each event is an ordinary lattice handle (glasma_batch_event gives it, for

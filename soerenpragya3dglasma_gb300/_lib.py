@@ -57,6 +57,10 @@ SIGNATURES = [
     ("glasma_fft3d", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("glasma_gauss_noalloc", ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("glasma_objective", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _D, _D, _D]),
+    ("glasma_adjoint", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      _D, _D, _D, _D, _D, _D, _D, _D]),
+    ("glasma_adjoint_last_error", ctypes.c_char_p, []),
     ("glasma_batch_create", ctypes.c_int, [ctypes.c_int, _I, _D, ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_void_p)]),
     ("glasma_batch_destroy", ctypes.c_int, [_H]),

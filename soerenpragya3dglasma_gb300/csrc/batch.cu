@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
 }
 
 template <typename T, typename I>
-__global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
     links_batch_kernel(const EventDesc<T>* __restrict__ ev, int n, long long total) {
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     const int e = find_event(ev, n, t, false);

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
 }
 
 template <typename T, typename I>
-__global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
     links_j_kernel(Geometry g, FieldPtrs<T> f, LParams<T> p) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
   if (idx >= (I)g.vol) return;

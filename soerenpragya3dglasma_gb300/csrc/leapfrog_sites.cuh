@@ -11,21 +11,27 @@ constexpr int kThreads = 128;
 
 // Blocks per SM the register allocation must leave room for (the register cap is 64K / (128 * n)),
 // chosen by measurement on GB300; overridable at build time for tuning sweeps.
+// (GB300 sweep, 128x128x512: FP32 K1 fastest at 5 blocks/SM, K2 at 8; FP64 is FP64-ALU bound.)
 #ifndef GLASMA_FP64_MIN_BLOCKS
 #define GLASMA_FP64_MIN_BLOCKS 2
 #endif
 #ifndef GLASMA_FP32_MIN_BLOCKS
-#define GLASMA_FP32_MIN_BLOCKS 3
+#define GLASMA_FP32_MIN_BLOCKS 5
+#endif
+#ifndef GLASMA_FP32_LINKS_MIN_BLOCKS
+#define GLASMA_FP32_LINKS_MIN_BLOCKS 8
 #endif
 template <typename T>
 struct Occupancy;
 template <>
 struct Occupancy<double> {
-  static constexpr int kMinBlocks = GLASMA_FP64_MIN_BLOCKS;
+  static constexpr int kMinBlocks = GLASMA_FP64_MIN_BLOCKS;       // electric-field kernel
+  static constexpr int kLinksMinBlocks = GLASMA_FP64_MIN_BLOCKS;  // link/J kernel
 };
 template <>
 struct Occupancy<float> {
   static constexpr int kMinBlocks = GLASMA_FP32_MIN_BLOCKS;
+  static constexpr int kLinksMinBlocks = GLASMA_FP32_LINKS_MIN_BLOCKS;
 };
 
 template <typename I>

@@ -204,6 +204,32 @@ class Lattice:
                                                   ctypes.byref(pt)))
         return r.value, pl.value, pt.value
 
+    # -- adjoint leapfrog
+    PL_OVER_PT = ((1, 1, -1, 1, 1, -1), (0, 0, 1, 0, 0, 1))
+    ENERGY = ((0.5,) * 6, (0,) * 6)
+
+    def objective(self, z_begin, z_end, form=PL_OVER_PT):
+        num = (ctypes.c_double * 6)(*form[0])
+        den = (ctypes.c_double * 6)(*form[1])
+        v = ctypes.c_double()
+        st = self.lib.glasma_objective(self.h, int(z_begin), int(z_end), num, den, ctypes.byref(v))
+        if st:
+            raise _lib.GlasmaError(st, self.lib.glasma_adjoint_last_error().decode(errors="replace"))
+        return v.value
+
+    def adjoint(self, dt, nsteps, z_begin, z_end, form=PL_OVER_PT, checkpoint_every=50):
+        """Objective after nsteps and its gradient w.r.t. the initial E and currents (host layout)."""
+        num = (ctypes.c_double * 6)(*form[0])
+        den = (ctypes.c_double * 6)(*form[1])
+        v = ctypes.c_double()
+        grads = {k: empty_field(k, self.N) for k in ("E", "Jp", "Jm", "JpStat", "JmStat")}
+        st = self.lib.glasma_adjoint(self.h, float(dt), int(nsteps), int(checkpoint_every), int(z_begin), int(z_end),
+                                     num, den, ctypes.byref(v),
+                                     *[grads[k].ctypes.data_as(_lib._D) for k in ("E", "Jp", "Jm", "JpStat", "JmStat")])
+        if st:
+            raise _lib.GlasmaError(st, self.lib.glasma_adjoint_last_error().decode(errors="replace"))
+        return v.value, grads
+
     # -- Coulomb gauge fixing (S/GAUGETRANSFORMATION)
     def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False):
         log = np.zeros((max(int(max_iters), 1), 7))
