@@ -147,6 +147,19 @@ int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double to
 /* GaugeTransformation::SetIdentity (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:41-60). */
 int glasma_gauge_reset(glasma_lattice* h);
 
+/* McLerran-Venugopalan initial state, as Simulation::Run builds it (S/Simulation.cpp:337-374:
+ * CollidingObjects::SetWilsonLines for each nucleus, then SingleSheet over z in [0,(Nz-2)/2] for
+ * the left and [Nz/2,Nz-1] for the right nucleus) or, with single_left != 0, one left-moving nucleus
+ * over all z (S/LeftNucleusSimulation.cpp).  zeta_left / zeta_right: the charge fluctuations the
+ * reference draws from its random generator (S/COLLIDINGOBJECTS/CollidingObjects.cpp:335-342), host
+ * arrays of 8*Nx*Ny N(0,1) numbers in its order a + 8*(x + Nx*y); qs scales them (g^2 mu), centre and
+ * sigma give the longitudinal profile, lambda and meff the smoothing, dt the time step of the
+ * evolved sheet.  Overwrites U, UOld, E and the four currents; ghost slices synced. */
+int glasma_mv_init(glasma_lattice* h, int single_left, const double* zeta_left, const double* zeta_right,
+                   double qs_left, double qs_right, int center_left, int center_right, double sigma, double lambda,
+                   double meff, double dt);
+const char* glasma_mv_last_error(void);
+
 /* Seeded synthetic fields generated on the device (benchmarks, demos): links exp(i link_amp t.r),
  * E = e_amp r, the four currents j_amp r, r ~ N(0,1) from a counter-based generator (SplitMix64 +
  * Box-Muller), ghost slices synced.  Same seed, same fields.  No reference counterpart. */

@@ -50,6 +50,9 @@ SIGNATURES = [
     ("glasma_reunitarize", ctypes.c_int, [_H]),
     ("glasma_coulomb_fix", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
     ("glasma_gauge_reset", ctypes.c_int, [_H]),
+    ("glasma_mv_init", ctypes.c_int, [_H, ctypes.c_int, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    ("glasma_mv_last_error", ctypes.c_char_p, []),
     ("glasma_fill_synthetic", ctypes.c_int, [_H, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_double]),
     ("glasma_autotune", ctypes.c_int, [_H, ctypes.c_double, _I]),

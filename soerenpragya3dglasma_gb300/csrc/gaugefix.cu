@@ -307,6 +307,17 @@ int ilog2(int n) {
 
 }  // namespace
 
+double2* make_twiddles(int n, cudaStream_t stream) {
+  const int count = is_pow2(n) ? (n / 2 > 0 ? n / 2 : 1) : n;
+  double2* tw = nullptr;
+  if (cudaMalloc(&tw, sizeof(double2) * count) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  twiddle_kernel<<<(count + 255) / 256, 256, 0, stream>>>(tw, n, count);
+  return tw;
+}
+
 struct GaugeFixState {
   Geometry g;
   int precision = -1;
@@ -332,7 +343,13 @@ int tile_lines_for(int n, long long st, long long nlines_total) {
 }
 
 cudaError_t fft_axis(GaugeFixState* s, int n, long long st, long long total, int inverse, cudaStream_t stream) {
-  const double2* tw = s->twiddles.at(n);
+  return fft_lines(s->X, n, st, total, inverse, s->twiddles.at(n), stream);
+}
+
+}  // namespace
+
+cudaError_t fft_lines(double2* X, int n, long long st, long long total, int inverse, const double2* tw,
+                      cudaStream_t stream) {
   const long long nlines = total / n;
   const int tl = tile_lines_for(n, st, nlines);
   const long long tiles = nlines / tl;
@@ -340,13 +357,15 @@ cudaError_t fft_axis(GaugeFixState* s, int n, long long st, long long total, int
   if (is_pow2(n)) {
     if (n == 1) return cudaSuccess;
     cudaFuncSetAttribute(fft_pow2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kFftMaxTile * 16 > smem ? kFftMaxTile * 16 : smem));
-    fft_pow2_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(s->X, n, ilog2(n), st, tl, tw, inverse);
+    fft_pow2_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, n, ilog2(n), st, tl, tw, inverse);
   } else {
     cudaFuncSetAttribute(dft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem > 48 * 1024 ? smem : 48 * 1024));
-    dft_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(s->X, n, st, tl, tw, inverse);
+    dft_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, n, st, tl, tw, inverse);
   }
   return cudaGetLastError();
 }
+
+namespace {
 
 // 3D transform of the 8 colour planes of X
 cudaError_t fft3d(GaugeFixState* s, int inverse, cudaStream_t stream) {

@@ -28,6 +28,13 @@ struct GaugeFixArgs {
 int gaugefix_run(GaugeFixState** state, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
                  double* log, int* iterations, std::string* err);
 void gaugefix_destroy(GaugeFixState* state);
+
+// Batched 1D transforms of length n in place over `total` complex values: element k of line l is
+// at l*n + k (st == 1) or at o*st*n + i + k*st (st > 1, l = (o, i)); unnormalised, sign -1 forward,
+// +1 inverse.  tw = make_twiddles(n) (cudaFree it when done).
+cudaError_t fft_lines(double2* X, int n, long long st, long long total, int inverse, const double2* tw,
+                      cudaStream_t stream);
+double2* make_twiddles(int n, cudaStream_t stream);
 // 3D transform (unnormalised, sign -1 forward / +1 inverse) of 8 colour planes X[a][z][y][x];
 // `in` / `out` may be host or device memory.
 int gaugefix_fft_test(GaugeFixState** state, const GaugeFixArgs& a, const double2* in, double2* out, int inverse,

@@ -103,6 +103,21 @@ class Lattice:
     def set_scale(self, a_scale):
         check(self.lib.glasma_set_scale(self.h, float(a_scale)))
 
+    def mv_init(self, zeta_left, zeta_right=None, qs=(0.5, 0.5), centers=None, sigma=4.0, lam=1.65, meff=0.2,
+                dt=0.125):
+        """MV collision (zeta_right given) or single left-moving nucleus (zeta_right None) on the GPU.
+        zeta_*: 8*Nx*Ny N(0,1) charge fluctuations in the order a + 8*(x + Nx*y)."""
+        zl = np.ascontiguousarray(zeta_left, dtype=np.float64)
+        zr = None if zeta_right is None else np.ascontiguousarray(zeta_right, dtype=np.float64)
+        nz = self.N[2]
+        centers = centers or (nz // 2 - nz // 5, nz // 2 + nz // 5)
+        st = self.lib.glasma_mv_init(self.h, int(zr is None), zl.ctypes.data_as(_lib._D),
+                                     zr.ctypes.data_as(_lib._D) if zr is not None else None, float(qs[0]),
+                                     float(qs[1]), int(centers[0]), int(centers[1]), float(sigma), float(lam),
+                                     float(meff), float(dt))
+        if st:
+            raise _lib.GlasmaError(st, self.lib.glasma_mv_last_error().decode(errors="replace"))
+
     def fill_synthetic(self, seed, link_amp=0.3, e_amp=0.1, j_amp=0.02):
         """Seeded synthetic fields generated on the device (links exp(i link_amp t.r), Gaussian E, J)."""
         check(self.lib.glasma_fill_synthetic(self.h, int(seed), float(link_amp), float(e_amp), float(j_amp)))
@@ -246,6 +261,10 @@ class Lattice:
         out = np.empty_like(X)
         check(self.lib.glasma_fft3d(self.h, X.ctypes.data, out.ctypes.data, int(inverse)))
         return out
+
+    def fft3d_device(self, in_ptr, out_ptr, inverse=False):
+        """Batched 3D FFT of 8 colour planes between device buffers (8*Nx*Ny*Nz complex doubles)."""
+        check(self.lib.glasma_fft3d(self.h, ctypes.c_void_p(int(in_ptr)), ctypes.c_void_p(int(out_ptr)), int(inverse)))
 
     def gauge_reset(self):
         check(self.lib.glasma_gauge_reset(self.h))

@@ -175,3 +175,20 @@ def test_pressure_anisotropy_from_emt_map(oracle):
     with _gpu(f, N, a) as lat:
         r, gl, gt = lat.pressure_anisotropy(z0, z1)
     assert np.allclose([gl, gt, r], [pl, pt, pl / pt], rtol=1e-11)
+
+
+def test_mv_init_matches_reference_golden(golden_dir):
+    """MV collision initial state built on the GPU from the same injected charge fluctuations the
+    reference's SetWilsonLines/SingleSheet consumed (golden fixture from the compiled reference)."""
+    g = _load(golden_dir, "mv_collision.npz")
+    N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
+    n = 8 * N[0] * N[1]
+    zl, zr = g["gauss_in"][:n], g["gauss_in"][n:2 * n]
+    with Lattice(N, a) as lat:
+        lat.mv_init(zl, zr, qs=(float(g["cfg_qs"]),) * 2, centers=(int(g["center_left"]), int(g["center_right"])),
+                    sigma=float(g["cfg_sigma"]), lam=float(g["cfg_lam"]), meff=float(g["cfg_meff"]), dt=dt)
+        out = lat.download_fields()
+        for k in FIELDS:
+            ref = g["init_" + k]
+            assert np.max(np.abs(out[k] - ref)) <= 1e-11 * max(np.max(np.abs(ref)), 1e-3), k
+        assert np.allclose(lat.bulk(), g["t0_bulk"], rtol=1e-10, atol=1e-11)
