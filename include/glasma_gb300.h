@@ -64,6 +64,10 @@ enum glasma_field {
 /* glasma_coulomb_fix flags */
 #define GLASMA_GF_PROJECT_ZERO_MODE 0x1u /* drop the p=0 mode of the update (the reference keeps
                                             it unnormalised); a documented deviation */
+#define GLASMA_GF_FFT_FP32 0x2u          /* run the acceleration step's two 3D transforms in FP32
+                                            (the gradient, the update and the links stay FP64): the
+                                            iterates differ from the reference's at the 1e-7 level,
+                                            the converged gauge is the same */
 
 /* Create a lattice (replaces Lattice::Init, S/LATTICE/SUNcVariables.cpp:71-90, and the
  * container constructors, S/LATTICE/GaugeLinks.cpp:110-127): links set to the identity,
@@ -93,14 +97,27 @@ int glasma_upload_device(glasma_lattice* h, int field, const double* device_aos)
 int glasma_download_device(glasma_lattice* h, int field, double* device_aos);
 
 /* nsteps x Dynamics::SUNc::Update (S/DYNAMICS/SUNcDynamics.cpp:353-378) with time step dt.
- * The electric-field/JStat sub-steps and the link/J sub-steps are fused into two kernels
- * per step.  SaveOldLink runs when GLASMA_STEP_SAVE_UOLD is set (for the last step of the
- * call, which leaves UOld exactly as the reference leaves it). */
+ * With the two-pass method (the default) the electric-field/JStat sub-steps and the link/J
+ * sub-steps are two kernels working in place; with the one-pass method each step is one kernel
+ * that reads the links and currents of time t from one set of buffers and writes those of t+dt
+ * to a second set, which the handle allocates on first use and swaps with the first after every
+ * step.  Both give bit-identical fields.  SaveOldLink runs when GLASMA_STEP_SAVE_UOLD is set (for
+ * the last step of the call, which leaves UOld exactly as the reference leaves it). */
 int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags);
 
-/* glasma_step with CUDA events recorded on the handle's stream around each of the two
- * kernels of every step; kernel_ms[0] / kernel_ms[1] receive the summed milliseconds of the
- * electric-field/JStat kernel and of the link/J kernel.  Waits for the last event. */
+/* Step method of the handle: GLASMA_STEP_TWO_PASS (default, no extra memory) or
+ * GLASMA_STEP_ONE_PASS (half the HBM traffic per step, 2 x (U + 4 currents) per site more memory;
+ * falls back to two-pass for a call when the second buffer set cannot be allocated).
+ * glasma_get_step_method reports the method the last glasma_step call used. */
+#define GLASMA_STEP_ONE_PASS 0
+#define GLASMA_STEP_TWO_PASS 1
+int glasma_set_step_method(glasma_lattice* h, int method);
+int glasma_get_step_method(glasma_lattice* h, int* method);
+
+/* glasma_step with CUDA events recorded on the handle's stream around the kernels of every
+ * step; kernel_ms[0] / kernel_ms[1] receive the summed milliseconds of the electric-field/JStat
+ * kernel and of the link/J kernel (two-pass), or of the one-pass kernel and 0 (one-pass).
+ * Waits for the last event. */
 int glasma_step_profiled(glasma_lattice* h, double dt, int nsteps, unsigned flags, double* kernel_ms);
 
 /* The individual sub-steps, each with the reference's ghost synchronisation:
@@ -165,8 +182,9 @@ const char* glasma_mv_last_error(void);
  * Box-Muller), ghost slices synced.  Same seed, same fields.  No reference counterpart. */
 int glasma_fill_synthetic(glasma_lattice* h, unsigned long long seed, double link_amp, double e_amp, double j_amp);
 
-/* Autotuner: times the electric-field kernel (computing, storing nothing) for each block tile
- * shape tile_x x (128/tile_x) sites of a z slice and keeps the fastest for this lattice;
+/* Autotuner: times the step kernel of the handle's step method (the one-pass kernel, or the
+ * electric-field kernel of the two-pass method), computing and storing nothing, for each block
+ * tile shape tile_x x (128/tile_x) sites of a z slice and keeps the fastest for this lattice;
  * *tile_x (may be NULL) receives it.  glasma_set_tile sets it by hand (tile_x divides 128). */
 int glasma_autotune(glasma_lattice* h, double dt, int* tile_x);
 int glasma_set_tile(glasma_lattice* h, int tile_x);
@@ -177,6 +195,9 @@ int glasma_set_tile(glasma_lattice* h, int tile_x);
  * fftw_plan_many_dft as S/FFT/FFT3D.cpp:126-138 uses it.  `in` and `out` may be host or device
  * pointers. */
 int glasma_fft3d(glasma_lattice* h, const double* in, double* out, int inverse);
+/* The same transform in FP32 (8 planes of complex floats, interleaved re/im), as the gauge fixer
+ * runs it with GLASMA_GF_FFT_FP32. */
+int glasma_fft3d_f32(glasma_lattice* h, const float* in, float* out, int inverse);
 
 /* Gauss-law violation with no device allocation.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc -- code running while another framework captures a

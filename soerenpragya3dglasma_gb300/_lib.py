@@ -18,6 +18,7 @@ FP64, FP32 = 0, 1
 FIELDS = {"U": 0, "UOld": 1, "E": 2, "Jp": 3, "Jm": 4, "JpStat": 5, "JmStat": 6, "G": 7, "UG": 8, "EG": 9}
 STEP_SAVE_UOLD = 0x1
 GF_PROJECT_ZERO_MODE = 0x1
+GF_FFT_FP32 = 0x2
 
 # (name, restype, argtypes) for every symbol declared in include/glasma_gb300.h
 _H = ctypes.c_void_p
@@ -37,6 +38,8 @@ SIGNATURES = [
     ("glasma_download_device", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p]),
     ("glasma_step", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_uint]),
     ("glasma_step_profiled", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_uint, _D]),
+    ("glasma_set_step_method", ctypes.c_int, [_H, ctypes.c_int]),
+    ("glasma_get_step_method", ctypes.c_int, [_H, _I]),
     ("glasma_update_efield", ctypes.c_int, [_H, ctypes.c_double]),
     ("glasma_update_jstat", ctypes.c_int, [_H, ctypes.c_double]),
     ("glasma_update_links", ctypes.c_int, [_H, ctypes.c_double]),
@@ -58,6 +61,7 @@ SIGNATURES = [
     ("glasma_autotune", ctypes.c_int, [_H, ctypes.c_double, _I]),
     ("glasma_set_tile", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_fft3d", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    ("glasma_fft3d_f32", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("glasma_gauss_noalloc", ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("glasma_objective", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _D, _D, _D]),

@@ -89,6 +89,7 @@ struct glasma_batch {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_dt = NAN;
+  std::vector<unsigned long long> swaps;  // each event's buffer-swap count when the table was built
 };
 
 namespace {
@@ -152,6 +153,8 @@ int build_descriptors(glasma_batch* b, double dt) {
   }
   b->k1_total = k1;
   b->k2_total = k2;
+  b->swaps.clear();
+  for (glasma_lattice* h : b->ev) b->swaps.push_back(h->swaps);
   const size_t bytes = sizeof(EventDesc<T>) * d.size();
   if (!b->d_desc) {
     cudaError_t e = cudaMalloc(&b->d_desc, bytes);
@@ -305,7 +308,9 @@ int glasma_batch_step(glasma_batch* b, double dt, int nsteps, int use_graph) {
   if (!b || nsteps < 0) return bfail(GLASMA_ERR_INVALID_ARGUMENT, "bad arguments");
   if (nsteps == 0) return GLASMA_OK;
   int st;
-  if (!(b->desc_dt == dt)) {
+  bool stale = b->swaps.size() != b->ev.size();  // an event stepped on its own swapped its buffers
+  for (size_t i = 0; !stale && i < b->ev.size(); i++) stale = b->swaps[i] != b->ev[i]->swaps;
+  if (!(b->desc_dt == dt) || stale) {
     st = b->precision == GLASMA_FP64 ? build_descriptors<double>(b, dt) : build_descriptors<float>(b, dt);
     if (st != GLASMA_OK) return st;
     if (b->graph) {

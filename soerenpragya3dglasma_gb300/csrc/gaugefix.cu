@@ -15,13 +15,18 @@
 // The ghost slices of UG are never written (the reference's gauge-fixed container keeps the
 // identity it was created with), so the backward z link at z = 0 is the identity.
 //
-// All arithmetic is FP64; G / UG / EG are stored in the handle's precision.
+// All arithmetic is FP64 (G / UG / EG are stored in the handle's precision), except that with
+// GLASMA_GF_FFT_FP32 the two transforms of the acceleration step run in FP32: they only
+// precondition the step, so the iteration still converges to the same gauge, measured in FP64.
 //
-// FFT: the 3D transform is three passes of batched 1D transforms along x, y and z over the
-// colour-major array X[a][z][y][x] (complex double).  A block stages a tile of lines in shared
-// memory (consecutive lines for the x pass; for the y and z passes a tile of consecutive x, so
-// every global access is a contiguous run), transforms it there and writes it back in place:
-// radix-2 decimation in time for power-of-two lengths, a direct DFT otherwise.
+// FFT: the gradient Delta^a is real, so colours (2q, 2q+1) travel as one complex plane
+// X[q] = Delta^{2q} + i Delta^{2q+1}: four complex 3D transforms per direction instead of the
+// reference's eight (the real factor, even in p, keeps the two colours apart on the way back).
+// A 3D transform is three passes of batched 1D transforms along x, y and z over X[q][z][y][x].
+// A block stages a tile of lines in shared memory (consecutive lines for the x pass; for the y
+// and z passes a tile of consecutive x, so every global access is a contiguous run), transforms it
+// there and writes it back in place: radix-2 decimation in time for power-of-two lengths, a direct
+// DFT otherwise.  On GB300 the FP64 transform is bound by the FP64 pipe, not by HBM.
 #include <map>
 #include <vector>
 
@@ -65,6 +70,9 @@ __device__ __forceinline__ void st_d(cx<T>* __restrict__ U, long long S, long lo
   }
 }
 
+__device__ __forceinline__ double2 cmk(double r, double i) { return make_double2(r, i); }
+__device__ __forceinline__ float2 cmk(float r, float i) { return make_float2(r, i); }
+
 __device__ __forceinline__ long long nbr(const Geometry& g, int x, int y, int z, int dx, int dy, int dz) {
   int xx = x + dx, yy = y + dy;
   xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
@@ -72,10 +80,13 @@ __device__ __forceinline__ long long nbr(const Geometry& g, int x, int y, int z,
   return site_index(g, xx, yy, z + dz);
 }
 
-// ---- deviation: X = Delta (imaginary part 0); partials {max|Delta|, sum Delta^2, min ReTr w, sum ReTr w}
-template <typename T>
+// ---- deviation: X[q] = Delta^{2q} + i Delta^{2q+1}, q < 4 (Delta is real: two colours share one
+// complex transform, and since the acceleration multiplies by a real factor even in p, the inverse
+// transform returns them in the real and imaginary parts); partials {max|Delta|, sum Delta^2,
+// min ReTr w, sum ReTr w}
+template <typename T, typename C>
 __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const cx<T>* UG, double c0, double c1,
-                                                               double c2, double2* X, double* partials) {
+                                                               double c2, C* X, double* partials) {
   double v[4] = {0.0, 0.0, 1.0e300, 0.0};
   const int op[4] = {1, 0, 2, 0};
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
@@ -107,8 +118,10 @@ __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const
     for (int a = 0; a < 8; a++) {
       v[0] = fmax(v[0], fabs(dev.a[a]));
       v[1] += dev.a[a] * dev.a[a];
-      X[(long long)a * g.vol + idx] = make_double2(dev.a[a], 0.0);
     }
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      X[(long long)q * g.vol + idx] = cmk((decltype(C::x))dev.a[2 * q], (decltype(C::x))dev.a[2 * q + 1]);
     const double lf = w.e[0].re + w.e[4].re + w.e[8].re;
     v[2] = fmin(v[2], lf);
     v[3] += lf;
@@ -116,11 +129,12 @@ __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const
   red::block_reduce_store<4>(v, op, partials + (long long)blockIdx.x * 4);
 }
 
-// ---- momentum-space acceleration
-__global__ void accelerate_kernel(int nx, int ny, int nz, double ax, double ay, double az, double2* X, int project_zero) {
+// ---- momentum-space acceleration of the 4 colour-pair planes
+template <typename C>
+__global__ void accelerate_kernel(int nx, int ny, int nz, double ax, double ay, double az, C* X, int project_zero) {
   const long long V = (long long)nx * ny * nz;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 8 * V) return;
+  if (i >= 4 * V) return;
   const long long site = i % V;
   const long long r = site / nx;
   const int px = (int)(site - r * nx), pz = (int)(r / ny), py = (int)(r - (long long)pz * ny);
@@ -129,18 +143,18 @@ __global__ void accelerate_kernel(int nx, int ny, int nz, double ax, double ay, 
                     (2.0 - 2.0 * cospi(2.0 * pz / (double)nz)) / (az * az);
   if (p2 > 0.0) {
     const double f = 1.0 / ((double)V * p2);
-    double2 v = X[i];
+    C v = X[i];
     v.x *= f;
     v.y *= f;
     X[i] = v;
   } else if (project_zero) {
-    X[i] = make_double2(0.0, 0.0);
+    X[i] = cmk((decltype(C::x))0, (decltype(C::x))0);
   }
 }
 
 // ---- update of G; partials {max step, sum step^2, guard count}
-template <typename T>
-__global__ void __launch_bounds__(kGfThreads) update_kernel(Geometry g, const double2* X, cx<T>* G, double alpha,
+template <typename T, typename C>
+__global__ void __launch_bounds__(kGfThreads) update_kernel(Geometry g, const C* X, cx<T>* G, double alpha,
                                                             double* partials) {
   double v[3] = {0.0, 0.0, 0.0};
   const int op[3] = {1, 0, 0};
@@ -148,7 +162,11 @@ __global__ void __launch_bounds__(kGfThreads) update_kernel(Geometry g, const do
        idx += (long long)gridDim.x * blockDim.x) {
     Alg<double> upd;
 #pragma unroll
-    for (int a = 0; a < 8; a++) upd.a[a] = X[(long long)a * g.vol + idx].x;
+    for (int q = 0; q < 4; q++) {
+      const C v = X[(long long)q * g.vol + idx];
+      upd.a[2 * q] = (double)v.x;
+      upd.a[2 * q + 1] = (double)v.y;
+    }
     Mat<double> wt, gm, gn;
     expi(-alpha, upd, wt);
     // the reference's guard (CoulombGaugeDeviation.cpp:57-68); written so that a NaN also trips it
@@ -211,11 +229,96 @@ __global__ void twiddle_kernel(double2* tw, int n, int count) {
   sincospi(-2.0 * (double)k / (double)n, &s, &c);
   tw[k] = make_double2(c, s);
 }
+__global__ void twiddle_narrow_kernel(const double2* tw, float2* out, int count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < count) out[k] = make_float2((float)tw[k].x, (float)tw[k].y);
+}
 
-// Element (line l, k) of a batch of 1D transforms of length n, stride st:
+// Radix-2 decimation in time over a tile of 2^log_tl lines of length 2^logn staged in shared
+// memory, with the twiddles (rows padded to n+1 values against bank conflicts).  Element k of
+// line t of tile `tile`:
+//   st == 1 : X[base + t*n + k],  base = tile * 2^log_tl * n            (consecutive lines)
+//   st  > 1 : X[base + t + k*st], base = o*st*n + i0, (o, i0) from tile (consecutive inner index)
+// so every global access is a contiguous run.  Shifts only: n and the tile height are powers of 2.
+template <typename C>
+__global__ void __launch_bounds__(kFftThreads) fft_pow2_kernel(C* X, int logn, long long st, int log_tl,
+                                                               long long tiles_per_row, const C* __restrict__ tw,
+                                                               int inverse) {
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  const int n = 1 << logn, half_n = n >> 1, tl = 1 << log_tl, pitch = n + 1;
+  C* tws = reinterpret_cast<C*>(fft_smem);
+  C* sm = tws + half_n;
+  for (int k = threadIdx.x; k < half_n; k += blockDim.x) {
+    C w = tw[k];
+    if (inverse) w.y = -w.y;
+    tws[k] = w;
+  }
+  const long long tile = blockIdx.x;
+  long long base, lstride, kstride;
+  if (st == 1) {
+    base = (tile << log_tl) << logn;
+    lstride = n;
+    kstride = 1;
+  } else {
+    const long long o = tile / tiles_per_row;
+    base = o * st * n + ((tile - o * tiles_per_row) << log_tl);
+    lstride = 1;
+    kstride = st;
+  }
+  const int total = tl << logn;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int t, k;
+    if (st == 1) {
+      t = idx >> logn;
+      k = idx & (n - 1);
+    } else {
+      t = idx & (tl - 1);
+      k = idx >> log_tl;
+    }
+    const int rk = (int)(__brev((unsigned)k) >> (32 - logn));
+    sm[t * pitch + rk] = X[base + t * lstride + k * kstride];
+  }
+  __syncthreads();
+  const int nbfly = tl << (logn - 1);
+  // stage 1: every twiddle is 1
+  for (int j = threadIdx.x; j < nbfly; j += blockDim.x) {
+    const int t = j >> (logn - 1), b = j & (half_n - 1);
+    const int i0 = t * pitch + 2 * b, i1 = i0 + 1;
+    const C a = sm[i0], c = sm[i1];
+    sm[i0] = cmk(a.x + c.x, a.y + c.y);
+    sm[i1] = cmk(a.x - c.x, a.y - c.y);
+  }
+  __syncthreads();
+  for (int s = 2; s <= logn; s++) {
+    const int hs = s - 1;
+    for (int j = threadIdx.x; j < nbfly; j += blockDim.x) {
+      const int t = j >> (logn - 1), b = j & (half_n - 1);
+      const int grp = b >> hs, pos = b & ((1 << hs) - 1);
+      const int i0 = t * pitch + (grp << s) + pos, i1 = i0 + (1 << hs);
+      const C w = tws[pos << (logn - s)];
+      const C a = sm[i0], c = sm[i1];
+      const auto tr = w.x * c.x - w.y * c.y, ti = w.x * c.y + w.y * c.x;
+      sm[i0] = cmk(a.x + tr, a.y + ti);
+      sm[i1] = cmk(a.x - tr, a.y - ti);
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int t, k;
+    if (st == 1) {
+      t = idx >> logn;
+      k = idx & (n - 1);
+    } else {
+      t = idx & (tl - 1);
+      k = idx >> log_tl;
+    }
+    X[base + t * lstride + k * kstride] = sm[t * pitch + k];
+  }
+}
+
+// Element (line l, k) of a batch of 1D transforms of length n, stride st (direct DFT path):
 //   st == 1 : l*n + k
 //   st  > 1 : o*st*n + i + k*st  with l = (o, i), i in [0, st)
-// A block owns `tw_lines` lines: consecutive l for st == 1, consecutive i for st > 1.
 __device__ __forceinline__ long long fft_addr(long long tile, int t, int k, int n, long long st, int tile_lines) {
   if (st == 1) return (tile * tile_lines + t) * (long long)n + k;
   const long long tiles_per_block = st / tile_lines;
@@ -224,57 +327,12 @@ __device__ __forceinline__ long long fft_addr(long long tile, int t, int k, int 
   return o * st * n + i + (long long)k * st;
 }
 
-__global__ void __launch_bounds__(kFftThreads) fft_pow2_kernel(double2* X, int n, int logn, long long st, int tile_lines,
-                                                               const double2* __restrict__ tw, int inverse) {
-  extern __shared__ double2 sm[];
-  const long long tile = blockIdx.x;
-  const int total = tile_lines * n;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    int t, k;
-    if (st == 1) {
-      t = idx / n;
-      k = idx - t * n;
-    } else {
-      t = idx % tile_lines;
-      k = idx / tile_lines;
-    }
-    const int rk = (int)(__brev((unsigned)k) >> (32 - logn));
-    sm[t * n + rk] = X[fft_addr(tile, t, k, n, st, tile_lines)];
-  }
-  __syncthreads();
-  const int halfn = n >> 1;
-  for (int s = 1; s <= logn; s++) {
-    const int half = 1 << (s - 1);
-    for (int j = threadIdx.x; j < tile_lines * halfn; j += blockDim.x) {
-      const int t = j / halfn, b = j - t * halfn;
-      const int grp = b >> (s - 1), pos = b & (half - 1);
-      const int i0 = t * n + (grp << s) + pos, i1 = i0 + half;
-      double2 w = tw[pos << (logn - s)];
-      if (inverse) w.y = -w.y;
-      const double2 a = sm[i0], c = sm[i1];
-      const double tr = w.x * c.x - w.y * c.y, ti = w.x * c.y + w.y * c.x;
-      sm[i0] = make_double2(a.x + tr, a.y + ti);
-      sm[i1] = make_double2(a.x - tr, a.y - ti);
-    }
-    __syncthreads();
-  }
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    int t, k;
-    if (st == 1) {
-      t = idx / n;
-      k = idx - t * n;
-    } else {
-      t = idx % tile_lines;
-      k = idx / tile_lines;
-    }
-    X[fft_addr(tile, t, k, n, st, tile_lines)] = sm[t * n + k];
-  }
-}
-
 // Direct DFT for lengths that are not powers of two; tw holds exp(-2 pi i k / n), k < n.
-__global__ void __launch_bounds__(kFftThreads) dft_kernel(double2* X, int n, long long st, int tile_lines,
-                                                          const double2* __restrict__ tw, int inverse) {
-  extern __shared__ double2 sm[];
+template <typename C>
+__global__ void __launch_bounds__(kFftThreads) dft_kernel(C* X, int n, long long st, int tile_lines,
+                                                          const C* __restrict__ tw, int inverse) {
+  extern __shared__ __align__(16) unsigned char fft_smem[];
+  C* sm = reinterpret_cast<C*>(fft_smem);
   const long long tile = blockIdx.x;
   const int total = tile_lines * n;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
@@ -286,15 +344,15 @@ __global__ void __launch_bounds__(kFftThreads) dft_kernel(double2* X, int n, lon
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     const int t = st == 1 ? idx / n : idx % tile_lines;
     const int k = st == 1 ? idx - t * n : idx / tile_lines;
-    double re = 0.0, im = 0.0;
+    decltype(C::x) re = 0, im = 0;
     for (int j = 0; j < n; j++) {
-      double2 w = tw[(int)(((long long)j * k) % n)];
+      C w = tw[(int)(((long long)j * k) % n)];
       if (inverse) w.y = -w.y;
-      const double2 a = sm[t * n + j];
+      const C a = sm[t * n + j];
       re += a.x * w.x - a.y * w.y;
       im += a.x * w.y + a.y * w.x;
     }
-    X[fft_addr(tile, t, k, n, st, tile_lines)] = make_double2(re, im);
+    X[fft_addr(tile, t, k, n, st, tile_lines)] = cmk(re, im);
   }
 }
 
@@ -304,29 +362,7 @@ int ilog2(int n) {
   while ((1 << l) < n) l++;
   return l;
 }
-
-}  // namespace
-
-double2* make_twiddles(int n, cudaStream_t stream) {
-  const int count = is_pow2(n) ? (n / 2 > 0 ? n / 2 : 1) : n;
-  double2* tw = nullptr;
-  if (cudaMalloc(&tw, sizeof(double2) * count) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  twiddle_kernel<<<(count + 255) / 256, 256, 0, stream>>>(tw, n, count);
-  return tw;
-}
-
-struct GaugeFixState {
-  Geometry g;
-  int precision = -1;
-  double2* X = nullptr;
-  std::map<int, double2*> twiddles;
-  std::vector<double> host_results;
-};
-
-namespace {
+int twiddle_count(int n) { return is_pow2(n) ? (n / 2 > 0 ? n / 2 : 1) : n; }
 
 int tile_lines_for(int n, long long st, long long nlines_total) {
   int cap = kFftMaxTile / n;
@@ -342,39 +378,79 @@ int tile_lines_for(int n, long long st, long long nlines_total) {
   return t;
 }
 
-cudaError_t fft_axis(GaugeFixState* s, int n, long long st, long long total, int inverse, cudaStream_t stream) {
-  return fft_lines(s->X, n, st, total, inverse, s->twiddles.at(n), stream);
-}
-
-}  // namespace
-
-cudaError_t fft_lines(double2* X, int n, long long st, long long total, int inverse, const double2* tw,
-                      cudaStream_t stream) {
+template <typename C>
+cudaError_t fft_lines_t(C* X, int n, long long st, long long total, int inverse, const C* tw, cudaStream_t stream) {
   const long long nlines = total / n;
   const int tl = tile_lines_for(n, st, nlines);
   const long long tiles = nlines / tl;
-  const size_t smem = (size_t)tl * n * sizeof(double2);
   if (is_pow2(n)) {
     if (n == 1) return cudaSuccess;
-    cudaFuncSetAttribute(fft_pow2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kFftMaxTile * 16 > smem ? kFftMaxTile * 16 : smem));
-    fft_pow2_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, n, ilog2(n), st, tl, tw, inverse);
+    const size_t smem = ((size_t)(n / 2) + (size_t)tl * (n + 1)) * sizeof(C);
+    cudaFuncSetAttribute(fft_pow2_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fft_pow2_kernel<C><<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, ilog2(n), st, ilog2(tl), st > 1 ? st / tl : 0,
+                                                                       tw, inverse);
   } else {
-    cudaFuncSetAttribute(dft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem > 48 * 1024 ? smem : 48 * 1024));
-    dft_kernel<<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, n, st, tl, tw, inverse);
+    const size_t smem = (size_t)tl * n * sizeof(C);
+    cudaFuncSetAttribute(dft_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(smem > 48 * 1024 ? smem : 48 * 1024));
+    dft_kernel<C><<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, n, st, tl, tw, inverse);
   }
   return cudaGetLastError();
 }
 
+}  // namespace
+
+double2* make_twiddles(int n, cudaStream_t stream) {
+  const int count = twiddle_count(n);
+  double2* tw = nullptr;
+  if (cudaMalloc(&tw, sizeof(double2) * count) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  twiddle_kernel<<<(count + 255) / 256, 256, 0, stream>>>(tw, n, count);
+  return tw;
+}
+
+cudaError_t fft_lines(double2* X, int n, long long st, long long total, int inverse, const double2* tw,
+                      cudaStream_t stream) {
+  return fft_lines_t<double2>(X, n, st, total, inverse, tw, stream);
+}
+
+struct GaugeFixState {
+  Geometry g;
+  int precision = -1;
+  void* X = nullptr;  // 8 V complex doubles: the gauge update uses 4 colour-pair planes of it
+  std::map<int, double2*> twiddles;
+  std::map<int, float2*> twiddles32;
+  std::vector<double> host_results;
+};
+
 namespace {
 
-// 3D transform of the 8 colour planes of X
-cudaError_t fft3d(GaugeFixState* s, int inverse, cudaStream_t stream) {
+// 3D transform (unnormalised) of `planes` planes X[p][z][y][x]: three passes of batched 1D transforms
+template <typename C>
+cudaError_t fft3d_t(const GaugeFixState* s, C* X, int planes, int inverse, const std::map<int, C*>& tws,
+                    cudaStream_t stream) {
   const Geometry& g = s->g;
-  const long long total = 8 * g.vol;
-  cudaError_t e = fft_axis(s, g.nx, 1, total, inverse, stream);
-  if (e == cudaSuccess) e = fft_axis(s, g.ny, g.nx, total, inverse, stream);
-  if (e == cudaSuccess) e = fft_axis(s, g.nz, g.plane, total, inverse, stream);
+  const long long total = (long long)planes * g.vol;
+  cudaError_t e = fft_lines_t<C>(X, g.nx, 1, total, inverse, tws.at(g.nx), stream);
+  if (e == cudaSuccess) e = fft_lines_t<C>(X, g.ny, g.nx, total, inverse, tws.at(g.ny), stream);
+  if (e == cudaSuccess) e = fft_lines_t<C>(X, g.nz, g.plane, total, inverse, tws.at(g.nz), stream);
   return e;
+}
+
+// FP32 twiddles, narrowed from the FP64 ones on first use
+cudaError_t ensure_twiddles32(GaugeFixState* s, cudaStream_t stream) {
+  for (auto& kv : s->twiddles) {
+    if (s->twiddles32.count(kv.first)) continue;
+    const int count = twiddle_count(kv.first);
+    float2* tw = nullptr;
+    cudaError_t e = cudaMalloc(&tw, sizeof(float2) * count);
+    if (e != cudaSuccess) return e;
+    twiddle_narrow_kernel<<<(count + 255) / 256, 256, 0, stream>>>(kv.second, tw, count);
+    s->twiddles32[kv.first] = tw;
+  }
+  return cudaGetLastError();
 }
 
 int prepare(GaugeFixState** ps, const GaugeFixArgs& a, std::string* err) {
@@ -458,17 +534,34 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
   int n = 0;
   int status = GLASMA_OK;
   const double minf0 = 2.0 * 3 * (1.0 / (g.a[0] * g.a[0]) + 1.0 / (g.a[1] * g.a[1]) + 1.0 / (g.a[2] * g.a[2]));
+  const bool fft32 = (flags & GLASMA_GF_FFT_FP32) != 0;
+  if (fft32 && (e = ensure_twiddles32(s, st)) != cudaSuccess) return cuda_err(e, "FP32 twiddles");
+  double2* X64 = static_cast<double2*>(s->X);
+  float2* X32 = static_cast<float2*>(s->X);
+  const long long tot = 4 * g.vol;
+  const int project = (flags & GLASMA_GF_PROJECT_ZERO_MODE) ? 1 : 0;
   while (n < max_iters && gmax > tol) {
-    deviation_kernel<T><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], s->X, part_dev);
+    if (fft32)
+      deviation_kernel<T, float2><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], X32, part_dev);
+    else
+      deviation_kernel<T, double2><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], X64, part_dev);
     red::finish_kernel<4><<<1, red::kThreads, 0, st>>>(part_dev, (int)nb, 1 | (0 << 2) | (2 << 4) | (0 << 6), res);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "deviation");
-    if ((e = fft3d(s, 0, st)) != cudaSuccess) return cuda_err(e, "fft forward");
-    const long long tot = 8 * g.vol;
-    accelerate_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2], s->X,
-                                                                     (flags & GLASMA_GF_PROJECT_ZERO_MODE) ? 1 : 0);
+    e = fft32 ? fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 0, s->twiddles, st);
+    if (e != cudaSuccess) return cuda_err(e, "fft forward");
+    if (fft32)
+      accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2],
+                                                                                X32, project);
+    else
+      accelerate_kernel<double2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1],
+                                                                                 g.a[2], X64, project);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
-    if ((e = fft3d(s, 1, st)) != cudaSuccess) return cuda_err(e, "fft backward");
-    update_kernel<T><<<nb, kGfThreads, 0, st>>>(g, s->X, G, alpha, part_upd);
+    e = fft32 ? fft3d_t<float2>(s, X32, 4, 1, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 1, s->twiddles, st);
+    if (e != cudaSuccess) return cuda_err(e, "fft backward");
+    if (fft32)
+      update_kernel<T, float2><<<nb, kGfThreads, 0, st>>>(g, X32, G, alpha, part_upd);
+    else
+      update_kernel<T, double2><<<nb, kGfThreads, 0, st>>>(g, X64, G, alpha, part_upd);
     red::finish_kernel<3><<<1, red::kThreads, 0, st>>>(part_upd, (int)nb, 1 | (0 << 2) | (0 << 4), res + 4);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "update");
     if ((e = transform_links()) != cudaSuccess) return cuda_err(e, "transform links");
@@ -523,6 +616,7 @@ void gaugefix_destroy(GaugeFixState* s) {
   if (!s) return;
   if (s->X) cudaFree(s->X);
   for (auto& kv : s->twiddles) cudaFree(kv.second);
+  for (auto& kv : s->twiddles32) cudaFree(kv.second);
   delete s;
 }
 
@@ -533,7 +627,26 @@ int gaugefix_fft_test(GaugeFixState** state, const GaugeFixArgs& a, const double
   if (st != GLASMA_OK) return st;
   const size_t bytes = sizeof(double2) * 8 * a.g.vol;
   cudaError_t e = cudaMemcpyAsync((*state)->X, in, bytes, cudaMemcpyDefault, a.stream);
-  if (e == cudaSuccess) e = fft3d(*state, inverse, a.stream);
+  if (e == cudaSuccess)
+    e = fft3d_t<double2>(*state, static_cast<double2*>((*state)->X), 8, inverse, (*state)->twiddles, a.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, (*state)->X, bytes, cudaMemcpyDefault, a.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(a.stream);
+  if (e != cudaSuccess) {
+    *err = cudaGetErrorString(e);
+    return GLASMA_ERR_CUDA;
+  }
+  return GLASMA_OK;
+}
+
+int gaugefix_fft_test_f32(GaugeFixState** state, const GaugeFixArgs& a, const float2* in, float2* out, int inverse,
+                          std::string* err) {
+  int st = prepare(state, a, err);
+  if (st != GLASMA_OK) return st;
+  const size_t bytes = sizeof(float2) * 8 * a.g.vol;
+  cudaError_t e = ensure_twiddles32(*state, a.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync((*state)->X, in, bytes, cudaMemcpyDefault, a.stream);
+  if (e == cudaSuccess)
+    e = fft3d_t<float2>(*state, static_cast<float2*>((*state)->X), 8, inverse, (*state)->twiddles32, a.stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, (*state)->X, bytes, cudaMemcpyDefault, a.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(a.stream);
   if (e != cudaSuccess) {

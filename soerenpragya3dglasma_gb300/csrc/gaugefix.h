@@ -39,5 +39,7 @@ double2* make_twiddles(int n, cudaStream_t stream);
 // `in` / `out` may be host or device memory.
 int gaugefix_fft_test(GaugeFixState** state, const GaugeFixArgs& a, const double2* in, double2* out, int inverse,
                       std::string* err);
+int gaugefix_fft_test_f32(GaugeFixState** state, const GaugeFixArgs& a, const float2* in, float2* out, int inverse,
+                          std::string* err);
 
 }  // namespace glasma

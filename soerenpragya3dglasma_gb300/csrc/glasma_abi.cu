@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/glasma_gb300.h"
@@ -74,6 +75,46 @@ FieldPtrs<T> ptrs(glasma_lattice* h) {
   p.JpStat = static_cast<T*>(h->f[GLASMA_FIELD_JPSTAT]);
   p.JmStat = static_cast<T*>(h->f[GLASMA_FIELD_JMSTAT]);
   return p;
+}
+
+// Buffers of the one-pass step's second set: the fields it writes (U, the four currents).
+constexpr int kSwapFields[5] = {GLASMA_FIELD_U, GLASMA_FIELD_JP, GLASMA_FIELD_JM, GLASMA_FIELD_JPSTAT,
+                                GLASMA_FIELD_JMSTAT};
+
+// FieldPtrs of the second set: E and UOld are shared with the first.
+template <typename T>
+FieldPtrs<T> alt_ptrs(glasma_lattice* h) {
+  FieldPtrs<T> p = ptrs<T>(h);
+  p.U = static_cast<cx<T>*>(h->alt[GLASMA_FIELD_U]);
+  p.Jp = static_cast<T*>(h->alt[GLASMA_FIELD_JP]);
+  p.Jm = static_cast<T*>(h->alt[GLASMA_FIELD_JM]);
+  p.JpStat = static_cast<T*>(h->alt[GLASMA_FIELD_JPSTAT]);
+  p.JmStat = static_cast<T*>(h->alt[GLASMA_FIELD_JMSTAT]);
+  return p;
+}
+
+// Allocates the second set (contents need no initialisation: every step writes all of it, ghost
+// slices included).  False, with nothing left allocated, when device memory is short.
+bool ensure_alt(glasma_lattice* h) {
+  for (int f : kSwapFields) {
+    if (h->alt[f]) continue;
+    void* p = nullptr;
+    if (cudaMalloc(&p, field_bytes(h, f)) != cudaSuccess) {
+      cudaGetLastError();
+      for (int k : kSwapFields) {
+        if (h->alt[k]) cudaFree(h->alt[k]);
+        h->alt[k] = nullptr;
+      }
+      return false;
+    }
+    h->alt[f] = p;
+  }
+  return true;
+}
+
+void swap_buffers(glasma_lattice* h) {
+  for (int f : kSwapFields) std::swap(h->f[f], h->alt[f]);
+  h->swaps++;
 }
 
 // identity links / zero fields, ghost slices included
@@ -187,6 +228,27 @@ int step_impl(glasma_lattice* h, double dt, int nsteps, unsigned flags, cudaEven
   // the fused kernels keep every ghost slice in sync after that.
   cudaError_t e = glasma::launch_sync_ghosts<cx<T>>(h->g, p.U, 27, h->stream);
   if (e != cudaSuccess) return cuda_fail(e, "ghost sync U");
+  if (h->step_method == GLASMA_STEP_ONE_PASS && ensure_alt(h)) {
+    h->last_method = GLASMA_STEP_ONE_PASS;
+    for (int n = 0; n < nsteps; n++) {
+      if (ev) cudaEventRecord(ev[3 * n], h->stream);
+      const bool save = (flags & GLASMA_STEP_SAVE_UOLD) && (n == nsteps - 1);
+      e = glasma::launch_fused_step<T>(h->g, ptrs<T>(h), alt_ptrs<T>(h), dt, save, h->tile_x, false, h->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "fused step");
+      if (ev) {
+        cudaEventRecord(ev[3 * n + 1], h->stream);
+        cudaEventRecord(ev[3 * n + 2], h->stream);
+      }
+      swap_buffers(h);
+      h->steps_done++;
+      if (h->reunit_every > 0 && h->steps_done % h->reunit_every == 0) {
+        e = glasma::launch_reunitarize<T>(h->g, static_cast<cx<T>*>(h->f[GLASMA_FIELD_U]), h->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "reunitarize");
+      }
+    }
+    return GLASMA_OK;
+  }
+  h->last_method = GLASMA_STEP_TWO_PASS;
   for (int n = 0; n < nsteps; n++) {
     if (ev) cudaEventRecord(ev[3 * n], h->stream);
     e = glasma::launch_efield_jstat<T>(h->g, p, dt, h->tile_x, h->stream);
@@ -251,6 +313,8 @@ int glasma_create(int nx, int ny, int nz, double ax, double ay, double az, int p
   h->a_scale = 1.0;
   h->real_bytes = precision == GLASMA_FP64 ? 8 : 4;
   h->tile_x = glasma::default_tile_x(nx);
+  h->step_method = GLASMA_STEP_TWO_PASS;  // faster on GB300 while the step is bound by arithmetic issue
+  h->last_method = GLASMA_STEP_TWO_PASS;
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -278,8 +342,10 @@ int glasma_destroy(glasma_lattice* h) {
   if (!h) return GLASMA_OK;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  for (int i = 0; i < 10; i++)
+  for (int i = 0; i < 10; i++) {
     if (h->f[i]) cudaFree(h->f[i]);
+    if (h->alt[i]) cudaFree(h->alt[i]);
+  }
   if (h->staging) cudaFree(h->staging);
   if (h->scratch) cudaFree(h->scratch);
   glasma::gaugefix_destroy(h->gf);
@@ -372,6 +438,28 @@ int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags) {
   if (flags & ~GLASMA_STEP_SAVE_UOLD) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown step flag");
   if (nsteps == 0) return GLASMA_OK;
   return h->precision == GLASMA_FP64 ? step_impl<double>(h, dt, nsteps, flags) : step_impl<float>(h, dt, nsteps, flags);
+}
+
+int glasma_set_step_method(glasma_lattice* h, int method) {
+  GLASMA_CHECK_HANDLE(h);
+  if (method != GLASMA_STEP_ONE_PASS && method != GLASMA_STEP_TWO_PASS)
+    return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown step method");
+  h->step_method = method;
+  if (method == GLASMA_STEP_TWO_PASS) {  // give the second buffer set back
+    GLASMA_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+    for (int f : kSwapFields) {
+      if (h->alt[f]) cudaFree(h->alt[f]);
+      h->alt[f] = nullptr;
+    }
+  }
+  return GLASMA_OK;
+}
+
+int glasma_get_step_method(glasma_lattice* h, int* method) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!method) return fail(GLASMA_ERR_INVALID_ARGUMENT, "method is null");
+  *method = h->last_method;
+  return GLASMA_OK;
 }
 
 int glasma_step_profiled(glasma_lattice* h, double dt, int nsteps, unsigned flags, double* kernel_ms) {
@@ -584,7 +672,8 @@ int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double to
                        int* iterations) {
   GLASMA_CHECK_HANDLE(h);
   if (max_iters < 0) return fail(GLASMA_ERR_INVALID_ARGUMENT, "max_iters < 0");
-  if (flags & ~GLASMA_GF_PROJECT_ZERO_MODE) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown gauge-fixing flag");
+  if (flags & ~(GLASMA_GF_PROJECT_ZERO_MODE | GLASMA_GF_FFT_FP32))
+    return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown gauge-fixing flag");
   int st;
   for (int f : {GLASMA_FIELD_G, GLASMA_FIELD_UG, GLASMA_FIELD_EG})
     if ((st = ensure_field(h, f))) return st;
@@ -627,12 +716,31 @@ int glasma_fft3d(glasma_lattice* h, const double* in, double* out, int inverse) 
   return st == GLASMA_OK ? GLASMA_OK : fail(st, err);
 }
 
+int glasma_fft3d_f32(glasma_lattice* h, const float* in, float* out, int inverse) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!in || !out) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null buffer");
+  int st = ensure_scratch(h);
+  if (st) return st;
+  glasma::GaugeFixArgs a = {};
+  a.g = h->g;
+  a.precision = h->precision;
+  a.a_scale = h->a_scale;
+  a.stream = h->stream;
+  a.scratch = h->scratch;
+  a.scratch_doubles = h->scratch_doubles;
+  std::string err;
+  st = glasma::gaugefix_fft_test_f32(&h->gf, a, reinterpret_cast<const float2*>(in), reinterpret_cast<float2*>(out),
+                                     inverse ? 1 : 0, &err);
+  return st == GLASMA_OK ? GLASMA_OK : fail(st, err);
+}
+
 int glasma_autotune(glasma_lattice* h, double dt, int* tile_x) {
   GLASMA_CHECK_HANDLE(h);
   const int candidates[5] = {128, 64, 32, 16, 8};
   cudaEvent_t e0, e1;
   GLASMA_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
   GLASMA_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+  const bool one_pass = h->step_method == GLASMA_STEP_ONE_PASS && ensure_alt(h);
   float best = 1e30f;
   int best_tx = h->tile_x;
   for (int tx : candidates) {
@@ -640,8 +748,13 @@ int glasma_autotune(glasma_lattice* h, double dt, int* tile_x) {
     float total = 0.f;
     for (int rep = 0; rep < 4; rep++) {
       cudaEventRecord(e0, h->stream);
-      cudaError_t e = GLASMA_DISPATCH(h, glasma::launch_efield_dry<double>(h->g, ptrs<double>(h), dt, tx, h->stream),
-                                      glasma::launch_efield_dry<float>(h->g, ptrs<float>(h), dt, tx, h->stream));
+      cudaError_t e =
+          one_pass ? GLASMA_DISPATCH(h, glasma::launch_fused_step<double>(h->g, ptrs<double>(h), alt_ptrs<double>(h), dt,
+                                                                          false, tx, true, h->stream),
+                                     glasma::launch_fused_step<float>(h->g, ptrs<float>(h), alt_ptrs<float>(h), dt, false,
+                                                                      tx, true, h->stream))
+                   : GLASMA_DISPATCH(h, glasma::launch_efield_dry<double>(h->g, ptrs<double>(h), dt, tx, h->stream),
+                                     glasma::launch_efield_dry<float>(h->g, ptrs<float>(h), dt, tx, h->stream));
       cudaEventRecord(e1, h->stream);
       if (e != cudaSuccess) {
         cudaEventDestroy(e0);

@@ -23,6 +23,10 @@ struct glasma_lattice {
   size_t scratch_doubles;
   glasma::GaugeFixState* gf;
   int tile_x;         // K1 tile width along x (autotuned)
+  void* alt[10];      // second buffer set of the one-pass step (U, JP, JM, JPSTAT, JMSTAT; lazily)
+  int step_method;    // GLASMA_STEP_ONE_PASS / GLASMA_STEP_TWO_PASS
+  int last_method;    // method the last glasma_step used
+  unsigned long long swaps;  // buffer swaps so far (batched launches rebuild their tables on change)
 };
 
 namespace glasma {

@@ -82,6 +82,12 @@ cudaError_t launch_efield_dry(const Geometry& g, FieldPtrs<T> f, double dt, int 
 template <typename T>
 cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second_half,
                            cudaStream_t stream);
+// The whole step in one launch: reads U, J, JStat of time t from `in`, writes those of t+dt to `out`
+// (distinct buffers), E in place in in.E, UOld (when save_uold) in in.UOld.  Bit-identical to
+// launch_efield_jstat followed by launch_links_j.  dry: compute, store nothing (autotuner).
+template <typename T>
+cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, double dt, bool save_uold,
+                              int tile_x, bool dry, cudaStream_t stream);
 template <typename T>
 cudaError_t launch_sync_ghosts(const Geometry& g, T* base, int components, cudaStream_t stream);
 template <typename T>

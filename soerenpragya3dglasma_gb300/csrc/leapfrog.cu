@@ -40,6 +40,14 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
 }
 
 template <typename T, typename I>
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kFusedMinBlocks)
+    fused_step_kernel(Geometry g, FieldPtrs<T> in, FieldPtrs<T> out, EParams<T> pe, LParams<T> pl, TileMap tm) {
+  int x, y, z;
+  if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
+  fused_site<T, I>(g, in, out, pe, pl, x, y, z);
+}
+
+template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads) j_only_kernel(Geometry g, FieldPtrs<T> f, T cj) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
   if (idx >= (I)g.vol) return;
@@ -100,16 +108,31 @@ __global__ void copy_kernel(const E* __restrict__ src, E* __restrict__ dst, long
 
 inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// The stencil kernels use no shared memory: ask for the whole unified L1/shared array as L1 (their
+// neighbour links are re-read from L1).  Once per kernel and process.
+template <typename K>
+void prefer_l1(K kernel) {
+  static bool done = false;
+  if (!done) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaGetLastError();
+    done = true;
+  }
+}
+
 template <typename T>
 cudaError_t launch_efield_kernel(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, int tile_x,
                                  cudaStream_t stream) {
   if (tile_x <= 0 || tile_x > kThreads || kThreads % tile_x) tile_x = kThreads;
   const TileMap tm = TileMap::make(g.nx, g.ny, tile_x, kThreads);
   const unsigned grid = (unsigned)tm.tiles(g.nz);
-  if (use_32bit_index(g))
+  if (use_32bit_index(g)) {
+    prefer_l1(efield_jstat_kernel<T, int>);
     efield_jstat_kernel<T, int><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
-  else
+  } else {
+    prefer_l1(efield_jstat_kernel<T, long long>);
     efield_jstat_kernel<T, long long><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
+  }
   return cudaGetLastError();
 }
 
@@ -154,8 +177,7 @@ cudaError_t launch_jstat_only(const Geometry& g, FieldPtrs<T> f, double dt, int 
 }
 
 template <typename T>
-cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second,
-                           cudaStream_t stream) {
+LParams<T> make_lparams(const Geometry& g, double dt, bool save_uold, bool do_j, bool do_second) {
   LParams<T> p;
   const double a3 = g.a[0] * g.a[1] * g.a[2];
   for (int mu = 0; mu < 3; mu++) p.cU[mu] = (T)(-(0.5 * dt) * g.a[mu] * g.a[mu] / a3);
@@ -163,6 +185,31 @@ cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool sa
   p.save_uold = save_uold ? 1 : 0;
   p.do_j = do_j ? 1 : 0;
   p.do_second = do_second ? 1 : 0;
+  return p;
+}
+
+template <typename T>
+cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, double dt, bool save_uold,
+                              int tile_x, bool dry, cudaStream_t stream) {
+  if (tile_x <= 0 || tile_x > kThreads || kThreads % tile_x) tile_x = kThreads;
+  const TileMap tm = TileMap::make(g.nx, g.ny, tile_x, kThreads);
+  const unsigned grid = (unsigned)tm.tiles(g.nz);
+  const EParams<T> pe = make_eparams<T>(g, dt, 1, 1, dry ? 1 : 0);
+  const LParams<T> pl = make_lparams<T>(g, dt, save_uold, true, true);
+  if (use_32bit_index(g)) {
+    prefer_l1(fused_step_kernel<T, int>);
+    fused_step_kernel<T, int><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
+  } else {
+    prefer_l1(fused_step_kernel<T, long long>);
+    fused_step_kernel<T, long long><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second,
+                           cudaStream_t stream) {
+  const LParams<T> p = make_lparams<T>(g, dt, save_uold, do_j, do_second);
   if (use_32bit_index(g))
     links_j_kernel<T, int><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
   else
@@ -206,6 +253,8 @@ cudaError_t launch_copy_links(const Geometry& g, const cx<T>* src, cx<T>* dst, c
 }
 
 #define GLASMA_INSTANTIATE(T)                                                                                   \
+  template cudaError_t launch_fused_step<T>(const Geometry&, FieldPtrs<T>, FieldPtrs<T>, double, bool, int, bool, \
+                                            cudaStream_t);                                                      \
   template cudaError_t launch_efield_jstat<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);       \
   template cudaError_t launch_efield_dry<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);         \
   template cudaError_t launch_efield_only<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);        \

@@ -21,17 +21,22 @@ constexpr int kThreads = 128;
 #ifndef GLASMA_FP32_LINKS_MIN_BLOCKS
 #define GLASMA_FP32_LINKS_MIN_BLOCKS 8
 #endif
+#ifndef GLASMA_FP32_FUSED_MIN_BLOCKS
+#define GLASMA_FP32_FUSED_MIN_BLOCKS 4
+#endif
 template <typename T>
 struct Occupancy;
 template <>
 struct Occupancy<double> {
   static constexpr int kMinBlocks = GLASMA_FP64_MIN_BLOCKS;       // electric-field kernel
   static constexpr int kLinksMinBlocks = GLASMA_FP64_MIN_BLOCKS;  // link/J kernel
+  static constexpr int kFusedMinBlocks = GLASMA_FP64_MIN_BLOCKS;  // one-pass step kernel
 };
 template <>
 struct Occupancy<float> {
   static constexpr int kMinBlocks = GLASMA_FP32_MIN_BLOCKS;
   static constexpr int kLinksMinBlocks = GLASMA_FP32_LINKS_MIN_BLOCKS;
+  static constexpr int kFusedMinBlocks = GLASMA_FP32_FUSED_MIN_BLOCKS;
 };
 
 template <typename I>
@@ -48,6 +53,20 @@ __device__ __forceinline__ void decode(const Geometry& g, I idx, int& x, int& y,
   x = (int)(idx - r * (I)g.nx);
   z = (int)(r / (I)g.ny);
   y = (int)(r - (I)z * (I)g.ny);
+}
+
+// v[mu] for a runtime mu without indexing the kernel-parameter array (which would copy it to the stack)
+template <typename T>
+__device__ __forceinline__ T pick3(const T (&v)[3], int mu) {
+  return mu == 0 ? v[0] : (mu == 1 ? v[1] : v[2]);
+}
+
+// acc += c (a - b), componentwise: the update form of UpdateJStat and UpdateJ.  Every path (K1, K2,
+// the fused step) uses this one expression, so they round identically.
+template <typename T>
+__device__ __forceinline__ void axpy_diff(Alg<T>& acc, T c, const Alg<T>& a, const Alg<T>& b) {
+#pragma unroll
+  for (int k = 0; k < 8; k++) acc.a[k] += c * (a.a[k] - b.a[k]);
 }
 
 // Staples of link mu at x in the (mu,nu) plane, weighted by c, added to acc.
@@ -107,7 +126,7 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
       load_link(f.U, S, mu, s, u);
       mul_nn(u, acc, P);
       Alg<T> force, e;
-      retr_itg(P, p.gc[mu], force);
+      retr_itg(P, pick3(p.gc, mu), force);
       load_alg(f.E, S, mu * 8, s, e);
 #pragma unroll
       for (int a = 0; a < 8; a++) e.a[a] += force.a[a];
@@ -133,8 +152,7 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
     inv_adj_mul(uzm, jc, down);
     load_alg(f.Jp, S, 0, s, jc);
     load_alg(f.JpStat, S, 0, s, st);
-#pragma unroll
-    for (int a = 0; a < 8; a++) st.a[a] += -p.cj * (jc.a[a] - down.a[a]);
+    axpy_diff(st, -p.cj, jc, down);
     if (!p.dry) {
       store_alg(f.JpStat, S, 0, s, st);
       if (sg >= 0) store_alg(f.JpStat, S, 0, sg, st);
@@ -143,8 +161,7 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
     inv_adj_mul(uzm, jc, down);
     load_alg(f.Jm, S, 0, s, jc);
     load_alg(f.JmStat, S, 0, s, st);
-#pragma unroll
-    for (int a = 0; a < 8; a++) st.a[a] += p.cj * (jc.a[a] - down.a[a]);
+    axpy_diff(st, p.cj, jc, down);
     if (!p.dry) {
       store_alg(f.JmStat, S, 0, s, st);
       if (sg >= 0) store_alg(f.JmStat, S, 0, sg, st);
@@ -197,7 +214,7 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
     Alg<T> e;
     load_alg(f.E, S, mu * 8, s, e);
     Mat<T> X, u, uh;
-    expi(p.cU[mu], e, X);
+    expi(pick3(p.cU, mu), e, X);
     load_link(f.U, S, mu, s, u);
     mul_nn(X, u, uh);
     if (p.save_uold) {
@@ -211,16 +228,14 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
       adj_mul(uh, st, up);
       load_alg(f.JpStat, S, 0, s, st);
       load_alg(f.Jp, S, 0, s, j);
-#pragma unroll
-      for (int a = 0; a < 8; a++) j.a[a] += -p.cj * (up.a[a] - st.a[a]);
+      axpy_diff(j, -p.cj, up, st);
       store_alg(f.Jp, S, 0, s, j);
       if (sg >= 0) store_alg(f.Jp, S, 0, sg, j);
       load_alg(f.JmStat, S, 0, szp, st);
       adj_mul(uh, st, up);
       load_alg(f.JmStat, S, 0, s, st);
       load_alg(f.Jm, S, 0, s, j);
-#pragma unroll
-      for (int a = 0; a < 8; a++) j.a[a] += p.cj * (up.a[a] - st.a[a]);
+      axpy_diff(j, p.cj, up, st);
       store_alg(f.Jm, S, 0, s, j);
       if (sg >= 0) store_alg(f.Jm, S, 0, sg, j);
     }
@@ -234,6 +249,136 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
   }
 }
 
-// UpdateJ alone (S/DYNAMICS/SUNcDynamics.cpp:238-269) with the links as they stand.
+// ---- the whole step in one pass -------------------------------------------------------------------
+// fused_site reads the links, currents and static currents of time t from `in` and writes those of
+// t+dt to `out` (a second set of buffers; E is updated in place, it is read only at its own site).
+// Because nothing it reads is written in the same launch, the sites are independent and the step is
+// one launch.  The static currents of t+dt at x+z, which UpdateJ at x needs, are recomputed here from
+// the inputs with K1's own expression, so the result is bit-identical to K1 followed by K2.
+//   E_mu(x)      += force(U(t)) [+ J term]                          UpdateElectricFields
+//   JStat(x)     += -/+ cj (J(x) - U_z^d(x-z) J(x-z) U_z(x-z))      UpdateJStat (also at x+z)
+//   Uh            = exp(i cU E_mu(x)) U_mu(x)                        UpdateGaugeLinks(dt/2)
+//   J(x)         += -/+ cj (Uh_z J Stat(x+z) Uh_z^d - JStat(x))     UpdateJ
+//   U_mu(x; t+dt) = exp(i cU E_mu(x)) Uh                             UpdateGaugeLinks(dt/2)
+template <typename T, typename I>
+__device__ __forceinline__ void fused_currents(const FieldPtrs<T>& in, const FieldPtrs<T>& out, I S, I plane, I s,
+                                               I sg, bool hi, const Mat<T>& uz, const Mat<T>& uhz, T cj, bool dry) {
+  const I szm = s - plane, szp = s + plane;
+  Alg<T> jc, down, sp, sm;
+  {
+    Mat<T> w;
+    load_link(in.U, S, 2, szm, w);
+    load_alg(in.Jp, S, 0, szm, jc);
+    inv_adj_mul(w, jc, down);
+    load_alg(in.Jp, S, 0, s, jc);
+    load_alg(in.JpStat, S, 0, s, sp);
+    axpy_diff(sp, -cj, jc, down);
+    load_alg(in.Jm, S, 0, szm, jc);
+    inv_adj_mul(w, jc, down);
+    load_alg(in.Jm, S, 0, s, jc);
+    load_alg(in.JmStat, S, 0, s, sm);
+    axpy_diff(sm, cj, jc, down);
+  }
+  if (!dry) {
+    store_alg(out.JpStat, S, 0, s, sp);
+    store_alg(out.JmStat, S, 0, s, sm);
+    if (sg >= 0) {
+      store_alg(out.JpStat, S, 0, sg, sp);
+      store_alg(out.JmStat, S, 0, sg, sm);
+    }
+  }
+  // static currents of t+dt one slice up (the ghost copy of this site's at the top slice)
+  Alg<T> up, um;
+  if (hi) {
+    up = sp;
+    um = sm;
+  } else {
+    load_alg(in.Jp, S, 0, s, jc);
+    inv_adj_mul(uz, jc, down);
+    load_alg(in.Jp, S, 0, szp, jc);
+    load_alg(in.JpStat, S, 0, szp, up);
+    axpy_diff(up, -cj, jc, down);
+    load_alg(in.Jm, S, 0, s, jc);
+    inv_adj_mul(uz, jc, down);
+    load_alg(in.Jm, S, 0, szp, jc);
+    load_alg(in.JmStat, S, 0, szp, um);
+    axpy_diff(um, cj, jc, down);
+  }
+  Alg<T> t, j;
+  adj_mul(uhz, up, t);
+  load_alg(in.Jp, S, 0, s, j);
+  axpy_diff(j, -cj, t, sp);
+  if (!dry) {
+    store_alg(out.Jp, S, 0, s, j);
+    if (sg >= 0) store_alg(out.Jp, S, 0, sg, j);
+  }
+  adj_mul(uhz, um, t);
+  load_alg(in.Jm, S, 0, s, j);
+  axpy_diff(j, cj, t, sm);
+  if (!dry) {
+    store_alg(out.Jm, S, 0, s, j);
+    if (sg >= 0) store_alg(out.Jm, S, 0, sg, j);
+  }
+}
+
+template <typename T, typename I>
+__device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>& in, const FieldPtrs<T>& out,
+                                           const EParams<T>& pe, const LParams<T>& pl, int x, int y, int z) {
+  const I S = (I)g.S, plane = (I)g.plane;
+  const I s = (I)x + (I)g.nx * ((I)y + (I)g.ny * (I)(z + 1));
+  const bool lo = (z == 0), hi = (z == g.nz - 1);
+  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
+  const bool dry = pe.dry != 0;
+  const I sxp = nb<I>(g, x, y, z, 1, 0, 0), sxm = nb<I>(g, x, y, z, -1, 0, 0);
+  const I syp = nb<I>(g, x, y, z, 0, 1, 0), sym = nb<I>(g, x, y, z, 0, -1, 0);
+  const I szp = s + plane, szm = s - plane;
+#pragma unroll 1
+  for (int mu = 0; mu < 3; mu++) {
+    Mat<T> acc;
+    set_zero(acc);
+    if (mu == 0) {
+      add_staples(in.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, pe.cnu[1], acc);
+      add_staples(in.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, pe.cnu[2], acc);
+    } else if (mu == 1) {
+      add_staples(in.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, pe.cnu[0], acc);
+      add_staples(in.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, pe.cnu[2], acc);
+    } else {
+      add_staples(in.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, pe.cnu[0], acc);
+      add_staples(in.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, pe.cnu[1], acc);
+    }
+    Mat<T> u, w;
+    load_link(in.U, S, mu, s, u);
+    mul_nn(u, acc, w);
+    Alg<T> force, e;
+    retr_itg(w, pick3(pe.gc, mu), force);
+    load_alg(in.E, S, mu * 8, s, e);
+#pragma unroll
+    for (int a = 0; a < 8; a++) e.a[a] += force.a[a];
+    if (mu == 2) {
+      Alg<T> jp, jm;
+      load_alg(in.Jp, S, 0, s, jp);
+      load_alg(in.Jm, S, 0, s, jm);
+#pragma unroll
+      for (int a = 0; a < 8; a++) e.a[a] += pe.jz * (jp.a[a] - jm.a[a]);
+    }
+    if (!dry) {
+      store_alg(in.E, S, mu * 8, s, e);
+      if (sg >= 0) store_alg(in.E, S, mu * 8, sg, e);
+    }
+    Mat<T> X, uh;
+    expi(pick3(pl.cU, mu), e, X);
+    mul_nn(X, u, uh);
+    if (pl.save_uold && !dry) {
+      store_link(in.UOld, S, mu, s, uh);
+      if (sg >= 0) store_link(in.UOld, S, mu, sg, uh);
+    }
+    mul_nn(X, uh, w);
+    if (!dry) {
+      store_link(out.U, S, mu, s, w);
+      if (sg >= 0) store_link(out.U, S, mu, sg, w);
+    }
+    if (mu == 2) fused_currents<T, I>(in, out, S, plane, s, sg, hi, u, uh, pl.cj, dry);
+  }
+}
 
 }  // namespace glasma

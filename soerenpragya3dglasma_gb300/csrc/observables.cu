@@ -11,8 +11,15 @@
 //
 // Every reduction is two-pass and deterministic: a fixed grid writes FP64 block partials
 // (warp shuffles, then shared memory), a one-block pass sums them in a fixed order.
-// Site arithmetic runs in FP64 for both storage precisions, so an FP32 lattice is measured
-// without adding FP32 rounding to 3 - ReTr(P).
+// Site arithmetic runs in FP64, except the magnetic term of the bulk energy on FP32 lattices,
+// which uses the identity (exact for any matrices)
+//   3 - ReTr(a b c^d d^d) = 1/2 ||A - B||^2 - 1/2 (n(a) + n(b) + n(c) + n(d)),
+//   A = a b, B = d c, n(u) = ||u||_F^2 - 3  (zero for unitary u):
+// A, B and ||A - B||^2 are formed in FP32, whose rounding then costs about 1e-7 ||A - B|| per
+// plaquette instead of 1e-7 (no cancellation against 3, so weak fields keep their digits), and the
+// norm terms are summed in FP64 per link (each link's n counted for the plaquettes it belongs to).
+#include <type_traits>
+
 #include "lattice.cuh"
 
 namespace glasma {
@@ -128,6 +135,37 @@ __device__ __forceinline__ void plaq_uudd(const Mat<double>& a, const Mat<double
   mul_nn(t1, t2, out);
 }
 
+// ||A - B||^2 of the plaquette a b (d c)^d in the (j,k) plane, A = U_j(x) U_k(x+j), B = U_k(x) U_j(x+k), FP32
+__device__ __forceinline__ float plaq_sqdiff_f(const cx<float>* __restrict__ U, long long S, int j, int k,
+                                               long long s, long long sj, long long sk) {
+  Mat<float> a, b, A, B;
+  load_link<float, long long>(U, S, j, s, a);
+  load_link<float, long long>(U, S, k, sj, b);
+  mul_nn(a, b, A);
+  load_link<float, long long>(U, S, k, s, a);
+  load_link<float, long long>(U, S, j, sk, b);
+  mul_nn(a, b, B);
+  float d2 = 0.f;
+#pragma unroll
+  for (int e = 0; e < 9; e++) {
+    const float dr = A.e[e].re - B.e[e].re, di = A.e[e].im - B.e[e].im;
+    d2 = fmaf(dr, dr, fmaf(di, di, d2));
+  }
+  return d2;
+}
+
+// n(u) = ||u||_F^2 - 3 in FP64 (every float x float product is exact in FP64)
+__device__ __forceinline__ double link_norm_dev(const cx<float>* __restrict__ U, long long S, int mu, long long s) {
+  const cx<float>* p = U + (long long)(mu * 9) * S + s;
+  double n = -3.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const cx<float> v = p[(long long)k * S];
+    n = fma((double)v.re, (double)v.re, fma((double)v.im, (double)v.im, n));
+  }
+  return n;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) bulk_kernel(Geometry g, FieldPtrs<T> f, double* partials) {
   double v[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -139,28 +177,44 @@ __global__ void __launch_bounds__(kRedThreads) bulk_kernel(Geometry g, FieldPtrs
     decode_vol(g, idx, x, y, z);
     const long long s = idx + g.plane;
     const long long sxp = nbs(g, x, y, z, 1, 0, 0), syp = nbs(g, x, y, z, 0, 1, 0), szp = s + g.plane;
-    Mat<double> a, b, c, d, P;
-    // Uxy = U_x(x) U_y(x+x) U_x^d(x+y) U_y^d(x)
-    load_link_d(f.U, S, 0, s, a);
-    load_link_d(f.U, S, 1, sxp, b);
-    load_link_d(f.U, S, 0, syp, c);
-    load_link_d(f.U, S, 1, s, d);
-    plaq_uudd(a, b, c, d, P);
-    v[2] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
-    // Uyz = U_y(x) U_z(x+y) U_y^d(x+z) U_z^d(x)
-    load_link_d(f.U, S, 1, s, a);
-    load_link_d(f.U, S, 2, syp, b);
-    load_link_d(f.U, S, 1, szp, c);
-    load_link_d(f.U, S, 2, s, d);
-    plaq_uudd(a, b, c, d, P);
-    v[0] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
-    // Uzx = U_z(x) U_x(x+z) U_z^d(x+x) U_x^d(x)
-    load_link_d(f.U, S, 2, s, a);
-    load_link_d(f.U, S, 0, szp, b);
-    load_link_d(f.U, S, 2, sxp, c);
-    load_link_d(f.U, S, 0, s, d);
-    plaq_uudd(a, b, c, d, P);
-    v[1] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
+    if constexpr (std::is_same<T, float>::value) {
+      // 4 (3 - ReTr P) = 2 ||A - B||^2 - 2 (n(a) + n(b) + n(c) + n(d)).  Summed over the lattice, a
+      // plane with two periodic directions counts each of its links twice; in the planes with z
+      // (open), the transverse link counts once at slice 0 and once more on the top ghost slice.
+      const double nx = link_norm_dev(f.U, S, 0, s), ny = link_norm_dev(f.U, S, 1, s), nz = link_norm_dev(f.U, S, 2, s);
+      const double wz = (z == 0) ? 1.0 : 2.0;
+      double gx = 0.0, gy = 0.0;
+      if (z == g.nz - 1) {
+        gx = link_norm_dev(f.U, S, 0, szp);
+        gy = link_norm_dev(f.U, S, 1, szp);
+      }
+      v[2] += 2.0 * (double)plaq_sqdiff_f(f.U, S, 0, 1, s, sxp, syp) - 2.0 * (2.0 * nx + 2.0 * ny);
+      v[0] += 2.0 * (double)plaq_sqdiff_f(f.U, S, 1, 2, s, syp, szp) - 2.0 * (2.0 * nz + wz * ny + gy);
+      v[1] += 2.0 * (double)plaq_sqdiff_f(f.U, S, 2, 0, s, szp, sxp) - 2.0 * (2.0 * nz + wz * nx + gx);
+    } else {
+      Mat<double> a, b, c, d, P;
+      // Uxy = U_x(x) U_y(x+x) U_x^d(x+y) U_y^d(x)
+      load_link_d(f.U, S, 0, s, a);
+      load_link_d(f.U, S, 1, sxp, b);
+      load_link_d(f.U, S, 0, syp, c);
+      load_link_d(f.U, S, 1, s, d);
+      plaq_uudd(a, b, c, d, P);
+      v[2] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
+      // Uyz = U_y(x) U_z(x+y) U_y^d(x+z) U_z^d(x)
+      load_link_d(f.U, S, 1, s, a);
+      load_link_d(f.U, S, 2, syp, b);
+      load_link_d(f.U, S, 1, szp, c);
+      load_link_d(f.U, S, 2, s, d);
+      plaq_uudd(a, b, c, d, P);
+      v[0] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
+      // Uzx = U_z(x) U_x(x+z) U_z^d(x+x) U_x^d(x)
+      load_link_d(f.U, S, 2, s, a);
+      load_link_d(f.U, S, 0, szp, b);
+      load_link_d(f.U, S, 2, sxp, c);
+      load_link_d(f.U, S, 0, s, d);
+      plaq_uudd(a, b, c, d, P);
+      v[1] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
+    }
     for (int mu = 0; mu < 3; mu++) {
       Alg<double> e;
       load_alg_d(f.E, S, mu * 8, s, e);

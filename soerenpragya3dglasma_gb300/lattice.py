@@ -164,8 +164,23 @@ class Lattice:
     def step(self, dt, nsteps=1, save_uold=True):
         check(self.lib.glasma_step(self.h, float(dt), int(nsteps), _lib.STEP_SAVE_UOLD if save_uold else 0))
 
+    STEP_METHODS = {"one_pass": 0, "two_pass": 1}
+
+    def set_step_method(self, method):
+        """"two_pass" (default: two kernels per step, in place) or "one_pass" (one kernel per step over
+        two buffer sets, half the HBM traffic).  Both give bit-identical fields."""
+        check(self.lib.glasma_set_step_method(self.h, self.STEP_METHODS[method]))
+
+    @property
+    def last_step_method(self):
+        """The method the last step() used."""
+        m = ctypes.c_int()
+        check(self.lib.glasma_get_step_method(self.h, ctypes.byref(m)))
+        return {v: k for k, v in self.STEP_METHODS.items()}[m.value]
+
     def step_profiled(self, dt, nsteps=1, save_uold=False):
-        """Like step(); returns the summed CUDA-event milliseconds of (efield_jstat, links_j)."""
+        """Like step(); returns the summed CUDA-event milliseconds of (efield_jstat, links_j) for the
+        two-pass method, (one-pass kernel, 0) for the one-pass method."""
         ms = np.zeros(2)
         check(self.lib.glasma_step_profiled(self.h, float(dt), int(nsteps), _lib.STEP_SAVE_UOLD if save_uold else 0,
                                             ms.ctypes.data_as(_lib._D)))
@@ -232,25 +247,29 @@ class Lattice:
             raise _lib.GlasmaError(st, self.lib.glasma_adjoint_last_error().decode(errors="replace"))
         return v.value
 
-    def adjoint(self, dt, nsteps, z_begin, z_end, form=PL_OVER_PT, checkpoint_every=50):
-        """Objective after nsteps and its gradient w.r.t. the initial E and currents (host layout)."""
+    def adjoint(self, dt, nsteps, z_begin, z_end, form=PL_OVER_PT, checkpoint_every=50, grads=True):
+        """Objective after nsteps and its gradient w.r.t. the initial E and currents (host layout;
+        None with grads=False, which leaves the gradients on the device unread)."""
         num = (ctypes.c_double * 6)(*form[0])
         den = (ctypes.c_double * 6)(*form[1])
         v = ctypes.c_double()
-        grads = {k: empty_field(k, self.N) for k in ("E", "Jp", "Jm", "JpStat", "JmStat")}
+        names = ("E", "Jp", "Jm", "JpStat", "JmStat")
+        out = {k: empty_field(k, self.N) for k in names} if grads else None
+        ptrs = [out[k].ctypes.data_as(_lib._D) for k in names] if grads else [None] * 5
         st = self.lib.glasma_adjoint(self.h, float(dt), int(nsteps), int(checkpoint_every), int(z_begin), int(z_end),
-                                     num, den, ctypes.byref(v),
-                                     *[grads[k].ctypes.data_as(_lib._D) for k in ("E", "Jp", "Jm", "JpStat", "JmStat")])
+                                     num, den, ctypes.byref(v), *ptrs)
         if st:
             raise _lib.GlasmaError(st, self.lib.glasma_adjoint_last_error().decode(errors="replace"))
-        return v.value, grads
+        return v.value, out
 
     # -- Coulomb gauge fixing (S/GAUGETRANSFORMATION)
-    def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False):
+    def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False, fft_fp32=False):
+        """Fourier-accelerated Coulomb gauge fixing; returns the per-iteration log rows
+        (n, max dev, avg dev, max step, avg step, min functional, functional / V)."""
         log = np.zeros((max(int(max_iters), 1), 7))
         n = ctypes.c_int()
-        check(self.lib.glasma_coulomb_fix(self.h, float(alpha), int(max_iters), float(tol),
-                                          _lib.GF_PROJECT_ZERO_MODE if project_zero_mode else 0,
+        flags = (_lib.GF_PROJECT_ZERO_MODE if project_zero_mode else 0) | (_lib.GF_FFT_FP32 if fft_fp32 else 0)
+        check(self.lib.glasma_coulomb_fix(self.h, float(alpha), int(max_iters), float(tol), flags,
                                           log.ctypes.data_as(_lib._D), ctypes.byref(n)))
         return log[: n.value]
 
@@ -262,9 +281,19 @@ class Lattice:
         check(self.lib.glasma_fft3d(self.h, X.ctypes.data, out.ctypes.data, int(inverse)))
         return out
 
-    def fft3d_device(self, in_ptr, out_ptr, inverse=False):
-        """Batched 3D FFT of 8 colour planes between device buffers (8*Nx*Ny*Nz complex doubles)."""
-        check(self.lib.glasma_fft3d(self.h, ctypes.c_void_p(int(in_ptr)), ctypes.c_void_p(int(out_ptr)), int(inverse)))
+    def fft3d_f32(self, X, inverse=False):
+        """The same transform in FP32: X complex64 of shape (8, Nz, Ny, Nx)."""
+        X = np.ascontiguousarray(X, dtype=np.complex64)
+        assert X.shape == (8, self.N[2], self.N[1], self.N[0])
+        out = np.empty_like(X)
+        check(self.lib.glasma_fft3d_f32(self.h, X.ctypes.data, out.ctypes.data, int(inverse)))
+        return out
+
+    def fft3d_device(self, in_ptr, out_ptr, inverse=False, fp32=False):
+        """Batched 3D FFT of 8 colour planes between device buffers (8*Nx*Ny*Nz complex doubles, or
+        complex floats with fp32)."""
+        fn = self.lib.glasma_fft3d_f32 if fp32 else self.lib.glasma_fft3d
+        check(fn(self.h, ctypes.c_void_p(int(in_ptr)), ctypes.c_void_p(int(out_ptr)), int(inverse)))
 
     def gauge_reset(self):
         check(self.lib.glasma_gauge_reset(self.h))

@@ -39,6 +39,32 @@ def test_batch_equals_individual_events(precision):
             assert np.array_equal(got[i][k], ref[k]), (i, k)
 
 
+def test_batch_after_events_stepped_alone():
+    """Stepping an event on its own (one-pass: its buffers swap) between batched steps: the batch
+    rebuilds its event table and the result equals stepping every event alone."""
+    fields = [O.random_fields(N, 350 + i) for i, N in enumerate(SHAPES)]
+    dt = 0.1
+    with Batch(SHAPES, precision="fp64") as b:
+        for ev, f in zip(b.events, fields):
+            ev.upload_fields(f)
+        b.step(dt, 2, use_graph=False)
+        for i in (1, 2):
+            b.events[i].set_step_method("one_pass")
+            b.events[i].step(dt, 1, save_uold=False)
+        b.step(dt, 3, use_graph=False)
+        got = [ev.download_fields(("U", "E", "Jp", "Jm", "JpStat", "JmStat")) for ev in b.events]
+    for i, (N, f) in enumerate(zip(SHAPES, fields)):
+        with Lattice(N) as lat:
+            lat.upload_fields(f)
+            lat.step(dt, 2, save_uold=False)
+            if i in (1, 2):
+                lat.step(dt, 1, save_uold=False)
+            lat.step(dt, 3, save_uold=False)
+            ref = lat.download_fields(("U", "E", "Jp", "Jm", "JpStat", "JmStat"))
+        for k in ref:
+            assert np.array_equal(got[i][k], ref[k]), (i, k)
+
+
 def test_batch_fp64_matches_oracle(oracle):
     fields = [O.random_fields(N, 400 + i) for i, N in enumerate(SHAPES)]
     dt, steps = 0.125, 5

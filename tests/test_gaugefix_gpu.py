@@ -36,6 +36,40 @@ def test_fft3d_matches_numpy(N):
     assert np.max(np.abs(B - refb)) / np.max(np.abs(refb)) < 1e-14
 
 
+@pytest.mark.parametrize("N", [(8, 8, 16), (16, 4, 32), (6, 5, 7)])
+def test_fft3d_f32_matches_numpy(N):
+    """The FP32 transform (the gauge fixer's GLASMA_GF_FFT_FP32 path): FP32 rounding, ~1e-7 log2(V)."""
+    rng = np.random.default_rng(sum(N) + 1)
+    X = (rng.standard_normal((8, N[2], N[1], N[0])) + 1j * rng.standard_normal((8, N[2], N[1], N[0]))).astype(np.complex64)
+    with Lattice(N) as lat:
+        F = lat.fft3d_f32(X)
+        B = lat.fft3d_f32(X, inverse=True)
+    Xd = X.astype(np.complex128)
+    ref = np.fft.fftn(Xd, axes=(1, 2, 3))
+    refb = np.fft.ifftn(Xd, axes=(1, 2, 3)) * (N[0] * N[1] * N[2])
+    assert np.max(np.abs(F - ref)) / np.max(np.abs(ref)) < 5e-6
+    assert np.max(np.abs(B - refb)) / np.max(np.abs(refb)) < 5e-6
+
+
+def test_fft_fp32_preconditioner_reaches_the_same_gauge():
+    """The acceleration step's transforms in FP32 only perturb each step by ~1e-7 of itself: the
+    deviation history follows the FP64 run and the gauge-fixed links agree far below the distance
+    still left to convergence."""
+    N = (8, 8, 16)
+    f = mild_config(N, 9)
+    out = {}
+    for fp32 in (False, True):
+        with Lattice(N) as lat:
+            lat.upload("U", f["U"])
+            log = lat.coulomb_fix(1.0, 100, tol=1e-12, project_zero_mode=True, fft_fp32=fp32)
+            out[fp32] = (log, lat.download("UG"))
+    l64, l32 = out[False][0], out[True][0]
+    assert len(l64) == len(l32) == 100
+    assert np.allclose(l32[:, 1:3], l64[:, 1:3], rtol=1e-4, atol=1e-12)
+    assert l32[-1, 1] < 1e-2 * l32[0, 1]
+    assert np.max(np.abs(out[True][1] - out[False][1])) < 1e-5
+
+
 def test_coulomb_matches_reference_golden(golden_dir):
     g = dict(np.load(os.path.join(golden_dir, "coulomb_mild.npz")))
     N, a = tuple(g["cfg_N"]), tuple(g["cfg_a"])

@@ -76,6 +76,43 @@ def test_leapfrog_matches_oracle(oracle, N, a, dt, seed):
         assert _rel(out[k], ref[k]) < 1e-12, k
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("N", [(6, 5, 8), (3, 7, 2), (16, 8, 4)])
+def test_one_pass_equals_two_pass_bit_exact(precision, N):
+    """The one-pass step (second buffer set, static currents one slice up recomputed per site) and
+    the two in-place kernels round identically: every field, ghost slices included."""
+    f = O.random_fields(N, 21)
+    kw = dict(reunitarize_every=3) if precision == "fp32" else {}
+    outs = []
+    for method in ("one_pass", "two_pass"):
+        with _gpu(f, N, (1.0, 1.1, 0.9), precision=precision, **kw) as lat:
+            lat.set_step_method(method)
+            lat.step(0.1, 7, save_uold=True)
+            assert lat.last_step_method == method
+            outs.append(lat.download_fields())
+    for k in FIELDS:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+def test_step_method_switch_mid_run(oracle):
+    """Odd and even step counts with each method, switching between calls, still follow the oracle."""
+    N, dt = (6, 6, 10), 0.1
+    f = O.random_fields(N, 22)
+    ref = O.copy_fields(f)
+    oracle.update(ref, N, (1.0, 1.0, 1.0), dt, 3, save_uold=False)
+    oracle.update(ref, N, (1.0, 1.0, 1.0), dt, 2, save_uold=False)
+    oracle.update(ref, N, (1.0, 1.0, 1.0), dt, 1, save_uold=True)
+    with _gpu(f, N, (1.0, 1.0, 1.0)) as lat:
+        lat.step(dt, 3, save_uold=False)
+        lat.set_step_method("two_pass")
+        lat.step(dt, 2, save_uold=False)
+        lat.set_step_method("one_pass")
+        lat.step(dt, 1, save_uold=True)
+        out = lat.download_fields()
+    for k in FIELDS:
+        assert _rel(out[k], ref[k]) < 1e-12, k
+
+
 def test_unsynced_ghosts_are_read_as_the_reference_reads_them(oracle):
     """Uploaded ghost slices that are out of date: the reference syncs U at the start of the
     electric update but reads the current ghosts of Jp/Jm as they stand."""
@@ -153,6 +190,25 @@ def test_fp32_tracks_fp64(oracle):
     assert _rel(out["U"], ref["U"]) < 1e-5
     assert _rel(out["E"], ref["E"]) < 1e-4
     assert umax < 1e-5
+
+
+@pytest.mark.parametrize("link_amp", [0.02, 0.3])
+def test_fp32_bulk_matches_fp64_measurement_of_same_fields(oracle, link_amp):
+    """The FP32 energy kernel (plaquette halves in FP32, trace and sums in FP64) against the oracle
+    measuring the very same FP32 fields in FP64: per-plane magnetic sums within 1e-6 relative,
+    electric sums within 1e-12, also for weak fields where 3 - ReTr(P) is small."""
+    N, a = (12, 10, 14), (1.0, 1.0, 1.0)
+    f = O.random_fields(N, 53, link_amp=link_amp, e_amp=0.1, j_amp=0.02)
+    with _gpu(f, N, a, precision="fp32") as lat:
+        got = lat.bulk()
+        stored = lat.download_fields()
+    want = oracle.bulk(stored, N, a)
+    # out[0..2] ESqr, [3..5] BSqr, [6..8] EDotJ, [9..15] T00, TXX, TYY, TZZ, ELECTRIC, MAGNETIC, SOURCE
+    for k in (3, 4, 5, 14):  # magnetic sums
+        assert abs(got[k] - want[k]) <= 1e-6 * abs(want[k]), k
+    for k in (0, 1, 2, 6, 7, 8, 13, 15):  # electric and source sums: FP64 arithmetic on the same floats
+        assert abs(got[k] - want[k]) <= 1e-12 * abs(want[k]) + 1e-14, k
+    assert abs(got[9] - want[9]) <= 1e-6 * abs(want[9])
 
 
 def test_fp32_reunitarize_restores_unitarity():
