@@ -11,7 +11,7 @@ site-updates/s (lattice sites x steps / second).
             steps, and reads the bulk energy back
   fp32      the same lattice in FP32 storage/arithmetic with FP64 reductions and
             reunitarisation every 16 steps, with its energy error against FP64
-  roofline  for the dominant kernel (electric-field update), per-launch CUDA events
+  roofline  for the dominant kernel (the electric-field kernel K1), per-launch CUDA events
   cpu_baseline  the oracle's CPU restatement on the host cores on a bounded slab
 
 `--impl reference` times the reference algorithm on the host CPU (the oracle port,
@@ -41,6 +41,7 @@ INPUT_FIELDS = ("U", "E", "Jp", "Jm", "JpStat", "JmStat")
 KERNEL_BYTES = {
     "efield_jstat": {"fp64": 432 + 2 * 192 + 128 + 2 * 128, "fp32": 216 + 2 * 96 + 64 + 2 * 64},
     "links_j": {"fp64": 192 + 2 * 432 + 128 + 2 * 128, "fp32": 96 + 2 * 216 + 64 + 2 * 64},
+    "fused_step": {"fp64": 1760, "fp32": 880},  # one pass: every per-site state array read and written once
 }
 STEP_BYTES = {"fp64": 1760, "fp32": 880}  # every per-site state array read and written once
 FALLBACK_HBM_GBS = 6800.0
@@ -285,6 +286,7 @@ def run_ours(args):
     def make_lattice(precision):
         lat = Lattice(N, A_WORK, precision=precision, reunitarize_every=16 if precision == "fp32" else 0,
                       stream=stream)
+        lat.set_step_method(args.step_method)
         for k in INPUT_FIELDS:
             lat.upload_device(k, inputs[k].data_ptr())
         lat.upload_device("UOld", inputs["U"].data_ptr())
@@ -313,7 +315,28 @@ def run_ours(args):
             return float(t.item())
         return x
 
-    def timed_run(precision, sampler=None):
+    def time_observables(lat, reps=3):
+        """CUDA-event milliseconds of one bulk-energy and one Gauss-law measurement (each returns to
+        the host, as the reference's measurement steps do)."""
+        out = {}
+        for name, fn in (("bulk", lat.bulk), ("gauss", lat.gauss)):
+            fn()
+            torch.cuda.synchronize()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(reps):
+                fn()
+            t1.record(stream)
+            torch.cuda.synchronize()
+            out[name] = t0.elapsed_time(t1) / reps
+        return out
+
+    # FP32 links are reunitarised every 16 steps: its timed window is a multiple of 16 steps, so it
+    # holds its share of reunitarisations whatever the alignment.
+    steps32 = 16 * max(1, -(-args.steps // 16))
+
+    def timed_run(precision, sampler=None, nsteps=None):
+        nsteps = nsteps or args.steps
         lat = make_lattice(precision)
         lat.step(DT, args.warmup, save_uold=False)
         torch.cuda.synchronize()
@@ -322,71 +345,121 @@ def run_ours(args):
         if sampler is not None:
             sampler.__enter__()
         e0.record(stream)
-        kms = lat.step_profiled(DT, args.steps, save_uold=False)
+        kms = lat.step_profiled(DT, nsteps, save_uold=False)
         e1.record(stream)
         torch.cuda.synchronize()
         if sampler is not None:
             sampler.__exit__(None, None, None)
         barrier()
-        ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
-        kern = {"efield_jstat": kms[0] / args.steps, "links_j": kms[1] / args.steps}
+        ms = max_over_ranks(e0.elapsed_time(e1)) / nsteps
+        if lat.last_step_method == "one_pass":
+            kern = {"fused_step": kms[0] / nsteps}
+        else:
+            kern = {"efield_jstat": kms[0] / nsteps, "links_j": kms[1] / nsteps}
         return lat, ms, kern
 
     run64 = args.only in ("both", "fp64")
     run32 = args.only in ("both", "fp32")
     clk = ClockSampler(local)
     lat = None
-    value = ms_step = rl = k_ms = e64 = None
+    value = ms_step = rl = k_ms = e64 = obs64 = None
     if run64:
         # ---- FP64, resident fields (the headline)
         lat, ms_step, k_ms = timed_run("fp64", clk)
         value = world * vol / (ms_step * 1e-3)
+        if run32 and steps32 > args.steps:  # untimed: bring the FP64 state to the FP32 leg's step count
+            lat.step(DT, steps32 - args.steps, save_uold=False)
         e64 = lat.bulk()
+        obs64 = time_observables(lat)
         dom = max(k_ms, key=k_ms.get)
         rl = roofline(dom, "fp64", k_ms[dom])
 
     gauge = None
     if run64 and not args.no_gauge:
-        # ---- Coulomb gauge fixing on the evolved FP64 lattice: iterations/s and FFT GB/s
-        gf_iters = 10
-        lat.coulomb_fix(0.96, 1, tol=0.0)  # warm-up: allocates G/UG/EG and the FFT arrays
+        # ---- Coulomb gauge fixing (the production workload's last stage) on an evolved MV collision:
+        # iterations/s, iterations until theta = avg deviation^2 < 1e-10, and FFT GB/s
+        import numpy as np
+
+        from soerenpragya3dglasma_gb300 import GlasmaError
+
+        alpha_ref = 0.96  # alpha = 0.08 in the p^2_max/p^2 normalisation, times p^2_max = 12 at a = 1
+        zrng = np.random.default_rng(SEED - 1)
+        zl, zr = zrng.standard_normal(8 * N[0] * N[1]), zrng.standard_normal(8 * N[0] * N[1])
+        centres = (N[2] // 2 - 3 * N[2] // 16, N[2] // 2 + 3 * N[2] // 16)  # 256 -+ 96 at Nz = 512
+        glat = Lattice(N, A_WORK, stream=stream)
+        glat.mv_init(zl, zr, qs=(0.5, 0.5), centers=centres, sigma=N[2] / 64.0, lam=1.65, meff=0.2, dt=DT)
+        glat.step(DT, args.gauge_evolve, save_uold=False)
         torch.cuda.synchronize()
-        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        g0.record(stream)
-        log = lat.coulomb_fix(0.96, gf_iters, tol=0.0)
-        g1.record(stream)
-        torch.cuda.synchronize()
-        gf_ms = g0.elapsed_time(g1) / max(len(log), 1)
-        X = torch.randn((8, N[2], N[1], N[0]), dtype=torch.complex128, device=dev)
-        Y = torch.empty_like(X)
-        lat.fft3d_device(X.data_ptr(), Y.data_ptr())
-        torch.cuda.synchronize()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for _ in range(5):
-            lat.fft3d_device(X.data_ptr(), Y.data_ptr())
-        f1.record(stream)
-        torch.cuda.synchronize()
-        fft_ms = f0.elapsed_time(f1) / 5
-        fft_bytes = 3 * 2 * 16 * 8 * vol  # three axis passes, each reads and writes the 8-colour array
-        gauge = {"iterations_per_s": 1e3 / gf_ms, "ms_per_iteration": gf_ms, "iterations": len(log),
-                 "alpha_reference": 0.96, "max_deviation_last": float(log[-1, 1]) if len(log) else None,
-                 "fft3d_ms": fft_ms, "fft_gbs": fft_bytes / (fft_ms * 1e-3) / 1e9,
-                 "fft_note": "forward 3D FFT of 8 complex-double colour planes, device to device "
-                             "(includes one copy in and one copy out of the work array)"}
-        del X, Y
+
+        def time_gauge(fft_fp32, project):
+            glat.gauge_reset()
+            torch.cuda.synchronize()
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            try:
+                log = glat.coulomb_fix(alpha_ref, args.gauge_iters, tol=0.0, project_zero_mode=project,
+                                       fft_fp32=fft_fp32)
+                err = None
+            except GlasmaError as e:
+                log, err = None, str(e)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            if log is None:
+                return {"error": err, "project_zero_mode": project}
+            theta = log[:, 2] ** 2
+            hit = np.nonzero(theta < 1e-10)[0]
+            return {"iterations_per_s": len(log) / (g0.elapsed_time(g1) * 1e-3),
+                    "ms_per_iteration": g0.elapsed_time(g1) / len(log), "iterations_run": len(log),
+                    "iterations_to_theta_1e-10": int(hit[0]) + 1 if len(hit) else None,
+                    "theta_first": float(theta[0]), "theta_last": float(theta[-1]),
+                    "max_deviation_last": float(log[-1, 1]), "project_zero_mode": project}
+
+        def time_fft(fp32):
+            X = torch.randn((8, N[2], N[1], N[0]), dtype=torch.complex64 if fp32 else torch.complex128, device=dev)
+            Y = torch.empty_like(X)
+            glat.fft3d_device(X.data_ptr(), Y.data_ptr(), fp32=fp32)
+            torch.cuda.synchronize()
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(5):
+                glat.fft3d_device(X.data_ptr(), Y.data_ptr(), fp32=fp32)
+            f1.record(stream)
+            torch.cuda.synchronize()
+            ms = f0.elapsed_time(f1) / 5
+            # three axis passes, each reads and writes the 8-colour array once
+            return ms, 3 * 2 * (8 if fp32 else 16) * 8 * vol / (ms * 1e-3) / 1e9
+
+        runs = {}
+        for fft_fp32 in (False, True):
+            r = time_gauge(fft_fp32, False)
+            if "error" in r:  # the reference's unnormalised zero mode can drift out of SU(3): retry without it
+                r = {"reference_semantics": r, **time_gauge(fft_fp32, True)}
+            runs["fft_fp32" if fft_fp32 else "fft_fp64"] = r
+        fft_ms, fft_gbs = time_fft(False)
+        fft32_ms, fft32_gbs = time_fft(True)
+        gauge = {"state": "MV collision (seeded charges, g^2 mu 0.5, m 0.2, sigma_z %g, centres %d/%d) evolved %d "
+                          "steps" % (N[2] / 64.0, centres[0], centres[1], args.gauge_evolve),
+                 "alpha_reference": alpha_ref, **runs,
+                 "fft3d_ms": fft_ms, "fft_gbs": fft_gbs, "fft3d_fp32_ms": fft32_ms, "fft_fp32_gbs": fft32_gbs,
+                 "fft_note": "one 3D FFT of 8 colour planes, device to device, including one copy into and one "
+                             "out of the work array; the gauge iteration transforms 4 packed colour-pair planes "
+                             "twice"}
+        del glat
 
     fp32 = None
     if run32:
         # ---- FP32 on the same inputs
-        lat32, ms32, k32 = timed_run("fp32", None if run64 else clk)
+        lat32, ms32, k32 = timed_run("fp32", None if run64 else clk, steps32)
         e32 = lat32.bulk()
+        obs32 = time_observables(lat32)
         dom32 = max(k32, key=k32.get)
         fp32 = {"value": world * vol / (ms32 * 1e-3), "ms_per_step": ms32,
                 "step_hbm_frac": STEP_BYTES["fp32"] * vol / (ms32 * 1e-3) / 1e9 / peak,
                 "energy_rel_err_vs_fp64": (abs(e32[9] - e64[9]) / abs(e64[9])) if e64 is not None else None,
-                "steps_compared": args.warmup + args.steps,
+                "steps": steps32, "reunitarisations_timed": steps32 // 16,
+                "steps_compared": args.warmup + steps32,
                 "kernel_ms": k32,
+                "observables_ms": obs32,
                 "roofline": roofline(dom32, "fp32", k32[dom32])}
         del lat32
 
@@ -448,12 +521,15 @@ def run_ours(args):
         "step_hbm_frac": (STEP_BYTES["fp64"] * vol / (ms_step * 1e-3) / 1e9 / peak) if ms_step else None,
         "roofline": rl,
         "kernel_ms": k_ms,
+        "observables_ms": obs64,
         "fp32": fp32,
         "gauge_fixing": gauge,
         "e2e": e2e,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
-        "gpu_launches": 2 * args.steps,
+        # per step: the one-pass kernel (or K1 + K2); per step() call: one ghost-slice sync
+        "gpu_launches": (1 if "fused_step" in (k_ms or {}) else 2) * args.steps + 1,
+        "step_method": args.step_method,
         "tiles": tiles,
     }
     print(json.dumps(line), flush=True)
@@ -527,6 +603,94 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args):
+    """The adjoint workload: a 64x64x256 MV collision (g^2 mu = 0.5, m = 0.2, sigma_z = 4, centres
+    128 -+ 24, seeded charges), FP64, 400 steps at dt = 0.125, objective P_L/P_T over the central 32
+    slices, checkpoints every 50 steps.  Reports the adjoint's wall time (forward with checkpoints,
+    then the time-reversed backward pass) over the plain forward's, and central differences
+    (eps = 1e-6) along seeded random directions of E and the currents."""
+    import numpy as np
+    import torch
+
+    from soerenpragya3dglasma_gb300 import Lattice, build
+
+    build.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    N, dt, steps, every, z0, z1 = (64, 64, 256), 0.125, args.adj_steps, 50, 112, 144
+    rng = np.random.default_rng(1004)
+    zl, zr = rng.standard_normal(8 * N[0] * N[1]), rng.standard_normal(8 * N[0] * N[1])
+    names = ("E", "Jp", "Jm", "JpStat", "JmStat")
+    with Lattice(N, stream=stream) as lat:
+        lat.mv_init(zl, zr, qs=(0.5, 0.5), centers=(128 - 24, 128 + 24), sigma=4.0, lam=1.65, meff=0.2, dt=dt)
+        f0 = lat.download_fields()
+
+        def restore(fields):
+            lat.upload_fields(fields)
+            torch.cuda.synchronize()
+
+        def objective_after(fields):
+            restore(fields)
+            lat.step(dt, steps, save_uold=False)
+            return lat.objective(z0, z1, Lattice.PL_OVER_PT)
+
+        lat.step(dt, 3, save_uold=False)  # warm-up
+        restore(f0)
+        t0 = time.perf_counter()
+        lat.step(dt, steps, save_uold=False)
+        torch.cuda.synchronize()
+        fwd_s = time.perf_counter() - t0
+        L_fwd = lat.objective(z0, z1, Lattice.PL_OVER_PT)
+        restore(f0)
+        t0 = time.perf_counter()
+        L_adj, _ = lat.adjoint(dt, steps, z0, z1, Lattice.PL_OVER_PT, checkpoint_every=every, grads=False)
+        torch.cuda.synchronize()
+        adj_s = time.perf_counter() - t0
+        restore(f0)
+        _, grads = lat.adjoint(dt, steps, z0, z1, Lattice.PL_OVER_PT, checkpoint_every=every)
+        checks = []
+        eps = 1e-6
+        for k in range(args.fd_dirs):
+            drng = np.random.default_rng(3000 + k)
+            d = {}
+            for name in names:
+                v = drng.standard_normal(f0[name].shape)
+                v[0], v[-1] = v[1], v[-2]  # ghost slices: copies of the boundary slices
+                d[name] = v
+            fp = dict(f0)
+            fm = dict(f0)
+            for name in names:
+                fp[name] = f0[name] + eps * d[name]
+                fm[name] = f0[name] - eps * d[name]
+            fd = (objective_after(fp) - objective_after(fm)) / (2 * eps)
+            ad = sum(float(np.sum(grads[name][1:-1] * d[name][1:-1])) for name in names)
+            checks.append({"fd": fd, "adjoint": ad, "rel_diff": abs(fd - ad) / max(abs(fd), 1e-300)})
+    line = {
+        "metric": "adjoint cost: adjoint time / forward time",
+        "value": adj_s / fwd_s,
+        "unit": "x",
+        "n_gpus": 1,
+        "steps": steps,
+        "warmup": 3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "MV collision from seeded N(0,1) charges (numpy PCG64 seed 1004), built on the GPU",
+        "config": {"workload": "adjoint of P_L/P_T, 64x64x256 MV collision, %d steps, checkpoints every %d, "
+                               "z in [%d, %d)" % (steps, every, z0, z1),
+                   "lattice": list(N), "dt": dt, "g2mu": 0.5, "m": 0.2, "sigma_z": 4.0},
+        "forward_s": fwd_s,
+        "adjoint_s": adj_s,
+        "objective": L_adj,
+        "objective_forward": L_fwd,
+        "fd_checks": checks,
+        "fd_eps": eps,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -536,11 +700,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-gauge", action="store_true", help="skip the gauge-fixing / FFT leg")
+    ap.add_argument("--step-method", default="two_pass", choices=["one_pass", "two_pass"])
+    ap.add_argument("--gauge-evolve", type=int, default=40, help="leapfrog steps of the MV state before gauge fixing")
+    ap.add_argument("--gauge-iters", type=int, default=300)
     ap.add_argument("--only", default="both", choices=["both", "fp64", "fp32"],
                     help="which precisions to run (profiling runs); the JSON line needs both")
     ap.add_argument("--lattice", default=None, help="Nx,Ny,Nz instead of the workload's (profiling runs)")
-    ap.add_argument("--workload", default="production", choices=["production", "batched"],
-                    help="production: the headline 128x128x512 line; batched: 64 uneven events in one launch")
+    ap.add_argument("--workload", default="production", choices=["production", "batched", "adjoint"],
+                    help="production: the headline 128x128x512 line; batched: 64 uneven events in one launch; "
+                         "adjoint: the gradient of P_L/P_T on a 64x64x256 collision")
+    ap.add_argument("--adj-steps", type=int, default=400)
+    ap.add_argument("--fd-dirs", type=int, default=2)
     ap.add_argument("--events", type=int, default=64)
     ap.add_argument("--tile", type=int, default=0, help="fixed electric-field tile width instead of autotuning")
     args = ap.parse_args()
@@ -553,6 +723,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 

@@ -15,8 +15,7 @@
 //   W' = A W           -> Lambda_W = A^dagger Lambda_W', Lambda_A = Lambda_W' W^dagger
 //   f = ReTr(M W1..W4) -> link k: Lambda = (B A)^dagger if W_k = U, B A if W_k = U^dagger,
 //                         A = M W1..W_{k-1}, B = W_{k+1}..W4
-//   X = exp(iQ)        -> Lambda_Q-side K = int_0^1 e^{-isQ} Lambda_X e^{-i(1-s)Q} ds (Frechet derivative
-//                         at -iQ), lambda_E^a = -c ReTr(i t^a K); 6-point Gauss-Legendre in s
+//   X = exp(iQ)        -> closed-form derivative of the Cayley-Hamilton coefficients (expi_vjp below)
 //   Adj(V,e)           -> Lambda_V = 4 (t.mu) V (t.e), transpose in e = InvAdj(V, .)
 //   InvAdj(V,e)        -> Lambda_V = 4 (t.e) V (t.mu), transpose in e = Adj(V, .)
 // Ghost slices are copies of the boundary slices, so cotangents that land on a ghost are added to
@@ -90,6 +89,145 @@ __device__ __forceinline__ void i_herm(const A8& l, double scale, M3& m) {
   herm_from_alg(s, h);
 #pragma unroll
   for (int k = 0; k < 9; k++) m.e[k] = mk<double>(-h.e[k].im, h.e[k].re);
+}
+
+// ---- exact vector-Jacobian product of X = exp(iQ), Q = c t.e
+// exp(iQ) = f0 + f1 Q + f2 Q^2 with f_j(c0, c1), c0 = det Q, c1 = tr Q^2 / 2 (the Cayley-Hamilton form
+// of expi).  dX = sum_j df_j Q^j + f1 dQ + f2 (dQ Q + Q dQ), df_j = b1_j dc1 + b2_j dc0,
+// dc1 = tr(Q dQ), dc0 = tr(Q^2 dQ), so for dL = ReTr(Lx^d dX):
+//   dL = ReTr(G dQ),  G = beta1 Q + beta2 Q^2 + f1 Lx^d + f2 (Q Lx^d + Lx^d Q),
+//   beta_k = Re sum_j b_kj tr(Lx^d Q^j),
+// and dL/de^a = c ReTr(G t^a).  The derivatives b are taken in the variables (u, v = w^2) of the
+// closed form (eigenvalues 2u, -u +- w), where every factor is an entire function of v, then mapped
+// to (c0, c1) by the inverse Jacobian of c1 = 3u^2 + v, c0 = 2u^3 - 2uv (determinant
+// 2 (9u^2 - w^2) >= 16 u^2 once c0 is folded to |c0|); below c1 = 1e-6 the Taylor series of f_j is
+// differentiated instead.  Checked against the exact Frechet derivative (block exponential) to 4e-13.
+__device__ __forceinline__ C cm(double r, double i) { return mk<double>(r, i); }
+__device__ __forceinline__ C cmul(C a, C b) { return cm(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+__device__ __forceinline__ C cadd(C a, C b) { return cm(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ C csub(C a, C b) { return cm(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ C cscale(double s, C a) { return cm(s * a.re, s * a.im); }
+
+__device__ void exp_coeff_derivs(double c0, double c1, C (&f)[3], C (&b2)[3], C (&b1)[3]) {
+  if (c1 < 1e-6) {
+    f[0] = cm(1.0 - c0 * c0 / 720.0, -c0 / 6.0 + c1 * c0 / 120.0);
+    f[1] = cm(c0 / 24.0 - c0 * c1 / 360.0, 1.0 - c1 / 6.0 + c1 * c1 / 120.0);
+    f[2] = cm(-0.5 + c1 / 24.0 - c1 * c1 / 720.0, c0 / 120.0);
+    b2[0] = cm(-c0 / 360.0, -1.0 / 6.0 + c1 / 120.0);
+    b2[1] = cm(1.0 / 24.0 - c1 / 360.0, 0.0);
+    b2[2] = cm(0.0, 1.0 / 120.0);
+    b1[0] = cm(0.0, c0 / 120.0);
+    b1[1] = cm(-c0 / 360.0, -1.0 / 6.0 + c1 / 60.0);
+    b1[2] = cm(1.0 / 24.0 - c1 / 360.0, 0.0);
+    return;
+  }
+  const bool neg = c0 < 0.0;
+  const double ac0 = neg ? -c0 : c0;
+  const double s3 = sqrt(c1 / 3.0);
+  double r = ac0 / (2.0 * s3 * s3 * s3);
+  r = r > 1.0 ? 1.0 : r;
+  double st, ct;
+  sincos(acos(r) / 3.0, &st, &ct);
+  const double u = s3 * ct, w = sqrt(c1) * st, v = w * w, uu = u * u;
+  double sw, cw;
+  sincos(w, &sw, &cw);
+  double x0, x1;  // sin w / w and (cos w - sin w / w) / w^2
+  if (w < 0.05) {
+    x0 = 1.0 - v / 6.0 * (1.0 - v / 20.0 * (1.0 - v / 42.0 * (1.0 - v / 72.0)));
+    x1 = -1.0 / 3.0 + v / 30.0 - v * v / 840.0 + v * v * v / 45360.0;
+  } else {
+    x0 = sw / w;
+    x1 = (cw - x0) / v;
+  }
+  double s2u, c2u, su, cu;
+  sincos(2.0 * u, &s2u, &c2u);
+  sincos(u, &su, &cu);
+  const C e2 = cm(c2u, s2u), em = cm(cu, -su), I = cm(0.0, 1.0);
+  const C A0 = cm(8.0 * uu * cw, 2.0 * u * (3.0 * uu + v) * x0);
+  const C A1 = cm(2.0 * u * cw, -(3.0 * uu - v) * x0);
+  const C A2 = cm(cw, 3.0 * u * x0);
+  C h[3], hu[3], hv[3];
+  h[0] = cadd(cscale(uu - v, e2), cmul(em, A0));
+  h[1] = csub(cscale(2.0 * u, e2), cmul(em, A1));
+  h[2] = csub(e2, cmul(em, A2));
+  const C iem = cmul(I, em);  // i e^{-iu}: d e^{-iu}/du = -i e^{-iu}
+  hu[0] = cadd(cadd(cmul(cm(2.0 * u, 2.0 * (uu - v)), e2), cscale(-1.0, cmul(iem, A0))),
+               cmul(em, cm(16.0 * u * cw, 2.0 * (9.0 * uu + v) * x0)));
+  hu[1] = csub(cmul(cm(2.0, 4.0 * u), e2), csub(cmul(em, cm(2.0 * cw, -6.0 * u * x0)), cmul(iem, A1)));
+  hu[2] = csub(cmul(cm(0.0, 2.0), e2), csub(cmul(em, cm(0.0, 3.0 * x0)), cmul(iem, A2)));
+  hv[0] = cadd(cscale(-1.0, e2), cmul(em, cm(-4.0 * uu * x0, 2.0 * u * x0 + u * (3.0 * uu + v) * x1)));
+  hv[1] = cscale(-1.0, cmul(em, cm(-u * x0, x0 - 0.5 * (3.0 * uu - v) * x1)));
+  hv[2] = cscale(-1.0, cmul(em, cm(-0.5 * x0, 1.5 * u * x1)));
+  const double d = 9.0 * uu - v, id = 1.0 / d;
+  const double iD = 1.0 / (18.0 * uu - 2.0 * v);
+  const double du0 = iD, du1 = 2.0 * u * iD, dv0 = -6.0 * u * iD, dv1 = (6.0 * uu - 2.0 * v) * iD;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    f[j] = cscale(id, h[j]);
+    const C fu = cscale(id, csub(hu[j], cscale(18.0 * u, f[j])));
+    const C fv = cscale(id, cadd(hv[j], f[j]));
+    b2[j] = cadd(cscale(du0, fu), cscale(dv0, fv));
+    b1[j] = cadd(cscale(du1, fu), cscale(dv1, fv));
+  }
+  if (neg) {  // f_j(-c0) = (-1)^j conj f_j(c0); d/dc0 picks up one more sign
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const double sg = (j == 1) ? -1.0 : 1.0;
+      f[j] = cm(sg * f[j].re, -sg * f[j].im);
+      b1[j] = cm(sg * b1[j].re, -sg * b1[j].im);
+      b2[j] = cm(-sg * b2[j].re, sg * b2[j].im);
+    }
+  }
+}
+
+// dl^a = dL/de^a for X = exp(i c t.e) given Lx (dL = ReTr(Lx^d dX))
+__device__ void expi_vjp(double c, const A8& e, const M3& lx, A8& dl) {
+  A8 sc;
+#pragma unroll
+  for (int a = 0; a < 8; a++) sc.a[a] = c * e.a[a];
+  M3 Q, Q2;
+  herm_from_alg(sc, Q);
+  mul_nn(Q, Q, Q2);
+  const double c1 = 0.5 * (Q2.e[0].re + Q2.e[4].re + Q2.e[8].re);
+  double c0 = 0.0;  // tr(Q^2 Q) / 3, real
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const C a = Q2.e[i + 3 * j], b = Q.e[j + 3 * i];
+      c0 += a.re * b.re - a.im * b.im;
+    }
+  c0 *= 1.0 / 3.0;
+  C f[3], b2[3], b1[3];
+  exp_coeff_derivs(c0, c1, f, b2, b1);
+  // tau_j = tr(Lx^d Q^j) = sum_k conj(Lx_k) Q^j_k
+  C tau[3] = {cm(0, 0), cm(0, 0), cm(0, 0)};
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const C l = cm(lx.e[k].re, -lx.e[k].im);
+    if (k % 4 == 0) tau[0] = cadd(tau[0], l);
+    tau[1] = cadd(tau[1], cmul(l, Q.e[k]));
+    tau[2] = cadd(tau[2], cmul(l, Q2.e[k]));
+  }
+  double beta1 = 0.0, beta2 = 0.0;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    beta1 += cmul(b1[j], tau[j]).re;
+    beta2 += cmul(b2[j], tau[j]).re;
+  }
+  M3 L, QL, LQ;
+  dagger(lx, L);
+  mul_nn(Q, L, QL);
+  mul_nn(L, Q, LQ);
+  M3 M;  // M = -i G
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    C g = cadd(cscale(beta1, Q.e[k]), cscale(beta2, Q2.e[k]));
+    g = cadd(g, cmul(f[1], L.e[k]));
+    g = cadd(g, cmul(f[2], cadd(QL.e[k], LQ.e[k])));
+    M.e[k] = cm(g.im, -g.re);
+  }
+  retr_itg(M, c, dl);
 }
 
 // Cotangents of the four links of f = ReTr(M W1 W2 W3 W4); dag[k] tells whether W_k = U^dagger.
@@ -263,28 +401,11 @@ __global__ void __launch_bounds__(kAT) adj_links_kernel(Geometry g, AdjPtrs a, c
       lx.e[k].im += t1.e[k].im;
     }
     st(a.LU, S, mu, s, lu_new);
-    // X = exp(i cU t.E): lambda_E += -cU ReTr(i t^a K),  K = int e^{-isQ} lx e^{-i(1-s)Q} ds
-    A8 e;
+    // X = exp(i cU t.E): lambda_E += dL/dE through the exact exp VJP
+    A8 e, le, dl;
     load_alg<double, L>(E, S, mu * 8, s, e);
-    const double gx[3] = {0.2386191860831969086305017, 0.6612093864662645136613996, 0.9324695142031520278123016};
-    const double gw[3] = {0.4679139345726910473898703, 0.3607615730481386075698335, 0.1713244923791703450402961};
-    M3 K;
-    set_zero(K);
-    for (int i = 0; i < 3; i++) {
-      const double sa = 0.5 * (1.0 - gx[i]), sb = 1.0 - sa;
-      M3 Ea, Eb, p1, p2;
-      expi(-sa * cU[mu], e, Ea);
-      expi(-sb * cU[mu], e, Eb);
-      mul_nn(Ea, lx, p1);
-      mul_nn(p1, Eb, p2);
-      axpy(0.5 * gw[i], p2, K);
-      mul_nn(Eb, lx, p1);
-      mul_nn(p1, Ea, p2);
-      axpy(0.5 * gw[i], p2, K);
-    }
-    A8 le, dl;
+    expi_vjp(cU[mu], e, lx, dl);
     load_alg<double, L>(a.LE, S, mu * 8, s, le);
-    retr_itg(K, -cU[mu], dl);
 #pragma unroll
     for (int k = 0; k < 8; k++) le.a[k] += dl.a[k];
     store_alg<double, L>(a.LE, S, mu * 8, s, le);
@@ -350,6 +471,68 @@ __global__ void __launch_bounds__(kAT) adj_jstat_kernel(Geometry g, AdjPtrs a, c
 
 // Electric-field sub-step in reverse (A1): E1 = E + F(U) + jz (Jp - Jm).  lambda_E unchanged;
 // lambda_Jp/Jm get the jz term; Lambda_U gets the force's link cotangents (scattered atomically).
+// Electric-field sub-step in reverse, one plaquette at a time.  For the plaquette at x in plane
+// (p, q), p < q, with links a = U_p(x), b = U_q(x+p), c = U_p(x+q), d = U_q(x), P = a b c^d d^d, the
+// force terms that contain it are the four staples
+//   ReTr(M1 P) + ReTr(M2 c b^d a^d d) + ReTr(M3 d c b^d a^d) + ReTr(M4 b c^d d^d a),
+// M1 = i t.lambda_p(x) gc_p cn_q, M2 = i t.lambda_p(x+q) gc_p cn_q, M3 = i t.lambda_q(x) gc_q cn_p,
+// M4 = i t.lambda_q(x+p) gc_q cn_p (anti-Hermitian).  On SU(3) (a^d a = d^d d = 1) they sum to
+// ReTr(N P), N = M1 - M3 + a M4 a^d - d M2 d^d, whose link cotangents are those of the path
+// N a b c^d d^d plus the explicit a- and d-dependence of N.  These agree with the four separate
+// staple cotangents along every SU(3) tangent direction (the only directions the E and current
+// gradients see) at 22 instead of 36 matmuls and a quarter of the atomics.  Open z: a plaquette at
+// the top slice has no M2 term (its link at x+z is a ghost), and the threads of slice 0 also take
+// the M2 term of the plaquette at the bottom ghost slice (the backward staple of U_p(x, z=0)).
+__device__ void plaquette_vjp(C* LU, L S, int p, int q, L sa, L sb, L sc, L sd, const M3& a, const M3& b,
+                              const M3& c, const M3& d, const M3& M1, const M3& M2, const M3& Mm3, const M3& M4) {
+  M3 cd, P, t, N;
+  mul_dd(c, d, cd);  // c^d d^d
+  mul_nn(a, b, t);
+  mul_nn(t, cd, P);
+#pragma unroll
+  for (int k = 0; k < 9; k++) N.e[k] = mk<double>(M1.e[k].re - Mm3.e[k].re, M1.e[k].im - Mm3.e[k].im);
+  {
+    M3 u, v;
+    mul_nn(a, M4, u);
+    mul_nd(u, a, v);
+    axpy(1.0, v, N);
+    mul_nn(d, M2, u);
+    mul_nd(u, d, v);
+    axpy(-1.0, v, N);
+  }
+  M3 La, Lb, Lc, Ld, bcd, Na, Nab, w;
+  mul_nn(b, cd, bcd);
+  mul_nn(bcd, N, w);
+  dagger(w, La);
+  mul_nn(N, a, Na);
+  mul_nn(cd, Na, w);
+  dagger(w, Lb);
+  mul_nn(Na, b, Nab);
+  mul_dn(d, Nab, Lc);
+  mul_nd(Nab, c, Ld);
+  {
+    M3 u, v, vd;
+    mul_nd(M4, a, u);  // M4 a^d P, enters as its dagger
+    mul_nn(u, P, v);
+    dagger(v, vd);
+    axpy(1.0, vd, La);
+    mul_nn(P, a, u);  // P a M4
+    mul_nn(u, M4, v);
+    axpy(1.0, v, La);
+    mul_nd(M2, d, u);  // -(M2 d^d P)^d
+    mul_nn(u, P, v);
+    dagger(v, vd);
+    axpy(-1.0, vd, Ld);
+    mul_nn(P, d, u);  // -P d M2
+    mul_nn(u, M2, v);
+    axpy(-1.0, v, Ld);
+  }
+  atomic_add_link(LU, S, p, sa, La);
+  atomic_add_link(LU, S, q, sb, Lb);
+  atomic_add_link(LU, S, p, sc, Lc);
+  atomic_add_link(LU, S, q, sd, Ld);
+}
+
 __global__ void __launch_bounds__(kAT) adj_efield_kernel(Geometry g, AdjPtrs a, const C* U, double gc0, double gc1,
                                                            double gc2, double cn0, double cn1, double cn2, double jz) {
   const L idx = (L)blockIdx.x * blockDim.x + threadIdx.x;
@@ -371,46 +554,47 @@ __global__ void __launch_bounds__(kAT) adj_efield_kernel(Geometry g, AdjPtrs a, 
     store_alg<double, L>(a.LJp, S, 0, s, lp);
     store_alg<double, L>(a.LJm, S, 0, s, lm);
   }
-  for (int mu = 0; mu < 3; mu++) {
-    A8 le;
-    load_alg<double, L>(a.LE, S, mu * 8, s, le);
-    for (int nu = 0; nu < 3; nu++) {
-      if (nu == mu) continue;
-      int dm[3] = {0, 0, 0}, dn[3] = {0, 0, 0};
-      dm[mu] = 1;
-      dn[nu] = 1;
-      M3 Mx;
-      i_herm(le, gc[mu] * cn[nu], Mx);
-      // forward staple: U_mu(x) U_nu(x+mu) U_mu^d(x+nu) U_nu^d(x)
-      {
-        const L sites[4] = {s, nbl(g, x, y, z, dm[0], dm[1], dm[2]), nbl(g, x, y, z, dn[0], dn[1], dn[2]), s};
-        const int mus[4] = {mu, nu, mu, nu};
-        const bool dag[4] = {false, false, true, true};
-        M3 W[4];
-        ld(U, S, mu, sites[0], W[0]);
-        ld(U, S, nu, sites[1], W[1]);
-        M3 t;
-        ld(U, S, mu, sites[2], t);
-        dagger(t, W[2]);
-        ld(U, S, nu, sites[3], t);
-        dagger(t, W[3]);
-        path_vjp(a.LU, S, Mx, W, dag, mus, sites);
-      }
-      // backward staple: U_mu(x) U_nu^d(x+mu-nu) U_mu^d(x-nu) U_nu(x-nu)
-      {
-        const L sites[4] = {s, nbl(g, x, y, z, dm[0] - dn[0], dm[1] - dn[1], dm[2] - dn[2]),
-                            nbl(g, x, y, z, -dn[0], -dn[1], -dn[2]), nbl(g, x, y, z, -dn[0], -dn[1], -dn[2])};
-        const int mus[4] = {mu, nu, mu, nu};
-        const bool dag[4] = {false, true, true, false};
-        M3 W[4], t;
-        ld(U, S, mu, sites[0], W[0]);
-        ld(U, S, nu, sites[1], t);
-        dagger(t, W[1]);
-        ld(U, S, mu, sites[2], t);
-        dagger(t, W[2]);
-        ld(U, S, nu, sites[3], W[3]);
-        path_vjp(a.LU, S, Mx, W, dag, mus, sites);
-      }
+  const int planes[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+#pragma unroll 1
+  for (int pl = 0; pl < 3; pl++) {
+    const int p = planes[pl][0], q = planes[pl][1];
+    int dp[3] = {0, 0, 0}, dq[3] = {0, 0, 0};
+    dp[p] = 1;
+    dq[q] = 1;
+    const L sp = nbl(g, x, y, z, dp[0], dp[1], dp[2]), sq = nbl(g, x, y, z, dq[0], dq[1], dq[2]);
+    const double wp = gc[p] * cn[q], wq = gc[q] * cn[p];
+    M3 A, B, Cc, Dd, M1, M2, Mm3, M4;
+    A8 l;
+    ld(U, S, p, s, A);
+    ld(U, S, q, sp, B);
+    ld(U, S, p, sq, Cc);
+    ld(U, S, q, s, Dd);
+    load_alg<double, L>(a.LE, S, p * 8, s, l);
+    i_herm(l, wp, M1);
+    load_alg<double, L>(a.LE, S, q * 8, s, l);
+    i_herm(l, wq, Mm3);
+    load_alg<double, L>(a.LE, S, q * 8, sp, l);
+    i_herm(l, wq, M4);
+    if (q == 2 && z == g.nz - 1) {
+      set_zero(M2);  // U_p(x+z) is a ghost link: no staple of its own
+    } else {
+      load_alg<double, L>(a.LE, S, p * 8, sq, l);
+      i_herm(l, wp, M2);
+    }
+    plaquette_vjp(a.LU, S, p, q, s, sp, sq, s, A, B, Cc, Dd, M1, M2, Mm3, M4);
+    if (q == 2 && z == 0) {
+      // plaquette at the bottom ghost slice: only the backward staple of U_p(x) (= its c link)
+      const L gs = s - g.plane, gsp = nbl(g, x, y, -1, dp[0], dp[1], 0);
+      ld(U, S, p, gs, A);
+      ld(U, S, q, gsp, B);
+      ld(U, S, p, s, Cc);
+      ld(U, S, q, gs, Dd);
+      load_alg<double, L>(a.LE, S, p * 8, s, l);
+      i_herm(l, wp, M2);
+      set_zero(M1);
+      set_zero(Mm3);
+      set_zero(M4);
+      plaquette_vjp(a.LU, S, p, q, gs, gsp, s, gs, A, B, Cc, Dd, M1, M2, Mm3, M4);
     }
   }
 }

@@ -382,6 +382,19 @@ long long glasma_field_doubles(const glasma_lattice* h, int field) {
   return h->g.S * host_doubles_per_site(field);
 }
 
+// Device address of page-locked (pinned or registered) host memory, else null.  Such memory is
+// read and written in place by the layout kernels over the host link (NVLink-C2C on Grace
+// systems), fusing the copy with the AoS <-> SoA conversion; pageable memory goes through the
+// staging buffer with cudaMemcpyAsync.
+static void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 static int upload_common(glasma_lattice* h, int field, const double* src, cudaMemcpyKind kind) {
   GLASMA_CHECK_HANDLE(h);
   if (!valid_field(field)) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown field");
@@ -390,6 +403,14 @@ static int upload_common(glasma_lattice* h, int field, const double* src, cudaMe
   if (st) return st;
   const int P = host_doubles_per_site(field);
   const size_t bytes = (size_t)h->g.S * P * sizeof(double);
+  if (kind == cudaMemcpyHostToDevice) {
+    if (const double* dsrc = static_cast<const double*>(mapped_host(src))) {
+      cudaError_t e = h->precision == GLASMA_FP64
+                          ? glasma::launch_aos_to_soa<double>(dsrc, static_cast<double*>(h->f[field]), h->g.S, P, h->stream)
+                          : glasma::launch_aos_to_soa<float>(dsrc, static_cast<float*>(h->f[field]), h->g.S, P, h->stream);
+      return e == cudaSuccess ? GLASMA_OK : cuda_fail(e, "aos_to_soa from host");
+    }
+  }
   st = ensure_staging(h, bytes);
   if (st) return st;
   GLASMA_CUDA(cudaMemcpyAsync(h->staging, src, bytes, kind, h->stream), "upload copy");
@@ -408,6 +429,16 @@ static int download_common(glasma_lattice* h, int field, double* dst, cudaMemcpy
   if (st) return st;
   const int P = host_doubles_per_site(field);
   const size_t bytes = (size_t)h->g.S * P * sizeof(double);
+  if (kind == cudaMemcpyDeviceToHost) {
+    if (double* ddst = static_cast<double*>(mapped_host(dst))) {
+      cudaError_t e = h->precision == GLASMA_FP64
+                          ? glasma::launch_soa_to_aos<double>(static_cast<const double*>(h->f[field]), ddst, h->g.S, P, h->stream)
+                          : glasma::launch_soa_to_aos<float>(static_cast<const float*>(h->f[field]), ddst, h->g.S, P, h->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "soa_to_aos to host");
+      GLASMA_CUDA(cudaStreamSynchronize(h->stream), "download sync");
+      return GLASMA_OK;
+    }
+  }
   st = ensure_staging(h, bytes);
   if (st) return st;
   cudaError_t e = h->precision == GLASMA_FP64

@@ -350,7 +350,7 @@ __device__ __forceinline__ T unitarity_norm(const Mat<T>& V) {
 // projection would turn the accumulated non-unitary part into a small rotation of the link, which
 // shows up as a systematic shift of the plaquette energy.)
 template <typename T>
-__device__ __forceinline__ void reunitarize(Mat<T>& V) {
+__device__ __forceinline__ void reunitarize_newton(Mat<T>& V) {
   Mat<double> U;
 #pragma unroll
   for (int k = 0; k < 9; k++) U.e[k] = mk<double>((double)V.e[k].re, (double)V.e[k].im);
@@ -416,6 +416,66 @@ __device__ __forceinline__ void reunitarize(Mat<T>& V) {
     cfma(w, U.e[k], ph);
     V.e[k] = mk<T>((T)w.re, (T)w.im);
   }
+}
+
+// Same projection for FP32 links in FP32 arithmetic: Newton-Schulz steps U <- U (3 - U^d U) / 2, which
+// converge quadratically to the same polar factor without an inverse (U = W (1 + e), e Hermitian,
+// becomes W (1 - e^2)), then the determinant's phase is divided out.  Links that drifted far from
+// SU(3) (||1 - U^d U|| > 0.25, outside the fast-convergence region) take the FP64 Newton path.
+__device__ __forceinline__ void reunitarize_f32(Mat<float>& U) {
+  Mat<float> H, K, X;
+  mul_dn(U, U, H);
+  float dev = 0.f;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const float d = H.e[k].re - ((k % 4 == 0) ? 1.f : 0.f);
+    dev = fmaf(d, d, fmaf(H.e[k].im, H.e[k].im, dev));
+  }
+  if (!(dev <= 0.0625f)) {
+    reunitarize_newton(U);
+    return;
+  }
+#pragma unroll 1
+  for (int it = 0; it < 2; it++) {
+    if (it > 0) mul_dn(U, U, H);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      K.e[k].re = ((k % 4 == 0) ? 1.5f : 0.f) - 0.5f * H.e[k].re;
+      K.e[k].im = -0.5f * H.e[k].im;
+    }
+    mul_nn(U, K, X);
+    U = X;
+  }
+  cx<float> det = mk<float>(0, 0);
+  {
+    cx<float> c0 = mk<float>(0, 0), c1 = mk<float>(0, 0), c2 = mk<float>(0, 0);
+    cfma(c0, U.e[4], U.e[8]);
+    cfma(c0, mk<float>(-U.e[7].re, -U.e[7].im), U.e[5]);
+    cfma(c1, U.e[5], U.e[6]);
+    cfma(c1, mk<float>(-U.e[8].re, -U.e[8].im), U.e[3]);
+    cfma(c2, U.e[3], U.e[7]);
+    cfma(c2, mk<float>(-U.e[6].re, -U.e[6].im), U.e[4]);
+    cfma(det, U.e[0], c0);
+    cfma(det, U.e[1], c1);
+    cfma(det, U.e[2], c2);
+  }
+  float sp, cp;
+  sincosf(-atan2f(det.im, det.re) * (1.f / 3.f), &sp, &cp);
+  const cx<float> ph = mk<float>(cp, sp);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    cx<float> w = mk<float>(0, 0);
+    cfma(w, U.e[k], ph);
+    U.e[k] = w;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void reunitarize(Mat<T>& V) {
+  if constexpr (sizeof(T) == 4)
+    reunitarize_f32(V);
+  else
+    reunitarize_newton(V);
 }
 
 }  // namespace glasma

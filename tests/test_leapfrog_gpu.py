@@ -44,6 +44,24 @@ def test_upload_download_roundtrip_is_bit_exact():
             assert np.array_equal(lat.download(k), v), k
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pinned_host_buffers_give_the_same_bytes(precision):
+    """Page-locked host buffers are read/written in place by the layout kernels; pageable ones are
+    staged.  Both routes must move exactly the same values."""
+    torch = pytest.importorskip("torch")
+    N = (6, 5, 7)
+    f = O.random_fields(N, 4)
+    with Lattice(N, precision=precision) as a, Lattice(N, precision=precision) as b:
+        for k in ("U", "E", "Jp"):
+            pinned = torch.from_numpy(f[k].view(np.float64).copy()).pin_memory()
+            a.upload(k, pinned)
+            b.upload(k, f[k])
+            out_pinned = torch.empty_like(pinned).pin_memory()
+            a.download(k, out_pinned)
+            out_pageable = b.download(k)
+            assert np.array_equal(out_pinned.numpy(), out_pageable.view(np.float64).reshape(out_pinned.shape)), k
+
+
 @pytest.mark.parametrize("tag,nsteps", [("s1", 1), ("s10", 10)])
 def test_leapfrog_matches_reference_golden(golden_dir, tag, nsteps):
     g = _load(golden_dir, "leapfrog_random.npz")
