@@ -483,8 +483,18 @@ __global__ void __launch_bounds__(kAT) adj_jstat_kernel(Geometry g, AdjPtrs a, c
 // gradients see) at 22 instead of 36 matmuls and a quarter of the atomics.  Open z: a plaquette at
 // the top slice has no M2 term (its link at x+z is a ghost), and the threads of slice 0 also take
 // the M2 term of the plaquette at the bottom ghost slice (the backward staple of U_p(x, z=0)).
-__device__ void plaquette_vjp(C* LU, L S, int p, int q, L sa, L sb, L sc, L sd, const M3& a, const M3& b,
-                              const M3& c, const M3& d, const M3& M1, const M3& M2, const M3& Mm3, const M3& M4) {
+__device__ __forceinline__ void atomic_add_alg(double* F, L S, int base, L s, double w, const A8& v) {
+  double* q = F + (L)base * S + s;
+#pragma unroll
+  for (int k = 0; k < 8; k++) atomicAdd(q + (L)k * S, w * v.a[k]);
+}
+
+// Also undoes this plaquette's share of the electric-field update on E (E_{t+1} -> E_t): the force
+// on a is wp ReTr(i t P), on d wq ReTr(i t P^d) = -wq ReTr(i t P), on c wp ReTr(i t d^d P^d d), on b
+// wq ReTr(i t a^d P a); rev_mask bit k selects the links (a, b, c, d) whose force is removed.
+__device__ void plaquette_vjp(C* LU, double* E, L S, int p, int q, L sa, L sb, L sc, L sd, const M3& a,
+                              const M3& b, const M3& c, const M3& d, const M3& M1, const M3& M2, const M3& Mm3,
+                              const M3& M4, double wp, double wq, unsigned rev_mask) {
   M3 cd, P, t, N;
   mul_dd(c, d, cd);  // c^d d^d
   mul_nn(a, b, t);
@@ -519,6 +529,13 @@ __device__ void plaquette_vjp(C* LU, L S, int p, int q, L sa, L sb, L sc, L sd, 
     mul_nn(P, a, u);  // P a M4
     mul_nn(u, M4, v);
     axpy(1.0, v, La);
+    if (rev_mask & 2u) {  // force on b: a^d (P a)
+      M3 r;
+      A8 fb;
+      mul_dn(a, u, r);
+      retr_itg(r, 1.0, fb);
+      atomic_add_alg(E, S, q * 8, sb, -wq, fb);
+    }
     mul_nd(M2, d, u);  // -(M2 d^d P)^d
     mul_nn(u, P, v);
     dagger(v, vd);
@@ -526,6 +543,19 @@ __device__ void plaquette_vjp(C* LU, L S, int p, int q, L sa, L sb, L sc, L sd, 
     mul_nn(P, d, u);  // -P d M2
     mul_nn(u, M2, v);
     axpy(-1.0, v, Ld);
+    if (rev_mask & 4u) {  // force on c: (P d)^d d
+      M3 r;
+      A8 fc;
+      mul_dn(u, d, r);
+      retr_itg(r, 1.0, fc);
+      atomic_add_alg(E, S, p * 8, sc, -wp, fc);
+    }
+  }
+  if (rev_mask & 9u) {  // forces on a and d
+    A8 fa;
+    retr_itg(P, 1.0, fa);
+    if (rev_mask & 1u) atomic_add_alg(E, S, p * 8, sa, -wp, fa);
+    if (rev_mask & 8u) atomic_add_alg(E, S, q * 8, sd, wq, fa);
   }
   atomic_add_link(LU, S, p, sa, La);
   atomic_add_link(LU, S, q, sb, Lb);
@@ -533,8 +563,9 @@ __device__ void plaquette_vjp(C* LU, L S, int p, int q, L sa, L sb, L sc, L sd, 
   atomic_add_link(LU, S, q, sd, Ld);
 }
 
-__global__ void __launch_bounds__(kAT) adj_efield_kernel(Geometry g, AdjPtrs a, const C* U, double gc0, double gc1,
-                                                           double gc2, double cn0, double cn1, double cn2, double jz) {
+__global__ void __launch_bounds__(kAT) adj_efield_kernel(Geometry g, AdjPtrs a, const C* U, double* E, const double* Jp,
+                                                           const double* Jm, double gc0, double gc1, double gc2,
+                                                           double cn0, double cn1, double cn2, double jz) {
   const L idx = (L)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.vol) return;
   int x, y, z;
@@ -553,6 +584,13 @@ __global__ void __launch_bounds__(kAT) adj_efield_kernel(Geometry g, AdjPtrs a, 
     }
     store_alg<double, L>(a.LJp, S, 0, s, lp);
     store_alg<double, L>(a.LJm, S, 0, s, lm);
+    // E_z(t) = E_z(t+1) - jz (Jp - Jm)(t); the plaquette forces are removed below
+    A8 jp, jm, dj;
+    load_alg<double, L>(Jp, S, 0, s, jp);
+    load_alg<double, L>(Jm, S, 0, s, jm);
+#pragma unroll
+    for (int k = 0; k < 8; k++) dj.a[k] = jp.a[k] - jm.a[k];
+    atomic_add_alg(E, S, 16, s, -jz, dj);
   }
   const int planes[3][2] = {{0, 1}, {0, 2}, {1, 2}};
 #pragma unroll 1
@@ -575,13 +613,14 @@ __global__ void __launch_bounds__(kAT) adj_efield_kernel(Geometry g, AdjPtrs a, 
     i_herm(l, wq, Mm3);
     load_alg<double, L>(a.LE, S, q * 8, sp, l);
     i_herm(l, wq, M4);
-    if (q == 2 && z == g.nz - 1) {
+    const bool top = (q == 2 && z == g.nz - 1);
+    if (top) {
       set_zero(M2);  // U_p(x+z) is a ghost link: no staple of its own
     } else {
       load_alg<double, L>(a.LE, S, p * 8, sq, l);
       i_herm(l, wp, M2);
     }
-    plaquette_vjp(a.LU, S, p, q, s, sp, sq, s, A, B, Cc, Dd, M1, M2, Mm3, M4);
+    plaquette_vjp(a.LU, E, S, p, q, s, sp, sq, s, A, B, Cc, Dd, M1, M2, Mm3, M4, wp, wq, top ? 11u : 15u);
     if (q == 2 && z == 0) {
       // plaquette at the bottom ghost slice: only the backward staple of U_p(x) (= its c link)
       const L gs = s - g.plane, gsp = nbl(g, x, y, -1, dp[0], dp[1], 0);
@@ -594,7 +633,7 @@ __global__ void __launch_bounds__(kAT) adj_efield_kernel(Geometry g, AdjPtrs a, 
       set_zero(M1);
       set_zero(Mm3);
       set_zero(M4);
-      plaquette_vjp(a.LU, S, p, q, gs, gsp, s, gs, A, B, Cc, Dd, M1, M2, Mm3, M4);
+      plaquette_vjp(a.LU, E, S, p, q, gs, gsp, s, gs, A, B, Cc, Dd, M1, M2, Mm3, M4, wp, wq, 4u);
     }
   }
 }
@@ -899,12 +938,13 @@ int glasma_adjoint(glasma_lattice* h, double dt, int nsteps, int checkpoint_ever
     adj_jstat_kernel<<<gridv(g.vol), kAT, 0, stm>>>(g, ap, U, Jp, Jm, cj);
     // JStat_t: the JStat sub-step with -dt
     launch_jstat_only<double>(g, fp, -dt, h->tile_x, stm);
-    // adjoint of the electric-field update (needs U_t)
-    adj_efield_kernel<<<gridv(g.vol), kAT, 0, stm>>>(g, ap, U, gamma / (g.a[0] * g.a[0]), gamma / (g.a[1] * g.a[1]),
-                                                    gamma / (g.a[2] * g.a[2]), 1.0 / (g.a[0] * g.a[0]),
-                                                    1.0 / (g.a[1] * g.a[1]), 1.0 / (g.a[2] * g.a[2]), jz);
-    // E_t: the electric-field sub-step with -dt
-    launch_efield_only<double>(g, fp, -dt, h->tile_x, stm);
+    // adjoint of the electric-field update (needs U_t), and E_t from E_{t+1}: the same plaquettes
+    // give the force that the sub-step added, which is removed again (then the E ghosts re-synced)
+    adj_efield_kernel<<<gridv(g.vol), kAT, 0, stm>>>(g, ap, U, E, Jp, Jm, gamma / (g.a[0] * g.a[0]),
+                                                    gamma / (g.a[1] * g.a[1]), gamma / (g.a[2] * g.a[2]),
+                                                    1.0 / (g.a[0] * g.a[0]), 1.0 / (g.a[1] * g.a[1]),
+                                                    1.0 / (g.a[2] * g.a[2]), jz);
+    launch_sync_ghosts<double>(g, E, 24, stm);
     // re-anchor on a stored checkpoint
     if (t % checkpoint_every == 0) load_state(t / checkpoint_every);
     cudaError_t e = cudaGetLastError();

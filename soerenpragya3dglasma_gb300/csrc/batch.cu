@@ -52,12 +52,17 @@ __device__ __forceinline__ int find_event(const EventDesc<T>* __restrict__ ev, i
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
     efield_batch_kernel(const EventDesc<T>* __restrict__ ev, int n, long long total) {
+  __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     const int e = find_event(ev, n, t, true);
+    // Local copies: the site body stores through these pointers, so references into the table
+    // would have to be re-read from global memory after every store.
     const Geometry g = ev[e].g;
+    const FieldPtrs<T> f = ev[e].f;
+    const EParams<T> ep = ev[e].ep;
+    const TileMap tm = ev[e].tm;
     int x, y, z;
-    if (ev[e].tm.site(t - ev[e].k1_begin, threadIdx.x, g.nx, g.ny, x, y, z))
-      efield_site<T, I>(g, ev[e].f, ev[e].ep, x, y, z);
+    if (tm.site(t - ev[e].k1_begin, threadIdx.x, g.nx, g.ny, x, y, z)) efield_site<T, I>(g, f, ep, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
   }
 }
 
@@ -67,8 +72,10 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     const int e = find_event(ev, n, t, false);
     const Geometry g = ev[e].g;
+    const FieldPtrs<T> f = ev[e].f;
+    const LParams<T> lp = ev[e].lp;
     const long long idx = (t - ev[e].k2_begin) * kThreads + threadIdx.x;
-    if (idx < g.vol) links_site<T, I>(g, ev[e].f, ev[e].lp, (I)idx);
+    if (idx < g.vol) links_site<T, I>(g, f, lp, (I)idx);
   }
 }
 

@@ -26,9 +26,10 @@ namespace {
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
     efield_jstat_kernel(Geometry g, FieldPtrs<T> f, EParams<T> p, TileMap tm) {
+  __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   int x, y, z;
   if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
-  efield_site<T, I>(g, f, p, x, y, z);
+  efield_site<T, I>(g, f, p, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
 }
 
 template <typename T, typename I>
@@ -42,9 +43,10 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kFusedMinBlocks)
     fused_step_kernel(Geometry g, FieldPtrs<T> in, FieldPtrs<T> out, EParams<T> pe, LParams<T> pl, TileMap tm) {
+  __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   int x, y, z;
   if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
-  fused_site<T, I>(g, in, out, pe, pl, x, y, z);
+  fused_site<T, I>(g, in, out, pe, pl, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
 }
 
 template <typename T, typename I>

@@ -69,14 +69,45 @@ __device__ __forceinline__ void axpy_diff(Alg<T>& acc, T c, const Alg<T>& a, con
   for (int k = 0; k < 8; k++) acc.a[k] += c * (a.a[k] - b.a[k]);
 }
 
+// FP64 staple sharing: for mu < nu the first product of link mu's upper staple in plane nu,
+// A = U_nu(x+mu) U_mu^d(x+nu), is the dagger of the first product of link nu's upper staple in plane
+// mu, so it is formed once and parked in the thread's own shared-memory slot until link nu needs it
+// (3 of the 27 staple matmuls saved; two slots suffice since the links are processed in order).
+// FP32 keeps the L1 for neighbour links instead (GLASMA_FP32_STAPLE_SHARE=1 turns it on there too).  Slot k, element e of thread t: sh[(k*9+e)*kThreads+t].
+#ifndef GLASMA_FP32_STAPLE_SHARE
+#define GLASMA_FP32_STAPLE_SHARE 0
+#endif
+template <typename T>
+struct StapleShare {
+  static constexpr int kSlots = (sizeof(T) == 8 || GLASMA_FP32_STAPLE_SHARE) ? 2 : 0;
+};
+enum StapleMode { kStapleCompute = 0, kStapleStore = 1, kStapleReuse = 2 };
+
 // Staples of link mu at x in the (mu,nu) plane, weighted by c, added to acc.
 template <typename T, typename I>
 __device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, I S, int mu, int nu, I s, I s_pmu, I s_pnu,
-                                            I s_pmu_mnu, I s_mnu, T c, Mat<T>& acc) {
+                                            I s_pmu_mnu, I s_mnu, T c, Mat<T>& acc, cx<T>* sh = nullptr,
+                                            int mode = kStapleCompute, int slot = 0) {
   Mat<T> a, b, t;
-  load_link(U, S, nu, s_pmu, a);
-  load_link(U, S, mu, s_pnu, b);
-  mul_nd(a, b, t);
+  if (sh && mode == kStapleReuse) {
+    const cx<T>* q = sh + (slot * 9) * kThreads + threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const cx<T> v = q[(j + 3 * i) * kThreads];
+        t.e[i + 3 * j] = mk<T>(v.re, -v.im);
+      }
+  } else {
+    load_link(U, S, nu, s_pmu, a);
+    load_link(U, S, mu, s_pnu, b);
+    mul_nd(a, b, t);
+    if (sh && mode == kStapleStore) {
+      cx<T>* q = sh + (slot * 9) * kThreads + threadIdx.x;
+#pragma unroll
+      for (int k = 0; k < 9; k++) q[k * kThreads] = t.e[k];
+    }
+  }
   load_link(U, S, nu, s, a);
   add_mul_nd(t, a, c, acc);
   load_link(U, S, nu, s_pmu_mnu, a);
@@ -99,7 +130,7 @@ struct EParams {
 // The electric-field and JStat update of one site (K1's per-site body).
 template <typename T, typename I>
 __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T>& f, const EParams<T>& p, int x, int y,
-                                            int z) {
+                                            int z, cx<T>* sh = nullptr) {
   const I S = (I)g.S, plane = (I)g.plane;
   const I s = (I)x + (I)g.nx * ((I)y + (I)g.ny * (I)(z + 1));
   const bool lo = (z == 0), hi = (z == g.nz - 1);
@@ -113,18 +144,18 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
       Mat<T> acc;
       set_zero(acc);
       if (mu == 0) {
-        add_staples(f.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc);
-        add_staples(f.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc);
+        add_staples(f.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc, sh, kStapleStore, 0);
+        add_staples(f.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc, sh, kStapleStore, 1);
       } else if (mu == 1) {
-        add_staples(f.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc);
-        add_staples(f.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc);
+        add_staples(f.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc, sh, kStapleReuse, 0);
+        add_staples(f.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc, sh, kStapleStore, 0);
       } else {
-        add_staples(f.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc);
-        add_staples(f.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc);
+        add_staples(f.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc, sh, kStapleReuse, 1);
+        add_staples(f.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc, sh, kStapleReuse, 0);
       }
       Mat<T> u, P;
       load_link(f.U, S, mu, s, u);
-      mul_nn(u, acc, P);
+      mul_nn_traceless(u, acc, P);
       Alg<T> force, e;
       retr_itg(P, pick3(p.gc, mu), force);
       load_alg(f.E, S, mu * 8, s, e);
@@ -214,8 +245,17 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
     Alg<T> e;
     load_alg(f.E, S, mu * 8, s, e);
     Mat<T> X, u, uh;
-    expi(pick3(p.cU, mu), e, X);
     load_link(f.U, S, mu, s, u);
+    // Without a use for U(t+dt/2) (UOld, the z-link J transport), the two half steps are one:
+    // exp(i c t.E)^2 = exp(2i c t.E), one matmul less (equal up to rounding).
+    if (p.do_second && !p.save_uold && !(mu == 2 && p.do_j)) {
+      expi(T(2) * pick3(p.cU, mu), e, X);
+      mul_nn(X, u, uh);
+      store_link(f.U, S, mu, s, uh);
+      if (sg >= 0) store_link(f.U, S, mu, sg, uh);
+      continue;
+    }
+    expi(pick3(p.cU, mu), e, X);
     mul_nn(X, u, uh);
     if (p.save_uold) {
       store_link(f.UOld, S, mu, s, uh);
@@ -323,7 +363,8 @@ __device__ __forceinline__ void fused_currents(const FieldPtrs<T>& in, const Fie
 
 template <typename T, typename I>
 __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>& in, const FieldPtrs<T>& out,
-                                           const EParams<T>& pe, const LParams<T>& pl, int x, int y, int z) {
+                                           const EParams<T>& pe, const LParams<T>& pl, int x, int y, int z,
+                                           cx<T>* sh = nullptr) {
   const I S = (I)g.S, plane = (I)g.plane;
   const I s = (I)x + (I)g.nx * ((I)y + (I)g.ny * (I)(z + 1));
   const bool lo = (z == 0), hi = (z == g.nz - 1);
@@ -337,18 +378,18 @@ __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>
     Mat<T> acc;
     set_zero(acc);
     if (mu == 0) {
-      add_staples(in.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, pe.cnu[1], acc);
-      add_staples(in.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, pe.cnu[2], acc);
+      add_staples(in.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, pe.cnu[1], acc, sh, kStapleStore, 0);
+      add_staples(in.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, pe.cnu[2], acc, sh, kStapleStore, 1);
     } else if (mu == 1) {
-      add_staples(in.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, pe.cnu[0], acc);
-      add_staples(in.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, pe.cnu[2], acc);
+      add_staples(in.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, pe.cnu[0], acc, sh, kStapleReuse, 0);
+      add_staples(in.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, pe.cnu[2], acc, sh, kStapleStore, 0);
     } else {
-      add_staples(in.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, pe.cnu[0], acc);
-      add_staples(in.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, pe.cnu[1], acc);
+      add_staples(in.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, pe.cnu[0], acc, sh, kStapleReuse, 1);
+      add_staples(in.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, pe.cnu[1], acc, sh, kStapleReuse, 0);
     }
     Mat<T> u, w;
     load_link(in.U, S, mu, s, u);
-    mul_nn(u, acc, w);
+    mul_nn_traceless(u, acc, w);
     Alg<T> force, e;
     retr_itg(w, pick3(pe.gc, mu), force);
     load_alg(in.E, S, mu * 8, s, e);
@@ -366,6 +407,15 @@ __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>
       if (sg >= 0) store_alg(in.E, S, mu * 8, sg, e);
     }
     Mat<T> X, uh;
+    if (!pl.save_uold && mu != 2) {  // one exp at twice the angle, as in links_site
+      expi(T(2) * pick3(pl.cU, mu), e, X);
+      mul_nn(X, u, w);
+      if (!dry) {
+        store_link(out.U, S, mu, s, w);
+        if (sg >= 0) store_link(out.U, S, mu, sg, w);
+      }
+      continue;
+    }
     expi(pick3(pl.cU, mu), e, X);
     mul_nn(X, u, uh);
     if (pl.save_uold && !dry) {

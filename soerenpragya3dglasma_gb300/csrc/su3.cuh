@@ -209,13 +209,56 @@ __device__ __forceinline__ void alg_from_herm(const Mat<T>& W, Alg<T>& out) {
   out.a[7] = (W.e[0].re + W.e[4].re - T(2) * W.e[8].re) * Consts<T>::inv_sqrt3();
 }
 
+// The entries of a Hermitian product that alg_from_herm reads: the upper triangle (0,1), (0,2),
+// (1,2) and the real diagonal.  Same arithmetic, per entry, as mul_nd / mul_nn.
+template <typename T>
+__device__ __forceinline__ void mul_nd_herm(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          acc.re = fma(A.e[i + 3 * k].re, B.e[j + 3 * k].re, acc.re);
+          acc.re = fma(A.e[i + 3 * k].im, B.e[j + 3 * k].im, acc.re);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma_nc(acc, A.e[i + 3 * k], B.e[j + 3 * k]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+}
+template <typename T>
+__device__ __forceinline__ void mul_nn_herm(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          acc.re = fma(A.e[i + 3 * k].re, B.e[k + 3 * j].re, acc.re);
+          acc.re = fma(-A.e[i + 3 * k].im, B.e[k + 3 * j].im, acc.re);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma(acc, A.e[i + 3 * k], B.e[k + 3 * j]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+}
+
 // out = V (t.e) V^dagger  (AdjointMultiplication)
 template <typename T>
 __device__ __forceinline__ void adj_mul(const Mat<T>& V, const Alg<T>& e, Alg<T>& out) {
   Mat<T> M, W, R;
   herm_from_alg(e, M);
   mul_nn(V, M, W);
-  mul_nd(W, V, R);
+  mul_nd_herm(W, V, R);
   alg_from_herm(R, out);
 }
 // out = V^dagger (t.e) V  (InverseAdjointMultiplication)
@@ -224,8 +267,31 @@ __device__ __forceinline__ void inv_adj_mul(const Mat<T>& V, const Alg<T>& e, Al
   Mat<T> M, W, R;
   herm_from_alg(e, M);
   mul_dn(V, M, W);
-  mul_nn(W, V, R);
+  mul_nn_herm(W, V, R);
   alg_from_herm(R, out);
+}
+
+// The entries of C = A B that retr_itg reads: every off-diagonal entry and the imaginary diagonal.
+// Same arithmetic, per entry, as mul_nn.
+template <typename T>
+__device__ __forceinline__ void mul_nn_traceless(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          acc.im = fma(A.e[i + 3 * k].re, B.e[k + 3 * j].im, acc.im);
+          acc.im = fma(A.e[i + 3 * k].im, B.e[k + 3 * j].re, acc.im);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma(acc, A.e[i + 3 * k], B.e[k + 3 * j]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
 }
 
 template <typename T>
@@ -253,7 +319,12 @@ __device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
   for (int a = 0; a < 8; a++) sc.a[a] = c * al.a[a];
   Mat<T> Q, Q2;
   herm_from_alg(sc, Q);
-  mul_nn(Q, Q, Q2);
+  // Q^2 is Hermitian: its upper triangle and real diagonal, the rest by conjugation
+  mul_nn_herm(Q, Q, Q2);
+  Q2.e[1] = mk<T>(Q2.e[3].re, -Q2.e[3].im);
+  Q2.e[2] = mk<T>(Q2.e[6].re, -Q2.e[6].im);
+  Q2.e[5] = mk<T>(Q2.e[7].re, -Q2.e[7].im);
+  Q2.e[0].im = Q2.e[4].im = Q2.e[8].im = T(0);
   const T c1 = T(0.5) * (Q2.e[0].re + Q2.e[4].re + Q2.e[8].re);
   // det Q = Q00 (Q11 Q22 - |Q12|^2) - ... ; real for Hermitian Q.  Expanded in the
   // Gell-Mann components for brevity: det Q = tr(Q^3)/3.
@@ -289,9 +360,9 @@ __device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
     } else {
       xi0 = sw / w;
     }
-    T s2u, c2u, su, cu;
-    Trig<T>::sincos_(T(2) * u, &s2u, &c2u);
+    T su, cu;
     Trig<T>::sincos_(u, &su, &cu);
+    const T c2u = cu * cu - su * su, s2u = T(2) * su * cu;  // e^{2iu} = (e^{iu})^2
     // e^{-iu} = (cu, -su)
     // h0 = (u^2-w^2) e^{2iu} + e^{-iu} (8u^2 cos w + 2iu(3u^2+w^2) xi0)
     const T a0r = T(8) * u2 * cw, a0i = T(2) * u * (T(3) * u2 + w2) * xi0;

@@ -175,7 +175,10 @@ def test_mv_collision_matches_reference_golden(golden_dir):
         lat.step(dt, int(g["cfg_steps"]))
         assert np.allclose(lat.bulk(), g["t8_bulk"], rtol=1e-11, atol=1e-11)
         assert np.allclose(lat.gauss(), g["t8_gauss"], rtol=1e-10, atol=1e-15)
-        assert np.allclose(lat.emt_map(), g["t8_emt"], rtol=1e-10, atol=1e-14)
+        # the map's entries (~1e-6 here) are slice averages of 3 - ReTr P with P ~ 1: FP64 rounding of
+        # the O(1) plaquettes leaves ~1e-14 absolute, whatever the operation order (the link update
+        # forms exp(2iQ) once where the reference applies exp(iQ) twice)
+        assert np.allclose(lat.emt_map(), g["t8_emt"], rtol=1e-10, atol=1e-13)
 
 
 def test_observables_match_oracle_on_larger_lattice(oracle):
