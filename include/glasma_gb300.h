@@ -238,8 +238,8 @@ const char* glasma_adjoint_last_error(void);
 /* ---- Batches of independent events (lattices of uneven sizes) advanced together.
  * No reference counterpart: the reference runs one event per process (seeds are farmed out as
  * separate jobs).  Each event is an ordinary lattice handle (glasma_batch_event gives it, for
- * uploads, downloads and observables); a batch step is one persistent launch per leapfrog kernel
- * over all events' tiles, bit-identical to stepping each event alone.  use_graph != 0 replays
+ * uploads, downloads and observables); a batch step is one launch per leapfrog kernel over all
+ * events' tiles (glasma_batch_set_launch), bit-identical to stepping each event alone.  use_graph != 0 replays
  * blocks of steps (reunitarize_every steps, or 16) from a CUDA graph captured on first use.
  * extents / spacings: 3 values per event. */
 typedef struct glasma_batch glasma_batch;
@@ -251,6 +251,13 @@ int glasma_batch_event(glasma_batch* b, int event, glasma_lattice** out);
 /* Autotunes the electric-field tile once per distinct lattice shape; tiles (may be NULL): n_events ints. */
 int glasma_batch_autotune(glasma_batch* b, double dt, int* tiles);
 int glasma_batch_step(glasma_batch* b, double dt, int nsteps, int use_graph);
+/* Launch shape of the two batch kernels (both cover all events in one launch):
+ * GLASMA_BATCH_PERSISTENT — as many blocks as the device holds at once, each walking the tile list;
+ * GLASMA_BATCH_TILE_GRID — one block per tile (warps of a block start together on their tile, which
+ * keeps the long per-site body in the instruction cache; the default).  Same arithmetic either way. */
+#define GLASMA_BATCH_PERSISTENT 0
+#define GLASMA_BATCH_TILE_GRID 1
+int glasma_batch_set_launch(glasma_batch* b, int mode);
 /* Per-event T00 (volume sum, FP64 reductions), n_events doubles. */
 int glasma_batch_energy(glasma_batch* b, double* t00);
 int glasma_batch_synchronize(glasma_batch* b);

@@ -52,6 +52,11 @@ class Batch:
         _bcheck(self.lib, self.lib.glasma_batch_autotune(self.b, float(dt), t))
         return list(t)
 
+    def set_launch(self, mode):
+        """"tile_grid" (default: one block per tile) or "persistent" (a device-filling grid walking the
+        tile list); both cover all events in one launch per kernel and give the same fields."""
+        _bcheck(self.lib, self.lib.glasma_batch_set_launch(self.b, {"persistent": 0, "tile_grid": 1}[mode]))
+
     def step(self, dt, nsteps, use_graph=True):
         _bcheck(self.lib, self.lib.glasma_batch_step(self.b, float(dt), int(nsteps), int(bool(use_graph))))
 

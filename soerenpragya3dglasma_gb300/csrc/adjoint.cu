@@ -254,7 +254,8 @@ __device__ void path_vjp(C* LU, L S, const M3& Mx, const M3 (&W)[4], const bool 
 }
 
 // ---------------------------------------------------------------- reverse reconstruction
-// U_{t+1} = X X U_t: store X = exp(i cU E_{t+1}) and Uh = X^d U_{t+1}; leave U = Uh (for the J inversion).
+// z link: U_{t+1} = X X U_t, store X = exp(i cU E_{t+1}) and Uh = X^d U_{t+1}, leave U = Uh (for the J
+// inversion); x, y links: U_{t+1} = X2 U_t, store X2 = exp(2i cU E_{t+1}), leave U = U_t.
 __global__ void __launch_bounds__(kAT) rev_links_kernel(Geometry g, C* U, const double* E, C* X, C* Uh, double c0,
                                                           double c1, double c2) {
   const L idx = (L)blockIdx.x * blockDim.x + threadIdx.x;
@@ -265,26 +266,26 @@ __global__ void __launch_bounds__(kAT) rev_links_kernel(Geometry g, C* U, const 
     A8 e;
     load_alg<double, L>(E, g.S, mu * 8, s, e);
     M3 x, u, uh;
-    expi(cU[mu], e, x);
+    // the x and y links advance in one step U_{t+1} = exp(2i cU t.E) U_t (as the forward step
+    // computes them): X holds that exponential and U_t follows at once; the z link keeps its half step
+    expi(mu == 2 ? cU[mu] : 2.0 * cU[mu], e, x);
     ld(U, g.S, mu, s, u);
     mul_dn(x, u, uh);
     st(X, g.S, mu, s, x);
-    st(Uh, g.S, mu, s, uh);
+    if (mu == 2) st(Uh, g.S, mu, s, uh);
     st(U, g.S, mu, s, uh);
   }
 }
-// U <- X^d U  (from Uh to U_t)
+// U_z <- X^d U_z  (from the half step to U_t)
 __global__ void __launch_bounds__(kAT) rev_links2_kernel(Geometry g, C* U, const C* X) {
   const L idx = (L)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.vol) return;
   const L s = idx + g.plane;
-  for (int mu = 0; mu < 3; mu++) {
-    M3 x, u, o;
-    ld(X, g.S, mu, s, x);
-    ld(U, g.S, mu, s, u);
-    mul_dn(x, u, o);
-    st(U, g.S, mu, s, o);
-  }
+  M3 x, u, o;
+  ld(X, g.S, 2, s, x);
+  ld(U, g.S, 2, s, u);
+  mul_dn(x, u, o);
+  st(U, g.S, 2, s, o);
 }
 
 // ---------------------------------------------------------------- adjoint sub-steps
@@ -366,9 +367,22 @@ __global__ void __launch_bounds__(kAT) adj_links_kernel(Geometry g, AdjPtrs a, c
   for (int mu = 0; mu < 3; mu++) {
     M3 xx, uh, u, lu, luh, lx, t1;
     ld(X, S, mu, s, xx);
-    ld(Uh, S, mu, s, uh);
     ld(U, S, mu, s, u);
     ld(a.LU, S, mu, s, lu);
+    if (mu != 2) {  // U_{t+1} = X2 U_t with X2 = exp(2i cU t.E)
+      A8 e, le, dl;
+      mul_dn(xx, lu, luh);
+      st(a.LU, S, mu, s, luh);
+      mul_nd(lu, u, lx);
+      load_alg<double, L>(E, S, mu * 8, s, e);
+      expi_vjp(2.0 * cU[mu], e, lx, dl);
+      load_alg<double, L>(a.LE, S, mu * 8, s, le);
+#pragma unroll
+      for (int k = 0; k < 8; k++) le.a[k] += dl.a[k];
+      store_alg<double, L>(a.LE, S, mu * 8, s, le);
+      continue;
+    }
+    ld(Uh, S, mu, s, uh);
     // A5: U1 = X Uh
     mul_dn(xx, lu, luh);
     mul_nd(lu, uh, lx);
@@ -492,23 +506,57 @@ __device__ __forceinline__ void atomic_add_alg(double* F, L S, int base, L s, do
 // Also undoes this plaquette's share of the electric-field update on E (E_{t+1} -> E_t): the force
 // on a is wp ReTr(i t P), on d wq ReTr(i t P^d) = -wq ReTr(i t P), on c wp ReTr(i t d^d P^d d), on b
 // wq ReTr(i t a^d P a); rev_mask bit k selects the links (a, b, c, d) whose force is removed.
+// V M V^d for anti-Hermitian M: the result is anti-Hermitian, so only its upper triangle and
+// imaginary diagonal are formed and the rest filled by -conjugation.
+__device__ __forceinline__ void conj_antiherm(const M3& V, const M3& M, M3& out) {
+  M3 VM;
+  mul_nn(V, M, VM);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      C acc = mk<double>(0, 0);
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {  // Im sum_k VM_ik conj(V_ik)
+          acc.im = fma(-VM.e[i + 3 * k].re, V.e[i + 3 * k].im, acc.im);
+          acc.im = fma(VM.e[i + 3 * k].im, V.e[i + 3 * k].re, acc.im);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma_nc(acc, VM.e[i + 3 * k], V.e[j + 3 * k]);
+        out.e[j + 3 * i] = mk<double>(-acc.re, acc.im);
+      }
+      out.e[i + 3 * j] = acc;
+    }
+}
+
+// Also undoes this plaquette's share of the electric-field update on E (E_{t+1} -> E_t): the force
+// on a is wp ReTr(i t P), on d -wq ReTr(i t P), on c wp ReTr(i t d^d P^d d), on b wq ReTr(i t a^d P a);
+// rev_mask bit k selects the links (a, b, c, d) whose force is removed.
+// With D = P - P^d and the M's anti-Hermitian, the explicit a- and d-dependence of N contributes
+// D a M4 to a's cotangent and -D d M2 to d's, and the b and c forces are (1/2) ReTr(i t a^d D a) and
+// -(1/2) ReTr(i t d^d D d) (ReTr(i t X) only sees the anti-Hermitian part of X).
 __device__ void plaquette_vjp(C* LU, double* E, L S, int p, int q, L sa, L sb, L sc, L sd, const M3& a,
                               const M3& b, const M3& c, const M3& d, const M3& M1, const M3& M2, const M3& Mm3,
                               const M3& M4, double wp, double wq, unsigned rev_mask) {
-  M3 cd, P, t, N;
+  M3 cd, P, t, N, Dm;
   mul_dd(c, d, cd);  // c^d d^d
   mul_nn(a, b, t);
   mul_nn(t, cd, P);
 #pragma unroll
-  for (int k = 0; k < 9; k++) N.e[k] = mk<double>(M1.e[k].re - Mm3.e[k].re, M1.e[k].im - Mm3.e[k].im);
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      Dm.e[i + 3 * j] = mk<double>(P.e[i + 3 * j].re - P.e[j + 3 * i].re, P.e[i + 3 * j].im + P.e[j + 3 * i].im);
+  conj_antiherm(a, M4, N);
   {
-    M3 u, v;
-    mul_nn(a, M4, u);
-    mul_nd(u, a, v);
-    axpy(1.0, v, N);
-    mul_nn(d, M2, u);
-    mul_nd(u, d, v);
-    axpy(-1.0, v, N);
+    M3 v;
+    conj_antiherm(d, M2, v);
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      N.e[k] = mk<double>(N.e[k].re - v.e[k].re + M1.e[k].re - Mm3.e[k].re,
+                          N.e[k].im - v.e[k].im + M1.e[k].im - Mm3.e[k].im);
   }
   M3 La, Lb, Lc, Ld, bcd, Na, Nab, w;
   mul_nn(b, cd, bcd);
@@ -521,33 +569,23 @@ __device__ void plaquette_vjp(C* LU, double* E, L S, int p, int q, L sa, L sb, L
   mul_dn(d, Nab, Lc);
   mul_nd(Nab, c, Ld);
   {
-    M3 u, v, vd;
-    mul_nd(M4, a, u);  // M4 a^d P, enters as its dagger
-    mul_nn(u, P, v);
-    dagger(v, vd);
-    axpy(1.0, vd, La);
-    mul_nn(P, a, u);  // P a M4
-    mul_nn(u, M4, v);
+    M3 Dx, v;
+    mul_nn(Dm, a, Dx);  // D a
+    mul_nn(Dx, M4, v);
     axpy(1.0, v, La);
-    if (rev_mask & 2u) {  // force on b: a^d (P a)
-      M3 r;
+    if (rev_mask & 2u) {  // force on b
       A8 fb;
-      mul_dn(a, u, r);
-      retr_itg(r, 1.0, fb);
+      mul_dn(a, Dx, v);
+      retr_itg(v, 0.5, fb);
       atomic_add_alg(E, S, q * 8, sb, -wq, fb);
     }
-    mul_nd(M2, d, u);  // -(M2 d^d P)^d
-    mul_nn(u, P, v);
-    dagger(v, vd);
-    axpy(-1.0, vd, Ld);
-    mul_nn(P, d, u);  // -P d M2
-    mul_nn(u, M2, v);
+    mul_nn(Dm, d, Dx);  // D d
+    mul_nn(Dx, M2, v);
     axpy(-1.0, v, Ld);
-    if (rev_mask & 4u) {  // force on c: (P d)^d d
-      M3 r;
+    if (rev_mask & 4u) {  // force on c
       A8 fc;
-      mul_dn(u, d, r);
-      retr_itg(r, 1.0, fc);
+      mul_dn(d, Dx, v);
+      retr_itg(v, -0.5, fc);
       atomic_add_alg(E, S, p * 8, sc, -wp, fc);
     }
   }

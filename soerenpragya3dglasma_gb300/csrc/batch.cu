@@ -1,9 +1,10 @@
 // batch.cu -- many independent lattices ("events") of uneven sizes advanced together.
 //
 // Each event is an ordinary lattice handle (its own fields, ghost slices, tile shape).  A step of
-// the whole batch is two persistent launches: the electric-field/JStat kernel walks the list of
-// all events' K1 tiles, the link/J kernel the list of all events' 128-site chunks; a block finds
-// its event by binary search over the per-event tile offsets.  The per-site arithmetic is the
+// the whole batch is two launches: the electric-field/JStat kernel walks the list of all events'
+// K1 tiles, the link/J kernel the list of all events' 128-site chunks (one block per tile, or a
+// persistent grid that strides through the list); a block finds its event by binary search over the
+// per-event tile offsets.  The per-site arithmetic is the
 // single-lattice kernels' (leapfrog_sites.cuh), so a batched step is bit-identical to stepping
 // every event on its own.  Blocks of steps are captured once into a CUDA graph and replayed.
 // No reference counterpart: the reference farms independent seeds out as separate jobs
@@ -35,26 +36,12 @@ struct EventDesc {
   long long k2_begin;  // first 128-site chunk of this event
 };
 
-template <typename T>
-__device__ __forceinline__ int find_event(const EventDesc<T>* __restrict__ ev, int n, long long t, bool k1) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    const long long b = k1 ? ev[mid].k1_begin : ev[mid].k2_begin;
-    if (b <= t)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
-    efield_batch_kernel(const EventDesc<T>* __restrict__ ev, int n, long long total) {
+    efield_batch_kernel(const EventDesc<T>* __restrict__ ev, const unsigned short* __restrict__ tile_ev, long long total) {
   __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-    const int e = find_event(ev, n, t, true);
+    const int e = tile_ev[t];
     // Local copies: the site body stores through these pointers, so references into the table
     // would have to be re-read from global memory after every store.
     const Geometry g = ev[e].g;
@@ -68,9 +55,9 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
 
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
-    links_batch_kernel(const EventDesc<T>* __restrict__ ev, int n, long long total) {
+    links_batch_kernel(const EventDesc<T>* __restrict__ ev, const unsigned short* __restrict__ tile_ev, long long total) {
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-    const int e = find_event(ev, n, t, false);
+    const int e = tile_ev[t];
     const Geometry g = ev[e].g;
     const FieldPtrs<T> f = ev[e].f;
     const LParams<T> lp = ev[e].lp;
@@ -89,10 +76,13 @@ struct glasma_batch {
   long long steps_done = 0;
   cudaStream_t own_stream = nullptr, stream = nullptr;
   void* d_desc = nullptr;
+  unsigned short* d_tile_ev = nullptr;  // event of every K1 tile, then of every K2 chunk
+  long long tile_ev_cap = 0;
   double desc_dt = NAN;
   long long k1_total = 0, k2_total = 0;
   bool idx32 = true;
   int grid1 = 0, grid2 = 0;
+  int launch_mode = GLASMA_BATCH_TILE_GRID;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_dt = NAN;
@@ -167,7 +157,30 @@ int build_descriptors(glasma_batch* b, double dt) {
     cudaError_t e = cudaMalloc(&b->d_desc, bytes);
     if (e != cudaSuccess) return bfail(GLASMA_ERR_OUT_OF_MEMORY, "cudaMalloc event table");
   }
-  cudaError_t e = cudaMemcpyAsync(b->d_desc, d.data(), bytes, cudaMemcpyHostToDevice, b->stream);
+  // tile -> event table: one load per block instead of a search through the event table
+  std::vector<unsigned short> tev((size_t)(k1 + k2));
+  for (size_t i = 0; i < d.size(); i++) {
+    const long long k1_end = i + 1 < d.size() ? d[i + 1].k1_begin : k1;
+    const long long k2_end = i + 1 < d.size() ? d[i + 1].k2_begin : k2;
+    for (long long t = d[i].k1_begin; t < k1_end; t++) tev[(size_t)t] = (unsigned short)i;
+    for (long long t = d[i].k2_begin; t < k2_end; t++) tev[(size_t)(k1 + t)] = (unsigned short)i;
+  }
+  if (b->tile_ev_cap < k1 + k2) {
+    if (b->d_tile_ev) {
+      cudaStreamSynchronize(b->stream);
+      cudaFree(b->d_tile_ev);
+      b->d_tile_ev = nullptr;
+    }
+    if (cudaMalloc(&b->d_tile_ev, sizeof(unsigned short) * (size_t)(k1 + k2)) != cudaSuccess) {
+      cudaGetLastError();
+      b->tile_ev_cap = 0;
+      return bfail(GLASMA_ERR_OUT_OF_MEMORY, "cudaMalloc tile table");
+    }
+    b->tile_ev_cap = k1 + k2;
+  }
+  cudaError_t e = cudaMemcpyAsync(b->d_tile_ev, tev.data(), sizeof(unsigned short) * tev.size(),
+                                  cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_desc, d.data(), bytes, cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return bcuda(e, "event table upload");
   // persistent grids: as many blocks as fit on the device at once
@@ -181,8 +194,13 @@ int build_descriptors(glasma_batch* b, double dt) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, long long>, kThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, long long>, kThreads, 0);
   }
-  b->grid1 = (int)std::min<long long>(k1, (long long)sms * std::max(per1, 1));
-  b->grid2 = (int)std::min<long long>(k2, (long long)sms * std::max(per2, 1));
+  if (b->launch_mode == GLASMA_BATCH_TILE_GRID && k1 < (1LL << 31) && k2 < (1LL << 31)) {
+    b->grid1 = (int)k1;
+    b->grid2 = (int)k2;
+  } else {
+    b->grid1 = (int)std::min<long long>(k1, (long long)sms * std::max(per1, 1));
+    b->grid2 = (int)std::min<long long>(k2, (long long)sms * std::max(per2, 1));
+  }
   b->desc_dt = dt;
   return GLASMA_OK;
 }
@@ -191,13 +209,12 @@ template <typename T>
 cudaError_t launch_batch_step(glasma_batch* b) {
   using namespace glasma;
   const EventDesc<T>* ev = static_cast<const EventDesc<T>*>(b->d_desc);
-  const int n = (int)b->ev.size();
   if (b->idx32) {
-    efield_batch_kernel<T, int><<<b->grid1, kThreads, 0, b->stream>>>(ev, n, b->k1_total);
-    links_batch_kernel<T, int><<<b->grid2, kThreads, 0, b->stream>>>(ev, n, b->k2_total);
+    efield_batch_kernel<T, int><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
+    links_batch_kernel<T, int><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total, b->k2_total);
   } else {
-    efield_batch_kernel<T, long long><<<b->grid1, kThreads, 0, b->stream>>>(ev, n, b->k1_total);
-    links_batch_kernel<T, long long><<<b->grid2, kThreads, 0, b->stream>>>(ev, n, b->k2_total);
+    efield_batch_kernel<T, long long><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
+    links_batch_kernel<T, long long><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total, b->k2_total);
   }
   return cudaGetLastError();
 }
@@ -228,6 +245,7 @@ extern "C" {
 int glasma_batch_create(int n_events, const int* extents, const double* spacings, int precision, int reunitarize_every,
                         glasma_batch** out) {
   if (!out || !extents || !spacings || n_events < 1) return bfail(GLASMA_ERR_INVALID_ARGUMENT, "bad arguments");
+  if (n_events > 65535) return bfail(GLASMA_ERR_INVALID_ARGUMENT, "at most 65535 events per batch");
   *out = nullptr;
   glasma_batch* b = new glasma_batch;
   b->precision = precision;
@@ -262,6 +280,7 @@ int glasma_batch_destroy(glasma_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (glasma_lattice* h : b->ev) glasma_destroy(h);
   if (b->d_desc) cudaFree(b->d_desc);
+  if (b->d_tile_ev) cudaFree(b->d_tile_ev);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
   return GLASMA_OK;
@@ -362,6 +381,21 @@ int glasma_batch_step(glasma_batch* b, double dt, int nsteps, int use_graph) {
   while (done < nsteps) {
     if ((e = one_step(b)) != cudaSuccess) return bcuda(e, "batch step");
     done++;
+  }
+  return GLASMA_OK;
+}
+
+int glasma_batch_set_launch(glasma_batch* b, int mode) {
+  if (!b || (mode != GLASMA_BATCH_PERSISTENT && mode != GLASMA_BATCH_TILE_GRID))
+    return bfail(GLASMA_ERR_INVALID_ARGUMENT, "bad batch or launch mode");
+  if (mode != b->launch_mode) {
+    b->launch_mode = mode;
+    b->desc_dt = NAN;  // grids are sized when the event table is built
+    if (b->graph) {
+      cudaStreamSynchronize(b->stream);
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
   }
   return GLASMA_OK;
 }

@@ -110,14 +110,18 @@ __global__ void copy_kernel(const E* __restrict__ src, E* __restrict__ dst, long
 
 inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-// The stencil kernels use no shared memory: ask for the whole unified L1/shared array as L1 (their
-// neighbour links are re-read from L1).  Once per kernel and process.
-template <typename K>
+// Stencil kernels without shared memory (the FP32 ones) ask for the whole unified L1/shared array as
+// L1, since their neighbour links are re-read from L1.  The FP64 ones keep per-thread staple slots in
+// shared memory and leave the split to the driver (a zero carve-out would cost them resident
+// blocks).  Once per kernel and process.
+template <typename T, typename K>
 void prefer_l1(K kernel) {
   static bool done = false;
   if (!done) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-    cudaGetLastError();
+    if (StapleShare<T>::kSlots == 0) {
+      cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+      cudaGetLastError();
+    }
     done = true;
   }
 }
@@ -129,10 +133,10 @@ cudaError_t launch_efield_kernel(const Geometry& g, FieldPtrs<T> f, const EParam
   const TileMap tm = TileMap::make(g.nx, g.ny, tile_x, kThreads);
   const unsigned grid = (unsigned)tm.tiles(g.nz);
   if (use_32bit_index(g)) {
-    prefer_l1(efield_jstat_kernel<T, int>);
+    prefer_l1<T>(efield_jstat_kernel<T, int>);
     efield_jstat_kernel<T, int><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
   } else {
-    prefer_l1(efield_jstat_kernel<T, long long>);
+    prefer_l1<T>(efield_jstat_kernel<T, long long>);
     efield_jstat_kernel<T, long long><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
   }
   return cudaGetLastError();
@@ -199,10 +203,10 @@ cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> o
   const EParams<T> pe = make_eparams<T>(g, dt, 1, 1, dry ? 1 : 0);
   const LParams<T> pl = make_lparams<T>(g, dt, save_uold, true, true);
   if (use_32bit_index(g)) {
-    prefer_l1(fused_step_kernel<T, int>);
+    prefer_l1<T>(fused_step_kernel<T, int>);
     fused_step_kernel<T, int><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
   } else {
-    prefer_l1(fused_step_kernel<T, long long>);
+    prefer_l1<T>(fused_step_kernel<T, long long>);
     fused_step_kernel<T, long long><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
   }
   return cudaGetLastError();

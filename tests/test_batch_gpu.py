@@ -39,6 +39,22 @@ def test_batch_equals_individual_events(precision):
             assert np.array_equal(got[i][k], ref[k]), (i, k)
 
 
+def test_batch_launch_modes_agree():
+    """One block per tile and the persistent grid run the same per-site arithmetic."""
+    fields = [O.random_fields(N, 330 + i) for i, N in enumerate(SHAPES)]
+    out = []
+    for mode in ("tile_grid", "persistent"):
+        with Batch(SHAPES, precision="fp32", reunitarize_every=16) as b:
+            b.set_launch(mode)
+            for ev, f in zip(b.events, fields):
+                ev.upload_fields(f)
+            b.step(0.1, 20, use_graph=True)
+            out.append([ev.download_fields(("U", "E", "Jp", "JmStat")) for ev in b.events])
+    for a, c in zip(out[0], out[1]):
+        for k in a:
+            assert np.array_equal(a[k], c[k]), k
+
+
 def test_batch_after_events_stepped_alone():
     """Stepping an event on its own (one-pass: its buffers swap) between batched steps: the batch
     rebuilds its event table and the result equals stepping every event alone."""
