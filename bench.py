@@ -558,7 +558,8 @@ def run_batched(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    shapes = batched_shapes(args.events)
+    shapes = ([tuple(int(v) for v in args.event_shape.split(","))] * args.events if args.event_shape
+              else batched_shapes(args.events))
     sites = sum(a * b * c for a, b, c in shapes)
     with Batch(shapes, precision="fp32", reunitarize_every=16, stream=stream) as b:
         for i, ev in enumerate(b.events):
@@ -600,6 +601,44 @@ def run_batched(args):
         "clocks": clk.summary(),
         "gpu_launches": 2 * args.steps + (args.steps // 16) * len(shapes),
     }
+    print(json.dumps(line), flush=True)
+
+
+def run_fft(args):
+    """The gauge fixer's batched 3D FFT on its own: 8 colour planes of the lattice (default
+    128x128x512, or --lattice), device to device, FP64 and FP32; GB/s counts three axis passes, each
+    reading and writing the array once (the copy in and out of the work array is inside the time)."""
+    import torch
+
+    from soerenpragya3dglasma_gb300 import Lattice, build
+
+    build.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    N = N_WORK
+    vol = N[0] * N[1] * N[2]
+    out = {}
+    with Lattice(N, stream=stream) as lat:
+        for fp32 in (False, True):
+            X = torch.randn((8, N[2], N[1], N[0]), dtype=torch.complex64 if fp32 else torch.complex128, device="cuda")
+            Y = torch.empty_like(X)
+            for _ in range(args.warmup):
+                lat.fft3d_device(X.data_ptr(), Y.data_ptr(), fp32=fp32)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                lat.fft3d_device(X.data_ptr(), Y.data_ptr(), fp32=fp32)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            out["fp32" if fp32 else "fp64"] = {"ms": ms, "gbs": 3 * 2 * (8 if fp32 else 16) * 8 * vol / (ms * 1e-3) / 1e9}
+    line = {"metric": "3D FFT GB/s (8 colour planes)", "value": out["fp64"]["gbs"], "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic N(0,1)",
+            "config": {"workload": "8-plane 3D FFT %dx%dx%d" % N, "lattice": list(N)}, "fp64": out["fp64"],
+            "fp32": out["fp32"]}
     print(json.dumps(line), flush=True)
 
 
@@ -706,9 +745,10 @@ def main():
     ap.add_argument("--only", default="both", choices=["both", "fp64", "fp32"],
                     help="which precisions to run (profiling runs); the JSON line needs both")
     ap.add_argument("--lattice", default=None, help="Nx,Ny,Nz instead of the workload's (profiling runs)")
-    ap.add_argument("--workload", default="production", choices=["production", "batched", "adjoint"],
+    ap.add_argument("--event-shape", default=None, help="NX,NY,NZ for every batched event (profiling runs)")
+    ap.add_argument("--workload", default="production", choices=["production", "batched", "adjoint", "fft"],
                     help="production: the headline 128x128x512 line; batched: 64 uneven events in one launch; "
-                         "adjoint: the gradient of P_L/P_T on a 64x64x256 collision")
+                         "adjoint: the gradient of P_L/P_T on a 64x64x256 collision; fft: the 3D FFT alone")
     ap.add_argument("--adj-steps", type=int, default=400)
     ap.add_argument("--fd-dirs", type=int, default=2)
     ap.add_argument("--events", type=int, default=64)
@@ -725,6 +765,8 @@ def main():
         run_batched(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "fft":
+        run_fft(args)
     else:
         run_ours(args)
 
