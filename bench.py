@@ -429,12 +429,29 @@ def run_ours(args):
             # three axis passes, each reads and writes the 8-colour array once
             return ms, 3 * 2 * (8 if fp32 else 16) * 8 * vol / (ms * 1e-3) / 1e9
 
+        def time_local(alg, param):
+            # the reference's two local updates (Los Alamos: checkerboard passes with the Cabibbo-Marinari
+            # max-trace projection; Jacobi: every site at once) on the same state
+            glat.gauge_reset()
+            torch.cuda.synchronize()
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            log = glat.coulomb_fix(param, args.local_gauge_iters, tol=0.0, algorithm=alg)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            return {"param": param, "ms_per_iteration": g0.elapsed_time(g1) / len(log), "iterations_run": len(log),
+                    "max_deviation_first": float(log[0, 1]), "max_deviation_last": float(log[-1, 1]),
+                    "functional_last": float(log[-1, 6])}
+
         runs = {}
         for fft_fp32 in (False, True):
             r = time_gauge(fft_fp32, False)
             if "error" in r:  # the reference's unnormalised zero mode can drift out of SU(3): retry without it
                 r = {"reference_semantics": r, **time_gauge(fft_fp32, True)}
             runs["fft_fp32" if fft_fp32 else "fft_fp64"] = r
+        if args.local_gauge_iters > 0:
+            runs["los_alamos"] = time_local("los_alamos", 0.0)
+            runs["jacobi"] = time_local("jacobi", 0.3)
         fft_ms, fft_gbs = time_fft(False)
         fft32_ms, fft32_gbs = time_fft(True)
         gauge = {"state": "MV collision (seeded charges, g^2 mu 0.5, m 0.2, sigma_z %g, centres %d/%d) evolved %d "
@@ -742,6 +759,8 @@ def main():
     ap.add_argument("--step-method", default="two_pass", choices=["one_pass", "two_pass"])
     ap.add_argument("--gauge-evolve", type=int, default=40, help="leapfrog steps of the MV state before gauge fixing")
     ap.add_argument("--gauge-iters", type=int, default=300)
+    ap.add_argument("--local-gauge-iters", type=int, default=20,
+                    help="iterations of the Los Alamos and Jacobi gauge fixers timed on the same state")
     ap.add_argument("--only", default="both", choices=["both", "fp64", "fp32"],
                     help="which precisions to run (profiling runs); the JSON line needs both")
     ap.add_argument("--lattice", default=None, help="Nx,Ny,Nz instead of the workload's (profiling runs)")

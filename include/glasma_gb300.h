@@ -61,6 +61,12 @@ enum glasma_field {
 /* glasma_step flags */
 #define GLASMA_STEP_SAVE_UOLD 0x1u /* write UOld = U(t+dt/2) of the last step (SaveOldLink) */
 
+/* glasma_coulomb_fix_algorithm algorithms: the three updates of S/GAUGETRANSFORMATION/ALGORITHMS/
+   (the reference compiles one, selected by a #define in CoulombGaugeFixing.cpp:4) */
+#define GLASMA_GF_FOURIER 0    /* FourierAccelerationAlgorithm; param = alphaStepSize (reference 2.0) */
+#define GLASMA_GF_LOS_ALAMOS 1 /* LosAlamosAlgorithm; param = OverRelaxationProbability (reference 0.0) */
+#define GLASMA_GF_JACOBI 2     /* JacobiAlgorithm; param = alphaStepSize (reference 0.3) */
+
 /* glasma_coulomb_fix flags */
 #define GLASMA_GF_PROJECT_ZERO_MODE 0x1u /* drop the p=0 mode of the update (the reference keeps
                                             it unnormalised); a documented deviation */
@@ -161,6 +167,23 @@ int glasma_reunitarize(glasma_lattice* h);
  * exits there). */
 int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double tol, unsigned flags, double* log,
                        int* iterations);
+/* SetCoulombGauge with any of the reference's three updates (S/GAUGETRANSFORMATION/ALGORITHMS/):
+ *   GLASMA_GF_FOURIER     glasma_coulomb_fix(h, param, max_iters, tol, flags, ...)
+ *   GLASMA_GF_LOS_ALAMOS  LosAlamosAlgorithm::UpdateGaugeTransformation (LosAlamos.cpp:13-95): the even
+ *                         sites ((x+y+z) even), links re-transformed, the odd sites, links re-transformed;
+ *                         per site G <- P(w)^d G with P = SUNcGroup::Extended::MaxTraceProjection
+ *                         (S/SUNc/SU3/GroupOperations.cpp:358-378, seven Cabibbo-Marinari sweeps), or
+ *                         G <- P^d P^d G (over-relaxation) when the site's draw is <= param.  The draws
+ *                         are a counter-based hash of (seed, 2*iteration + pass, site): reproducible, and
+ *                         independent of the order the sites are visited in (the reference's rng() stream
+ *                         depends on its OpenMP schedule).  With param = 0 (the reference's value) no draw
+ *                         matters and the iterates are the reference's.
+ *   GLASMA_GF_JACOBI      JacobiAlgorithm::UpdateGaugeTransformation (Jacobi.cpp:13-80): every site at once,
+ *                         G <- exp(-i param t.Delta)^d G.
+ * flags: Fourier only (0 otherwise).  Log rows, stopping rule, G persistence and the unitarity guard as
+ * for glasma_coulomb_fix. */
+int glasma_coulomb_fix_algorithm(glasma_lattice* h, int algorithm, double param, unsigned long long seed, int max_iters,
+                                 double tol, unsigned flags, double* log, int* iterations);
 /* GaugeTransformation::SetIdentity (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:41-60). */
 int glasma_gauge_reset(glasma_lattice* h);
 
@@ -176,6 +199,28 @@ int glasma_mv_init(glasma_lattice* h, int single_left, const double* zeta_left, 
                    double qs_left, double qs_right, int center_left, int center_right, double sigma, double lambda,
                    double meff, double dt);
 const char* glasma_mv_last_error(void);
+
+/* Configuration files in the reference's text format: IO::SaveConfiguration and
+ * IO::SaveConfigurationJ (S/IO/SaveConfiguration.cpp:6-93) write the links, E and the four currents
+ * one entry per line, ghost slices included, with 15 significant digits; IO::LoadConfiguration
+ * (S/IO/LoadConfiguration.cpp:3-200) reads them back.  Any path may be NULL to skip that file.
+ * Reading checks the entries' order and count and returns GLASMA_ERR_INVALID_ARGUMENT (message in
+ * glasma_io_last_error) where the reference exits; it reads all eight colours of the currents file
+ * (the reference's loader fills colours 0-2 only) and uploads nothing unless every file read cleanly.
+ * The _host forms work on host arrays in the reference's layout and need no GPU. */
+int glasma_save_text(glasma_lattice* h, const char* links_path, const char* efield_path, const char* currents_path);
+int glasma_load_text(glasma_lattice* h, const char* links_path, const char* efield_path, const char* currents_path);
+int glasma_write_text_host(int nx, int ny, int nz, const double* U, const double* E, const double* JpStat,
+                           const double* Jp, const double* JmStat, const double* Jm, const char* links_path,
+                           const char* efield_path, const char* currents_path);
+int glasma_read_text_host(int nx, int ny, int nz, double* U, double* E, double* JpStat, double* Jp, double* JmStat,
+                          double* Jm, const char* links_path, const char* efield_path, const char* currents_path);
+/* Binary restart file (no reference counterpart): U, UOld, E and the four currents in the
+ * reference's host layout after a 64-byte header (lattice shape, spacings, step count); loading
+ * reproduces the fields bit for bit.  The lattice shape must match the handle's. */
+int glasma_save_binary(glasma_lattice* h, const char* path);
+int glasma_load_binary(glasma_lattice* h, const char* path);
+const char* glasma_io_last_error(void);
 
 /* Seeded synthetic fields generated on the device (benchmarks, demos): links exp(i link_amp t.r),
  * E = e_amp r, the four currents j_amp r, r ~ N(0,1) from a counter-based generator (SplitMix64 +

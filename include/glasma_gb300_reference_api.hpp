@@ -376,17 +376,75 @@ inline void CreateMap(const std::string& fname, GaugeLinks* U, GaugeLinks* UOld,
 }  // namespace EnergyMomentumTensor
 }  // namespace Observables
 
-// S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:6-96
+// S/IO/SaveConfiguration.cpp:6-93 and S/IO/LoadConfiguration.cpp:3-200: text configuration files,
+// named as the reference names them (OutputDirectory + stem + "ID" + seed + ".txt").  Errors throw
+// glasma_dropin::Error where the reference exits.
+namespace RandomNumberGenerator {
+inline long int MySEED = 0;
+}
+namespace IO {
+inline std::string OutputDirectory = "";
+inline std::string ConfigurationFileName(const std::string& stem) {
+  return OutputDirectory + stem + "ID" + std::to_string(RandomNumberGenerator::MySEED) + ".txt";
+}
+inline void io_check(int status) {
+  if (status != GLASMA_OK)
+    throw glasma_dropin::Error(status, std::string(glasma_status_string(status)) + ": " + glasma_io_last_error());
+}
+inline void SaveConfiguration(const std::string& Ufname, const std::string& Efname) {
+  glasma_dropin::push(SUNcGaugeLinks::U, SUNcElectricFields::E);
+  io_check(glasma_save_text(glasma_dropin::handle(), ConfigurationFileName(Ufname).c_str(),
+                            ConfigurationFileName(Efname).c_str(), nullptr));
+}
+inline void SaveConfigurationJ(const std::string& Jfname) {
+  glasma_dropin::push(SUNcChargeDensity::Jp, SUNcChargeDensity::Jm, SUNcChargeDensity::JpStat,
+                      SUNcChargeDensity::JmStat);
+  io_check(glasma_save_text(glasma_dropin::handle(), nullptr, nullptr, ConfigurationFileName(Jfname).c_str()));
+}
+// Full paths, as the reference's loader takes them.
+inline void LoadConfiguration(const std::string& Ufname, const std::string& Efname, const std::string& Jfname) {
+  io_check(glasma_load_text(glasma_dropin::handle(), Ufname.c_str(), Efname.c_str(), Jfname.c_str()));
+  glasma_dropin::wrote(SUNcGaugeLinks::U, SUNcElectricFields::E, SUNcChargeDensity::Jp, SUNcChargeDensity::Jm,
+                       SUNcChargeDensity::JpStat, SUNcChargeDensity::JmStat);
+}
+}  // namespace IO
+
+// S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:6-96.  The reference compiles one of its three updates,
+// chosen by a #define in CoulombGaugeFixing.cpp:4; here the same macro names, defined before this header
+// is included, choose it (GAUGE_FIXING_ALGORITHM_LOS_ALAMOS, GAUGE_FIXING_ALGORITHM_JACOBI), and the
+// Fourier-accelerated update is the default, as in the reference.
 namespace CoulombGaugeFixing {
 inline glasma_dropin::DOUBLE GlobalMaxDeviation = 0.0, GlobalAvgDeviation = 0.0, GlobalMaxStepSize = 0.0,
                              GlobalAvgStepSize = 0.0, GlobalMinGaugeFunctional = 0.0, GlobalSumGaugeFunctional = 0.0;
-inline glasma_dropin::DOUBLE alphaStepSize = 2.0;  // FourierAccelerationAlgorithm::alphaStepSize
+namespace FourierAccelerationAlgorithm {
+inline glasma_dropin::DOUBLE alphaStepSize = 2.0;  // FourierAcceleration.cpp:6
+}
+namespace LosAlamosAlgorithm {
+inline glasma_dropin::DOUBLE OverRelaxationProbability = 0.0;  // LosAlamos.cpp:6
+// the over-relaxation draws: a counter-based hash of (DrawSeed, iteration, pass, site)
+inline unsigned long long DrawSeed = 0;
+}
+namespace JacobiAlgorithm {
+inline glasma_dropin::DOUBLE alphaStepSize = 0.3;  // Jacobi.cpp:6
+}
 // Writes one log line per iteration to fname (n, max dev, avg dev, max step, avg step, min F, sum F / V).
 inline void SetCoulombGauge(const std::string& fname, int TotalSteps) {
   glasma_dropin::push(SUNcGaugeLinks::U, SUNcElectricFields::E);
   std::vector<double> log((size_t)(TotalSteps > 0 ? TotalSteps : 1) * 7);
   int n = 0;
-  glasma_dropin::check(glasma_coulomb_fix(glasma_dropin::handle(), alphaStepSize, TotalSteps, 1e-15, 0, log.data(), &n));
+#if defined(GAUGE_FIXING_ALGORITHM_LOS_ALAMOS)
+  const int algorithm = GLASMA_GF_LOS_ALAMOS;
+  const double param = LosAlamosAlgorithm::OverRelaxationProbability;
+#elif defined(GAUGE_FIXING_ALGORITHM_JACOBI)
+  const int algorithm = GLASMA_GF_JACOBI;
+  const double param = JacobiAlgorithm::alphaStepSize;
+#else
+  const int algorithm = GLASMA_GF_FOURIER;
+  const double param = FourierAccelerationAlgorithm::alphaStepSize;
+#endif
+  glasma_dropin::check(glasma_coulomb_fix_algorithm(glasma_dropin::handle(), algorithm, param,
+                                                    LosAlamosAlgorithm::DrawSeed, TotalSteps, 1e-15, 0, log.data(),
+                                                    &n));
   if (n > 0) {
     const double* last = log.data() + (size_t)(n - 1) * 7;
     GlobalMaxDeviation = last[1];

@@ -509,6 +509,76 @@ void gauge_transform_efield(const Lat& l, const double* E, double* EG, cplx* G) 
   sync_G(G, l);
 }
 
+// ------------------------------------------------------------- Coulomb gauge deviation at one site
+// GET_LOCAL_GAUGE_VIOLATION (S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41):
+// w(x) = sum_mu c_mu (UG_mu(x) + UG_mu^dagger(x - mu)), the z term only if Nz > 1; Delta^a = ReTr(i t^a w).
+void gauge_deviation(const Lat& l, const cplx* UG, int x, int y, int z, const double* cw, cplx* w, double* dev) {
+  const double zterm = l.N[2] > 1 ? 1.0 : 0.0;
+  const cplx* u0 = L(UG, l, x, y, z, 0);
+  const cplx* u1 = L(UG, l, x, y, z, 1);
+  const cplx* u2 = L(UG, l, x, y, z, 2);
+  const cplx* d0 = L(UG, l, x - 1, y, z, 0);
+  const cplx* d1 = L(UG, l, x, y - 1, z, 1);
+  const cplx* d2 = L(UG, l, x, y, z - 1, 2);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      const int k = mi(i, j), kt = mi(j, i);
+      w[k] = cw[0] * (u0[k] + std::conj(d0[kt])) + cw[1] * (u1[k] + std::conj(d1[kt])) +
+             zterm * cw[2] * (u2[k] + std::conj(d2[kt]));
+    }
+  retr_itg(w, dev);
+}
+
+// ------------------------------------------------------------- local gauge-fixing updates
+// The draw that decides over-relaxation at one site of one checkerboard pass (the reference calls
+// RandomNumberGenerator::rng() there, S/GAUGETRANSFORMATION/ALGORITHMS/LosAlamos.cpp:51): a
+// counter-based hash of (seed, 2 * iteration + pass, site), so that any implementation draws the
+// same number for the same site whatever order it visits the sites in.  The mixing function is the
+// splitmix64 finaliser (Steele, Lea & Flood, OOPSLA 2014); the result is uniform in [0, 1).
+inline uint64_t gf_mix(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+double gf_uniform(uint64_t seed, long iteration, int pass, long site) {
+  const uint64_t k = gf_mix(seed ^ gf_mix((uint64_t)(2 * iteration + pass)));
+  return (double)(gf_mix(k ^ (uint64_t)site) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// One Cabibbo-Marinari step in the SU(2) subgroup of rows/columns (p, q)
+// (S/SUNc/SU3/util/CabbiboMarinariProjection.cpp:4-62, CABBIBO_MARINARI_STEP :73-92):
+//   A_pp = (V_pp^* + V_qq)/n, A_pq = (V_qp^* - V_pq)/n, A_qp = (V_pq^* - V_qp)/n, A_qq = (V_qq^* + V_pp)/n,
+//   n = sqrt(|V_pp^* + V_qq|^2 + |V_qp^* - V_pq|^2), the identity elsewhere; Gc <- A Gc, V <- A V.
+// Only rows p and q of Gc and V change.
+void cm_subgroup(int p, int q, cplx* Gc, cplx* V) {
+  const cplx s = std::conj(V[mi(p, p)]) + V[mi(q, q)];
+  const cplx t = std::conj(V[mi(q, p)]) - V[mi(p, q)];
+  const double inv = 1.0 / std::sqrt(std::norm(s) + std::norm(t));
+  const cplx App = inv * s, Apq = inv * t;
+  const cplx Aqp = inv * (std::conj(V[mi(p, q)]) - V[mi(q, p)]), Aqq = inv * (std::conj(V[mi(q, q)]) + V[mi(p, p)]);
+  for (cplx* M : {Gc, V})
+    for (int j = 0; j < 3; j++) {
+      const cplx rp = M[mi(p, j)], rq = M[mi(q, j)];
+      M[mi(p, j)] = App * rp + Apq * rq;
+      M[mi(q, j)] = Aqp * rp + Aqq * rq;
+    }
+}
+// SUNcGroup::Extended::MaxTraceProjection (S/SUNc/SU3/GroupOperations.cpp:358-378): seven sweeps over
+// the subgroups (0,1), (0,2), (1,2) accumulate Gc, which maximises Re tr(Gc w); the result is Gc^dagger.
+void max_trace_projection(const cplx* w, cplx* out) {
+  cplx Gc[9] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+  cplx V[9];
+  std::memcpy(V, w, sizeof(V));
+  for (int n = 0; n < 7; n++) {
+    cm_subgroup(0, 1, Gc, V);
+    cm_subgroup(0, 2, Gc, V);
+    cm_subgroup(1, 2, Gc, V);
+  }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) out[mi(i, j)] = std::conj(Gc[mi(j, i)]);
+}
+
 }  // namespace
 
 // =============================================================== C entry points
@@ -778,7 +848,6 @@ int oracle_coulomb_fix(const int* N, const double* a, double aScale, const doubl
   std::vector<cplx> X((size_t)8 * V);
   double cw[3];
   for (int mu = 0; mu < 3; mu++) cw[mu] = (aScale / l.a[mu]) * (aScale / l.a[mu]);
-  const double zterm = Nz > 1 ? 1.0 : 0.0;
   double gmaxdev = 1.0;
   int n = 0;
   int status = 0;
@@ -790,20 +859,8 @@ int oracle_coulomb_fix(const int* N, const double* a, double aScale, const doubl
       for (int y = 0; y < Ny; y++)
         for (int x = 0; x < Nx; x++) {
           cplx w[9];
-          const cplx* u0 = L(UG, l, x, y, z, 0);
-          const cplx* u1 = L(UG, l, x, y, z, 1);
-          const cplx* u2 = L(UG, l, x, y, z, 2);
-          const cplx* d0 = L(UG, l, x - 1, y, z, 0);
-          const cplx* d1 = L(UG, l, x, y - 1, z, 1);
-          const cplx* d2 = L(UG, l, x, y, z - 1, 2);
-          for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) {
-              const int k = mi(i, j), kt = mi(j, i);
-              w[k] = cw[0] * (u0[k] + std::conj(d0[kt])) + cw[1] * (u1[k] + std::conj(d1[kt])) +
-                     zterm * cw[2] * (u2[k] + std::conj(d2[kt]));
-            }
           double dev[8];
-          retr_itg(w, dev);
+          gauge_deviation(l, UG, x, y, z, cw, w, dev);
           const long site = x + (long)Nx * (y + (long)Ny * z);
           for (int aa = 0; aa < 8; aa++) {
             maxdev = std::max(maxdev, std::fabs(dev[aa]));
@@ -848,6 +905,109 @@ int oracle_coulomb_fix(const int* N, const double* a, double aScale, const doubl
           std::memcpy(GF(G, l, x, y, z), gn, sizeof(gn));
         }
     gauge_transform_links(l, U, UG, G);
+    gmaxdev = maxdev;
+    if (log_out) {
+      double* o = log_out + 7 * n;
+      o[0] = n;
+      o[1] = maxdev;
+      o[2] = std::sqrt(sqdev / (8.0 * V));
+      o[3] = maxstep;
+      o[4] = std::sqrt(sqstep / (8.0 * V));
+      o[5] = minf;
+      o[6] = sumf / V;
+    }
+    n++;
+    if (bad) {
+      status = 5;
+      break;
+    }
+  }
+  if (status == 0) {
+    gauge_transform_links(l, U, UG, G);
+    gauge_transform_efield(l, E, EG, G);
+  }
+  *n_out = n;
+  return status;
+}
+
+double oracle_gf_uniform(unsigned long long seed, long iteration, int pass, long site) {
+  return gf_uniform(seed, iteration, pass, site);
+}
+
+// SetCoulombGauge (S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:32-88) with one of the two local updates
+// the reference compiles next to the Fourier-accelerated one:
+//   algorithm 1  LosAlamosAlgorithm (S/GAUGETRANSFORMATION/ALGORITHMS/LosAlamos.cpp:13-95): the even
+//                sites ((x+y+z) % 2 == 0), the links re-transformed, the odd sites, the links
+//                re-transformed.  At each site wTilde = MaxTraceProjection(w), G <- wTilde^d G, or
+//                G <- wTilde^d wTilde^d G (over-relaxation) unless the site's draw exceeds param (the
+//                reference's OverRelaxationProbability).  The monitors are reset before the even pass
+//                and accumulate over both.
+//   algorithm 2  JacobiAlgorithm (S/GAUGETRANSFORMATION/ALGORITHMS/Jacobi.cpp:13-80): every site at
+//                once, wTilde = exp(-i param t.Delta) (param: the reference's alphaStepSize), G <- wTilde^d G.
+// Both read only the links transformed before the pass and write only G at the site itself, so the
+// sites of a pass are independent.  Monitors, guard and log rows as in oracle_coulomb_fix; seed and the
+// iteration index of this call select the over-relaxation draws (gf_uniform).
+int oracle_coulomb_fix_local(const int* N, const double* a, double aScale, const double* Uin, const double* E,
+                             double* Gin, double* UGin, double* EG, int algorithm, double param,
+                             unsigned long long seed, int total_steps, double tol, double* log_out, int* n_out) {
+  *n_out = 0;
+  if (algorithm != 1 && algorithm != 2) return 1;
+  Lat l = make_lat(N, a, aScale);
+  const cplx* U = reinterpret_cast<const cplx*>(Uin);
+  cplx* G = reinterpret_cast<cplx*>(Gin);
+  cplx* UG = reinterpret_cast<cplx*>(UGin);
+  const long V = l.volume();
+  std::memcpy(UG + 27 * l.s(0, 0, 0), U + 27 * l.s(0, 0, 0), sizeof(cplx) * 27 * V);
+  std::memcpy(EG + 24 * l.s(0, 0, 0), E + 24 * l.s(0, 0, 0), sizeof(double) * 24 * V);
+  gauge_transform_links(l, U, UG, G);
+  const int Nx = l.N[0], Ny = l.N[1], Nz = l.N[2];
+  double cw[3];
+  for (int mu = 0; mu < 3; mu++) cw[mu] = (aScale / l.a[mu]) * (aScale / l.a[mu]);
+  const double minf0 = 2.0 * 3 * (1.0 / (l.a[0] * l.a[0]) + 1.0 / (l.a[1] * l.a[1]) + 1.0 / (l.a[2] * l.a[2]));
+  const int passes = algorithm == 1 ? 2 : 1;
+  double gmaxdev = 1.0;
+  int n = 0, status = 0;
+  while (n < total_steps && gmaxdev > tol) {
+    double maxdev = 0.0, sqdev = 0.0, sumf = 0.0, minf = minf0, maxstep = 0.0, sqstep = 0.0;
+    int bad = 0;
+    for (int pass = 0; pass < passes; pass++) {
+#pragma omp parallel for reduction(+ : sqdev, sumf, sqstep, bad) reduction(max : maxdev, maxstep) \
+    reduction(min : minf) schedule(static)
+      for (int z = 0; z < Nz; z++)
+        for (int y = 0; y < Ny; y++)
+          for (int x = 0; x < Nx; x++) {
+            if (algorithm == 1 && (x + y + z) % 2 != pass) continue;
+            cplx w[9], wt[9], gn[9];
+            double dev[8];
+            gauge_deviation(l, UG, x, y, z, cw, w, dev);
+            for (int aa = 0; aa < 8; aa++) {
+              maxdev = std::max(maxdev, std::fabs(dev[aa]));
+              sqdev += dev[aa] * dev[aa];
+            }
+            const double lf = retr(w);
+            minf = std::min(minf, lf);
+            sumf += lf;
+            if (algorithm == 1)
+              max_trace_projection(w, wt);
+            else
+              expi(-param, dev, wt);
+            if (unitarity_norm(wt) > 1e-13) bad += 1;
+            const double st = std::abs(cplx(3.0) - wt[0] - wt[4] - wt[8]);
+            maxstep = std::max(maxstep, st);
+            sqstep += st * st;
+            cplx* g = GF(G, l, x, y, z);
+            const long site = x + (long)Nx * (y + (long)Ny * z);
+            if (algorithm == 1 && !(gf_uniform(seed, n, pass, site) > param)) {
+              cplx t[9];
+              mul_dd(wt, wt, t);  // DDU (S/SUNc/AdvancedOperations.cpp:119-131)
+              mul_nn(t, g, gn);
+            } else {
+              mul_dn(wt, g, gn);  // DU (S/SUNc/SU3/GroupOperations.cpp:166-180)
+            }
+            std::memcpy(g, gn, sizeof(gn));
+          }
+      gauge_transform_links(l, U, UG, G);
+    }
     gmaxdev = maxdev;
     if (log_out) {
       double* o = log_out + 7 * n;

@@ -181,6 +181,12 @@ class Oracle:
         L.oracle_coulomb_fix.argtypes = [_ip, _dp, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, ctypes.c_double,
                                          ctypes.c_int, ctypes.c_double, _dp, _ip]
         L.oracle_coulomb_fix.restype = ctypes.c_int
+        L.oracle_coulomb_fix_local.argtypes = [_ip, _dp, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                               ctypes.c_double, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_double,
+                                               _dp, ctypes.POINTER(ctypes.c_int)]
+        L.oracle_coulomb_fix_local.restype = ctypes.c_int
+        L.oracle_gf_uniform.argtypes = [ctypes.c_ulonglong, ctypes.c_long, ctypes.c_int, ctypes.c_long]
+        L.oracle_gf_uniform.restype = ctypes.c_double
         L.oracle_expi.argtypes = [ctypes.c_double, _dp, _dp]
         L.oracle_adj_mul.argtypes = [_dp, _dp, _dp]
         L.oracle_inv_adj_mul.argtypes = [_dp, _dp, _dp]
@@ -191,6 +197,15 @@ class Oracle:
 
     def threads(self):
         return self.lib.oracle_get_threads()
+
+    def coulomb_fix_local(self, algorithm, param, total_steps, uniforms=()):
+        """Los Alamos / Jacobi gauge fixing with the reference's own update functions; uniforms are
+        what its rng() returns, in call order (construct with threads=1 for a fixed order)."""
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        log = np.zeros((max(total_steps, 1), 7))
+        n = self.lib.ref_coulomb_local(LOCAL_GAUGE_ALGORITHMS[algorithm], param, _ptr(u), u.size, total_steps,
+                                       _ptr(log), total_steps)
+        return log[:n]
 
     def expi(self, c, alpha):
         out = np.zeros(9, dtype=np.complex128)
@@ -237,6 +252,37 @@ class Oracle:
                                          _ptr(EG), alpha, total_steps, tol, _ptr(log), ctypes.byref(n))
         return st, log[: n.value], UG, EG
 
+    def coulomb_fix_local(self, f, G, N, a, algorithm, param, total_steps, seed=0, tol=1e-15, a_scale=1.0,
+                          UG=None, EG=None):
+        """Los Alamos (algorithm "los_alamos", param = over-relaxation probability) or Jacobi
+        ("jacobi", param = step size) gauge fixing; returns (status, log[n,7], UG, EG), G updated in place."""
+        UG = identity_links(N) if UG is None else UG
+        EG = zero_efield(N) if EG is None else EG
+        log = np.zeros((max(total_steps, 1), 7))
+        n = ctypes.c_int()
+        st = self.lib.oracle_coulomb_fix_local(_ivec(N), _dvec(a), a_scale, _ptr(f["U"]), _ptr(f["E"]), _ptr(G),
+                                               _ptr(UG), _ptr(EG), LOCAL_GAUGE_ALGORITHMS[algorithm], param, seed,
+                                               total_steps, tol, _ptr(log), ctypes.byref(n))
+        return st, log[: n.value], UG, EG
+
+    def gf_uniforms_in_site_order(self, N, seed, iterations):
+        """The over-relaxation draws of the Los Alamos update in the order a single-threaded sweep
+        of the reference consumes them: per iteration the even sites, then the odd sites, z outer,
+        x inner."""
+        out = []
+        for n in range(iterations):
+            for parity in (0, 1):
+                for z in range(N[2]):
+                    for y in range(N[1]):
+                        for x in range(N[0]):
+                            if (x + y + z) % 2 == parity:
+                                site = x + N[0] * (y + N[1] * z)
+                                out.append(self.lib.oracle_gf_uniform(seed, n, parity, site))
+        return np.array(out)
+
+
+LOCAL_GAUGE_ALGORITHMS = {"los_alamos": 1, "jacobi": 2}
+
 
 # ----------------------------------------------------------------- the reference itself
 _FIELD_ID = {"U": 0, "UOld": 1, "E": 2, "Jp": 3, "Jm": 4, "JpStat": 5, "JmStat": 6, "G": 7, "UG": 8, "EG": 9}
@@ -264,10 +310,15 @@ class Reference:
         L.ref_emt_map.argtypes = [_dp]
         L.ref_coulomb.argtypes = [ctypes.c_double, ctypes.c_int, _dp, ctypes.c_int]
         L.ref_coulomb.restype = ctypes.c_int
+        L.ref_coulomb_local.argtypes = [ctypes.c_int, ctypes.c_double, _dp, ctypes.c_long, ctypes.c_int, _dp,
+                                        ctypes.c_int]
+        L.ref_coulomb_local.restype = ctypes.c_int
         L.ref_expi.argtypes = [ctypes.c_double, _dp, _dp]
         L.ref_matrix_ilog.argtypes = [ctypes.c_double, _dp, _dp]
         L.ref_set_outdir.argtypes = [ctypes.c_char_p]
         L.ref_set_threads.argtypes = [ctypes.c_int]
+        L.ref_save_configuration.argtypes = [ctypes.c_char_p] * 3
+        L.ref_load_configuration.argtypes = [ctypes.c_char_p] * 3
         L.ref_mv_init.argtypes = [_dp, ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]
         self._tmp = tempfile.mkdtemp(prefix="glasma_ref_")
@@ -276,6 +327,16 @@ class Reference:
             L.ref_set_threads(int(threads))
         self.N = tuple(N)
         L.ref_init(_ivec(N), _dvec(a))
+
+    def save_configuration(self):
+        """IO::SaveConfiguration + SaveConfigurationJ of the current fields; returns the three paths
+        (links, E, currents)."""
+        self.lib.ref_save_configuration(b"U", b"E", b"J")
+        return tuple(os.path.join(self._tmp, "%sID0.txt" % k) for k in ("U", "E", "J"))
+
+    def load_configuration(self, links, efield, currents):
+        """IO::LoadConfiguration into the reference's fields (it exits on malformed files)."""
+        self.lib.ref_load_configuration(str(links).encode(), str(efield).encode(), str(currents).encode())
 
     def set_fields(self, f):
         for k, v in f.items():
@@ -328,6 +389,15 @@ class Reference:
     def coulomb_fix(self, alpha, total_steps):
         log = np.zeros((max(total_steps, 1), 7))
         n = self.lib.ref_coulomb(alpha, total_steps, _ptr(log), total_steps)
+        return log[:n]
+
+    def coulomb_fix_local(self, algorithm, param, total_steps, uniforms=()):
+        """Los Alamos / Jacobi gauge fixing with the reference's own update functions; uniforms are
+        what its rng() returns, in call order (construct with threads=1 for a fixed order)."""
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        log = np.zeros((max(total_steps, 1), 7))
+        n = self.lib.ref_coulomb_local(LOCAL_GAUGE_ALGORITHMS[algorithm], param, _ptr(u), u.size, total_steps,
+                                       _ptr(log), total_steps)
         return log[:n]
 
     def expi(self, c, alpha):

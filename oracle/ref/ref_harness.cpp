@@ -97,7 +97,10 @@ static std::vector<double> Injected;
 static size_t Cursor = 0;
 void Init(long int SEED) { MySEED = SEED; }
 DOUBLE Gauss() { return Cursor < Injected.size() ? Injected[Cursor++] : 0.0; }
-DOUBLE rng() { return 0.5; }
+// rng() replays injected uniforms (the Los Alamos over-relaxation draws), 0.5 once they run out
+static std::vector<double> Uniforms;
+static size_t UniformCursor = 0;
+DOUBLE rng() { return UniformCursor < Uniforms.size() ? Uniforms[UniformCursor++] : 0.5; }
 std::complex<DOUBLE> ComplexGauss() {
   DOUBLE re = Gauss(), im = Gauss();
   return std::complex<DOUBLE>(re, im) / M_SQRT2;
@@ -138,6 +141,8 @@ void SUNcMatrix(DOUBLE Amplitude, SU_Nc_FUNDAMENTAL_FORMAT* V) {
 #include "FFT/FFT3D.cpp"
 #include "COLLIDINGOBJECTS/CollidingObjects.cpp"
 #include "INITIALCONDITIONS/SUNCCURRENTS/RevSingleNucleus.cpp"
+#include "IO/SaveConfiguration.cpp"
+#include "IO/LoadConfiguration.cpp"
 
 #include <cstdio>
 #include <fstream>
@@ -221,6 +226,17 @@ void ref_get_field(int which, double* data) {
 
 void ref_set_threads(int n) { omp_set_num_threads(n); }
 
+// IO::SaveConfiguration and IO::SaveConfigurationJ (S/IO/SaveConfiguration.cpp:6-93): the files are
+// <outdir>/<stem>ID<seed>.txt.
+void ref_save_configuration(const char* u_stem, const char* e_stem, const char* j_stem) {
+  IO::SaveConfiguration(u_stem, e_stem);
+  IO::SaveConfigurationJ(j_stem);
+}
+// IO::LoadConfiguration (S/IO/LoadConfiguration.cpp:190-200) from full paths; exits on malformed files.
+void ref_load_configuration(const char* u_path, const char* e_path, const char* j_path) {
+  IO::LoadConfiguration(u_path, e_path, j_path);
+}
+
 // nsteps x Dynamics::SUNc::Update (S/DYNAMICS/SUNcDynamics.cpp:353-378); returns seconds spent.
 double ref_update(int nsteps, double dt) {
   Dynamics::dTStep = dt;
@@ -289,6 +305,46 @@ int ref_coulomb(double alpha, int total_steps, double* log_out, int max_rows) {
   int n = 0;
   for (size_t i = 0; i < rows.size() && n < max_rows; i++, n++)
     for (int k = 0; k < 7 && k < (int)rows[i].size(); k++) log_out[7 * n + k] = rows[i][k];
+  return n;
+}
+
+// SetCoulombGauge's loop (S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:32-88) with the Los Alamos
+// (algorithm 1, param = OverRelaxationProbability) or the Jacobi (2, param = alphaStepSize) update in
+// place of the Fourier-accelerated one.  The reference selects its algorithm with a #define inside
+// CoulombGaugeFixing.cpp, so the loop is restated here around the reference's own
+// LosAlamosAlgorithm / JacobiAlgorithm::UpdateGaugeTransformation; the log rows come from the
+// Global* monitors at full precision.  uniforms: the values rng() returns, in call order.
+int ref_coulomb_local(int algorithm, double param, const double* uniforms, long n_uniforms, int total_steps,
+                      double* log_out, int max_rows) {
+  RandomNumberGenerator::Uniforms.assign(uniforms, uniforms + n_uniforms);
+  RandomNumberGenerator::UniformCursor = 0;
+  if (algorithm == 1)
+    CoulombGaugeFixing::LosAlamosAlgorithm::OverRelaxationProbability = param;
+  else
+    CoulombGaugeFixing::JacobiAlgorithm::alphaStepSize = param;
+  GaugeTransformation::Operations::CopyFields();
+  GaugeTransformation::Operations::GaugeTransformLinks();
+  CoulombGaugeFixing::GlobalMaxDeviation = 1;
+  int n = 0;
+  while (n < total_steps && CoulombGaugeFixing::GlobalMaxDeviation > std::pow(10.0, -15)) {
+    if (algorithm == 1)
+      CoulombGaugeFixing::LosAlamosAlgorithm::UpdateGaugeTransformation();
+    else
+      CoulombGaugeFixing::JacobiAlgorithm::UpdateGaugeTransformation();
+    if (n < max_rows) {
+      double* o = log_out + 7 * n;
+      o[0] = n;
+      o[1] = CoulombGaugeFixing::GlobalMaxDeviation;
+      o[2] = CoulombGaugeFixing::GlobalAvgDeviation;
+      o[3] = CoulombGaugeFixing::GlobalMaxStepSize;
+      o[4] = CoulombGaugeFixing::GlobalAvgStepSize;
+      o[5] = CoulombGaugeFixing::GlobalMinGaugeFunctional;
+      o[6] = CoulombGaugeFixing::GlobalSumGaugeFunctional;
+    }
+    n++;
+  }
+  GaugeTransformation::Operations::GaugeTransformLinks();
+  GaugeTransformation::Operations::GaugeTransformElectricFields();
   return n;
 }
 

@@ -19,6 +19,7 @@ FIELDS = {"U": 0, "UOld": 1, "E": 2, "Jp": 3, "Jm": 4, "JpStat": 5, "JmStat": 6,
 STEP_SAVE_UOLD = 0x1
 GF_PROJECT_ZERO_MODE = 0x1
 GF_FFT_FP32 = 0x2
+GF_ALGORITHMS = {"fourier": 0, "los_alamos": 1, "jacobi": 2}
 
 # (name, restype, argtypes) for every symbol declared in include/glasma_gb300.h
 _H = ctypes.c_void_p
@@ -52,6 +53,8 @@ SIGNATURES = [
     ("glasma_pressure_anisotropy", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _D, _D, _D]),
     ("glasma_reunitarize", ctypes.c_int, [_H]),
     ("glasma_coulomb_fix", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
+    ("glasma_coulomb_fix_algorithm", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong,
+                                                    ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
     ("glasma_gauge_reset", ctypes.c_int, [_H]),
     ("glasma_mv_init", ctypes.c_int, [_H, ctypes.c_int, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
@@ -62,6 +65,13 @@ SIGNATURES = [
     ("glasma_set_tile", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_fft3d", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("glasma_fft3d_f32", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    ("glasma_save_text", ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
+    ("glasma_load_text", ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
+    ("glasma_write_text_host", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_void_p] * 6 + [ctypes.c_char_p] * 3),
+    ("glasma_read_text_host", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_void_p] * 6 + [ctypes.c_char_p] * 3),
+    ("glasma_save_binary", ctypes.c_int, [_H, ctypes.c_char_p]),
+    ("glasma_load_binary", ctypes.c_int, [_H, ctypes.c_char_p]),
+    ("glasma_io_last_error", ctypes.c_char_p, []),
     ("glasma_gauss_noalloc", ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double] * 4 +
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("glasma_objective", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _D, _D, _D]),

@@ -15,6 +15,10 @@
 // The ghost slices of UG are never written (the reference's gauge-fixed container keeps the
 // identity it was created with), so the backward z link at z = 0 is the identity.
 //
+// The Los Alamos and Jacobi updates that the reference compiles beside the Fourier one
+// (S/GAUGETRANSFORMATION/ALGORITHMS/LosAlamos.cpp, Jacobi.cpp) run through the same loop with a
+// local update in place of the FFT steps: local_update_kernel, one launch per checkerboard pass.
+//
 // All arithmetic is FP64 (G / UG / EG are stored in the handle's precision), except that with
 // GLASMA_GF_FFT_FP32 the two transforms of the acceleration step run in FP32: they only
 // precondition the step, so the iteration still converges to the same gauge, measured in FP64.
@@ -80,6 +84,30 @@ __device__ __forceinline__ long long nbr(const Geometry& g, int x, int y, int z,
   return site_index(g, xx, yy, z + dz);
 }
 
+// w(x) = sum_mu c_mu (UG_mu(x) + UG_mu^d(x - mu)) at interior site s = (x, y, z); c2 = 0 when Nz = 1
+// (GET_LOCAL_GAUGE_VIOLATION, S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41)
+template <typename T>
+__device__ __forceinline__ void site_w(const Geometry& g, const cx<T>* UG, int x, int y, int z, long long s, double c0,
+                                       double c1, double c2, Mat<double>& w) {
+  const double c[3] = {c0, c1, c2};
+  const long long back[3] = {nbr(g, x, y, z, -1, 0, 0), nbr(g, x, y, z, 0, -1, 0), s - g.plane};
+  set_zero(w);
+  for (int mu = 0; mu < 3; mu++) {
+    if (c[mu] == 0.0) continue;
+    Mat<double> u, d;
+    ld_d(UG, g.S, mu * 9, s, u);
+    ld_d(UG, g.S, mu * 9, back[mu], d);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const int k = i + 3 * j, kt = j + 3 * i;
+        w.e[k].re += c[mu] * (u.e[k].re + d.e[kt].re);
+        w.e[k].im += c[mu] * (u.e[k].im - d.e[kt].im);
+      }
+  }
+}
+
 // ---- deviation: X[q] = Delta^{2q} + i Delta^{2q+1}, q < 4 (Delta is real: two colours share one
 // complex transform, and since the acceleration multiplies by a real factor even in p, the inverse
 // transform returns them in the real and imaginary parts); partials {max|Delta|, sum Delta^2,
@@ -94,24 +122,8 @@ __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const
     const long long r = idx / g.nx;
     const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
     const long long s = idx + g.plane;
-    const double c[3] = {c0, c1, c2};
-    const long long back[3] = {nbr(g, x, y, z, -1, 0, 0), nbr(g, x, y, z, 0, -1, 0), s - g.plane};
     Mat<double> w;
-    set_zero(w);
-    for (int mu = 0; mu < 3; mu++) {
-      if (c[mu] == 0.0) continue;
-      Mat<double> u, d;
-      ld_d(UG, g.S, mu * 9, s, u);
-      ld_d(UG, g.S, mu * 9, back[mu], d);
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-          const int k = i + 3 * j, kt = j + 3 * i;
-          w.e[k].re += c[mu] * (u.e[k].re + d.e[kt].re);
-          w.e[k].im += c[mu] * (u.e[k].im - d.e[kt].im);
-        }
-    }
+    site_w(g, UG, x, y, z, s, c0, c1, c2, w);
     Alg<double> dev;
     retr_itg(w, 1.0, dev);
 #pragma unroll
@@ -181,6 +193,123 @@ __global__ void __launch_bounds__(kGfThreads) update_kernel(Geometry g, const C*
     st_d(G, g.S, 0, s, gn);
   }
   red::block_reduce_store<3>(v, op, partials + (long long)blockIdx.x * 3);
+}
+
+// ---- local updates: Los Alamos (LosAlamos.cpp:13-95) and Jacobi (Jacobi.cpp:13-80)
+// The over-relaxation draw of one site of one checkerboard pass: splitmix64's finaliser (Steele, Lea &
+// Flood, OOPSLA 2014) over (seed, 2 * iteration + pass, site), uniform in [0, 1).  Counter-based, so
+// the draw does not depend on the order in which threads visit the sites.
+__device__ __forceinline__ unsigned long long gf_mix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double gf_uniform(unsigned long long seed, int iteration, int pass, long long site) {
+  const unsigned long long k = gf_mix(seed ^ gf_mix((unsigned long long)(2LL * iteration + pass)));
+  return (double)(gf_mix(k ^ (unsigned long long)site) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ cx<double> cmul(const cx<double>& a, const cx<double>& b) {
+  return mk<double>(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+// One Cabibbo-Marinari step in the SU(2) subgroup of rows/columns (p, q)
+// (S/SUNc/SU3/util/CabbiboMarinariProjection.cpp:4-62, step :73-92): the subgroup element
+//   A_pp = (V_pp^* + V_qq)/n, A_pq = (V_qp^* - V_pq)/n, A_qp = (V_pq^* - V_qp)/n, A_qq = (V_qq^* + V_pp)/n
+// multiplies Gc and V from the left; only their rows p and q change.
+template <int p, int q>
+__device__ __forceinline__ void cm_subgroup(Mat<double>& Gc, Mat<double>& V) {
+  const cx<double> vpp = V.e[p + 3 * p], vqq = V.e[q + 3 * q], vpq = V.e[p + 3 * q], vqp = V.e[q + 3 * p];
+  const cx<double> s = mk<double>(vpp.re + vqq.re, vqq.im - vpp.im);
+  const cx<double> t = mk<double>(vqp.re - vpq.re, -vqp.im - vpq.im);
+  const double inv = 1.0 / sqrt(s.re * s.re + s.im * s.im + (t.re * t.re + t.im * t.im));
+  const cx<double> App = mk<double>(inv * s.re, inv * s.im), Apq = mk<double>(inv * t.re, inv * t.im);
+  const cx<double> Aqp = mk<double>(inv * (vpq.re - vqp.re), inv * (-vpq.im - vqp.im));
+  const cx<double> Aqq = mk<double>(inv * (vqq.re + vpp.re), inv * (vpp.im - vqq.im));
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const cx<double> gp = Gc.e[p + 3 * j], gq = Gc.e[q + 3 * j];
+    const cx<double> a = cmul(App, gp), b = cmul(Apq, gq), c = cmul(Aqp, gp), d = cmul(Aqq, gq);
+    Gc.e[p + 3 * j] = mk<double>(a.re + b.re, a.im + b.im);
+    Gc.e[q + 3 * j] = mk<double>(c.re + d.re, c.im + d.im);
+    const cx<double> vp = V.e[p + 3 * j], vq = V.e[q + 3 * j];
+    const cx<double> e = cmul(App, vp), f = cmul(Apq, vq), h = cmul(Aqp, vp), k = cmul(Aqq, vq);
+    V.e[p + 3 * j] = mk<double>(e.re + f.re, e.im + f.im);
+    V.e[q + 3 * j] = mk<double>(h.re + k.re, h.im + k.im);
+  }
+}
+// SUNcGroup::Extended::MaxTraceProjection (S/SUNc/SU3/GroupOperations.cpp:358-378): seven sweeps over
+// the subgroups (0,1), (0,2), (1,2); returns Gc^d, Gc the accumulated product (it maximises Re tr(Gc w)).
+__device__ __forceinline__ void max_trace_projection(const Mat<double>& w, Mat<double>& out) {
+  Mat<double> Gc, V = w;
+#pragma unroll
+  for (int k = 0; k < 9; k++) Gc.e[k] = mk<double>(k % 4 == 0 ? 1.0 : 0.0, 0.0);
+#pragma unroll 1
+  for (int n = 0; n < 7; n++) {
+    cm_subgroup<0, 1>(Gc, V);
+    cm_subgroup<0, 2>(Gc, V);
+    cm_subgroup<1, 2>(Gc, V);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) out.e[i + 3 * j] = mk<double>(Gc.e[j + 3 * i].re, -Gc.e[j + 3 * i].im);
+}
+
+// One pass of a local update over the sites of one checkerboard parity (pass 0 / 1, Los Alamos) or over
+// every site (pass -1, Jacobi).  A parity pass enumerates half-rows: slot k of row (y, z) is
+// x = ((pass + y + z) & 1) + 2k, so a warp's lanes all hold sites of the pass.  Each site reads only
+// the transformed links UG and writes only its own G, so the sites of a pass are independent.
+// partials {max|Delta|, sum Delta^2, min ReTr w, sum ReTr w, max step, sum step^2, guard count}
+template <typename T>
+__global__ void __launch_bounds__(kGfThreads) local_update_kernel(Geometry g, const cx<T>* UG, cx<T>* G, double c0,
+                                                                  double c1, double c2, int los_alamos, int pass,
+                                                                  double param, unsigned long long seed, int iteration,
+                                                                  double* partials) {
+  double v[7] = {0.0, 0.0, 1.0e300, 0.0, 0.0, 0.0, 0.0};
+  const int op[7] = {1, 0, 2, 0, 1, 0, 0};
+  const int hx = pass < 0 ? g.nx : (g.nx + 1) >> 1;
+  const long long n = (long long)hx * g.ny * g.nz;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long r = idx / hx;
+    const int k = (int)(idx - r * hx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+    const int x = pass < 0 ? k : (((pass + y + z) & 1) + 2 * k);
+    if (x >= g.nx) continue;
+    const long long s = site_index(g, x, y, z);
+    Mat<double> w, wt, gm, gn;
+    site_w(g, UG, x, y, z, s, c0, c1, c2, w);
+    Alg<double> dev;
+    retr_itg(w, 1.0, dev);
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      v[0] = fmax(v[0], fabs(dev.a[a]));
+      v[1] += dev.a[a] * dev.a[a];
+    }
+    const double lf = w.e[0].re + w.e[4].re + w.e[8].re;
+    v[2] = fmin(v[2], lf);
+    v[3] += lf;
+    if (los_alamos)
+      max_trace_projection(w, wt);
+    else
+      expi(-param, dev, wt);
+    // the reference's guard (CoulombGaugeDeviation.cpp:57-68); written so that a NaN also trips it
+    if (!(unitarity_norm(wt) <= 1e-13)) v[6] += 1.0;
+    const double sr = 3.0 - wt.e[0].re - wt.e[4].re - wt.e[8].re, si = -(wt.e[0].im + wt.e[4].im + wt.e[8].im);
+    const double step = sqrt(sr * sr + si * si);
+    v[4] = fmax(v[4], step);
+    v[5] += step * step;
+    ld_d(G, g.S, 0, s, gm);
+    if (los_alamos && !(gf_uniform(seed, iteration, pass, s - g.plane) > param)) {
+      Mat<double> t;
+      mul_dd(wt, wt, t);  // over-relaxation, DDU (S/SUNc/AdvancedOperations.cpp:119-131)
+      mul_nn(t, gm, gn);
+    } else {
+      mul_dn(wt, gm, gn);  // DU (S/SUNc/SU3/GroupOperations.cpp:166-180)
+    }
+    st_d(G, g.S, 0, s, gn);
+  }
+  red::block_reduce_store<7>(v, op, partials + (long long)blockIdx.x * 7);
 }
 
 // ---- UG_mu(x) = G(x) U_mu(x) G^d(x+mu), interior sites
@@ -488,39 +617,60 @@ int prepare(GaugeFixState** ps, const GaugeFixArgs& a, std::string* err) {
   return GLASMA_OK;
 }
 
+// CopyFields (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:93-97): interior slices only
+template <typename T>
+cudaError_t copy_fields(const GaugeFixArgs& a) {
+  const Geometry& g = a.g;
+  const cx<T>* U = static_cast<const cx<T>*>(a.U);
+  const T* E = static_cast<const T*>(a.E);
+  cx<T>* UG = static_cast<cx<T>*>(a.UG);
+  T* EG = static_cast<T*>(a.EG);
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < 27 && e == cudaSuccess; c++)
+    e = cudaMemcpyAsync(UG + (long long)c * g.S + g.plane, U + (long long)c * g.S + g.plane, sizeof(cx<T>) * g.vol,
+                        cudaMemcpyDeviceToDevice, a.stream);
+  for (int c = 0; c < 24 && e == cudaSuccess; c++)
+    e = cudaMemcpyAsync(EG + (long long)c * g.S + g.plane, E + (long long)c * g.S + g.plane, sizeof(T) * g.vol,
+                        cudaMemcpyDeviceToDevice, a.stream);
+  return e;
+}
+// GaugeTransformLinks: UG from U and G, then the ghost slices of G
+template <typename T>
+cudaError_t transform_links_all(const GaugeFixArgs& a) {
+  const unsigned tb = (unsigned)((a.g.vol + 127) / 128);
+  transform_links_kernel<T><<<tb, 128, 0, a.stream>>>(a.g, static_cast<const cx<T>*>(a.U),
+                                                      static_cast<const cx<T>*>(a.G), static_cast<cx<T>*>(a.UG));
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_sync_ghosts<cx<T>>(a.g, static_cast<cx<T>*>(a.G), 9, a.stream);
+  return e;
+}
+// After the last iteration (CoulombGaugeFixing.cpp:84-86): GaugeTransformLinks, GaugeTransformElectricFields
+template <typename T>
+cudaError_t finish_fields(const GaugeFixArgs& a) {
+  cudaError_t e = transform_links_all<T>(a);
+  if (e != cudaSuccess) return e;
+  const unsigned tb = (unsigned)((a.g.vol + 127) / 128);
+  transform_efield_kernel<T><<<tb, 128, 0, a.stream>>>(a.g, static_cast<const T*>(a.E),
+                                                       static_cast<const cx<T>*>(a.G), static_cast<T*>(a.EG));
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_sync_ghosts<cx<T>>(a.g, static_cast<cx<T>*>(a.G), 9, a.stream)) != cudaSuccess) return e;
+  return cudaStreamSynchronize(a.stream);
+}
+
 template <typename T>
 int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
              double* log, int* iterations, std::string* err) {
   const Geometry& g = a.g;
   cudaStream_t st = a.stream;
-  const cx<T>* U = static_cast<const cx<T>*>(a.U);
-  const T* E = static_cast<const T*>(a.E);
   cx<T>* G = static_cast<cx<T>*>(a.G);
-  cx<T>* UG = static_cast<cx<T>*>(a.UG);
-  T* EG = static_cast<T*>(a.EG);
+  const cx<T>* UG = static_cast<const cx<T>*>(a.UG);
   auto cuda_err = [&](cudaError_t e, const char* where) {
     *err = std::string(where) + ": " + cudaGetErrorString(e);
     return GLASMA_ERR_CUDA;
   };
   cudaError_t e;
-  // CopyFields (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:93-97): interior slices only
-  for (int c = 0; c < 27; c++) {
-    e = cudaMemcpyAsync(UG + (long long)c * g.S + g.plane, U + (long long)c * g.S + g.plane, sizeof(cx<T>) * g.vol,
-                        cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) return cuda_err(e, "copy U");
-  }
-  for (int c = 0; c < 24; c++) {
-    e = cudaMemcpyAsync(EG + (long long)c * g.S + g.plane, E + (long long)c * g.S + g.plane, sizeof(T) * g.vol,
-                        cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) return cuda_err(e, "copy E");
-  }
-  const unsigned tb = (unsigned)((g.vol + 127) / 128);
-  auto transform_links = [&]() {
-    transform_links_kernel<T><<<tb, 128, 0, st>>>(g, U, G, UG);
-    cudaError_t e2 = cudaGetLastError();
-    if (e2 == cudaSuccess) e2 = launch_sync_ghosts<cx<T>>(g, G, 9, st);
-    return e2;
-  };
+  if ((e = copy_fields<T>(a)) != cudaSuccess) return cuda_err(e, "copy fields");
+  auto transform_links = [&]() { return transform_links_all<T>(a); };
   if ((e = transform_links()) != cudaSuccess) return cuda_err(e, "transform links");
 
   const double cw[3] = {(a.a_scale / g.a[0]) * (a.a_scale / g.a[0]), (a.a_scale / g.a[1]) * (a.a_scale / g.a[1]),
@@ -589,11 +739,75 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
   }
   *iterations = n;
   if (status != GLASMA_OK) return status;
-  if ((e = transform_links()) != cudaSuccess) return cuda_err(e, "transform links");
-  transform_efield_kernel<T><<<tb, 128, 0, st>>>(g, E, G, EG);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "transform E");
-  if ((e = launch_sync_ghosts<cx<T>>(g, G, 9, st)) != cudaSuccess) return cuda_err(e, "sync G");
-  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e, "final sync");
+  if ((e = finish_fields<T>(a)) != cudaSuccess) return cuda_err(e, "final transform");
+  return GLASMA_OK;
+}
+
+// SetCoulombGauge with the Los Alamos (los_alamos != 0) or the Jacobi update: per iteration one pass
+// over every site (Jacobi) or the even and then the odd sites (Los Alamos), the links re-transformed
+// after each pass; the monitors of both passes of an iteration are reduced together (the reference
+// resets them before the even pass only, LosAlamos.cpp:16-23).
+template <typename T>
+int run_local_impl(const GaugeFixArgs& a, int los_alamos, double param, unsigned long long seed, int max_iters,
+                   double tol, double* log, int* iterations, std::string* err) {
+  const Geometry& g = a.g;
+  cudaStream_t st = a.stream;
+  cx<T>* G = static_cast<cx<T>*>(a.G);
+  cx<T>* UG = static_cast<cx<T>*>(a.UG);
+  auto cuda_err = [&](cudaError_t e, const char* where) {
+    *err = std::string(where) + ": " + cudaGetErrorString(e);
+    return GLASMA_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = copy_fields<T>(a)) != cudaSuccess) return cuda_err(e, "copy fields");
+  if ((e = transform_links_all<T>(a)) != cudaSuccess) return cuda_err(e, "transform links");
+  const double cw[3] = {(a.a_scale / g.a[0]) * (a.a_scale / g.a[0]), (a.a_scale / g.a[1]) * (a.a_scale / g.a[1]),
+                        g.nz > 1 ? (a.a_scale / g.a[2]) * (a.a_scale / g.a[2]) : 0.0};
+  const int passes = los_alamos ? 2 : 1;
+  const long long slots = (long long)(los_alamos ? (g.nx + 1) / 2 : g.nx) * g.ny * g.nz;
+  const unsigned nb = blocks_for(slots, kGfThreads, kGfBlocks);
+  double* part = a.scratch;                        // passes * nb * 7
+  double* res = a.scratch + (size_t)kGfBlocks * 14;  // 7 results
+  const double minf0 = 2.0 * 3 * (1.0 / (g.a[0] * g.a[0]) + 1.0 / (g.a[1] * g.a[1]) + 1.0 / (g.a[2] * g.a[2]));
+  double h[7];
+  double gmax = 1.0;
+  int n = 0, status = GLASMA_OK;
+  while (n < max_iters && gmax > tol) {
+    for (int pass = 0; pass < passes; pass++) {
+      local_update_kernel<T><<<nb, kGfThreads, 0, st>>>(g, UG, G, cw[0], cw[1], cw[2], los_alamos,
+                                                        los_alamos ? pass : -1, param, seed, n,
+                                                        part + (size_t)pass * nb * 7);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "local update");
+      if ((e = transform_links_all<T>(a)) != cudaSuccess) return cuda_err(e, "transform links");
+    }
+    red::finish_kernel<7><<<1, red::kThreads, 0, st>>>(
+        part, (int)(nb * passes), 1 | (0 << 2) | (2 << 4) | (0 << 6) | (1 << 8) | (0 << 10) | (0 << 12), res);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "monitor reduction");
+    if ((e = cudaMemcpyAsync(h, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+      return cuda_err(e, "monitor copy");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e, "monitor sync");
+    const double V = (double)g.vol;
+    gmax = h[0];
+    if (log) {
+      double* o = log + 7 * (size_t)n;
+      o[0] = n;
+      o[1] = h[0];
+      o[2] = sqrt(h[1] / (8.0 * V));
+      o[3] = h[4];
+      o[4] = sqrt(h[5] / (8.0 * V));
+      o[5] = h[2] < minf0 ? h[2] : minf0;
+      o[6] = h[3] / V;
+    }
+    n++;
+    if (h[6] > 0.0) {
+      *err = "gauge update left SU(3) by more than 1e-13 (the reference exits here)";
+      status = GLASMA_ERR_NUMERICAL;
+      break;
+    }
+  }
+  *iterations = n;
+  if (status != GLASMA_OK) return status;
+  if ((e = finish_fields<T>(a)) != cudaSuccess) return cuda_err(e, "final transform");
   return GLASMA_OK;
 }
 
@@ -611,6 +825,21 @@ int gaugefix_run(GaugeFixState** state, const GaugeFixArgs& a, double alpha, int
   return a.precision == GLASMA_FP64 ? run_impl<double>(*state, a, alpha, max_iters, tol, flags, log, iterations, err)
                                     : run_impl<float>(*state, a, alpha, max_iters, tol, flags, log, iterations, err);
 }
+
+int gaugefix_run_local(const GaugeFixArgs& a, int algorithm, double param, unsigned long long seed, int max_iters,
+                       double tol, double* log, int* iterations, std::string* err) {
+  *iterations = 0;
+  if (a.scratch_doubles < gaugefix_scratch_doubles()) {
+    *err = "scratch too small";
+    return GLASMA_ERR_INVALID_ARGUMENT;
+  }
+  const int los_alamos = algorithm == GLASMA_GF_LOS_ALAMOS ? 1 : 0;
+  return a.precision == GLASMA_FP64
+             ? run_local_impl<double>(a, los_alamos, param, seed, max_iters, tol, log, iterations, err)
+             : run_local_impl<float>(a, los_alamos, param, seed, max_iters, tol, log, iterations, err);
+}
+
+size_t gaugefix_scratch_doubles() { return (size_t)kGfBlocks * 14 + 16; }
 
 void gaugefix_destroy(GaugeFixState* s) {
   if (!s) return;

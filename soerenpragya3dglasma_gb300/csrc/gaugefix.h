@@ -27,6 +27,12 @@ struct GaugeFixArgs {
 
 int gaugefix_run(GaugeFixState** state, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
                  double* log, int* iterations, std::string* err);
+// Los Alamos (GLASMA_GF_LOS_ALAMOS, param = over-relaxation probability) or Jacobi (GLASMA_GF_JACOBI,
+// param = step size) Coulomb gauge fixing; needs no FFT state.
+int gaugefix_run_local(const GaugeFixArgs& a, int algorithm, double param, unsigned long long seed, int max_iters,
+                       double tol, double* log, int* iterations, std::string* err);
+// scratch doubles the gauge fixers need (reduction partials and results)
+size_t gaugefix_scratch_doubles();
 void gaugefix_destroy(GaugeFixState* state);
 
 // Batched 1D transforms of length n in place over `total` complex values: element k of line l is

@@ -175,7 +175,8 @@ int ensure_staging(glasma_lattice* h, size_t bytes) {
 }
 
 int ensure_scratch(glasma_lattice* h) {
-  const size_t need = (size_t)glasma::observable_scratch_doubles(h->g) + (size_t)h->g.nz * 16 + 64;
+  size_t need = (size_t)glasma::observable_scratch_doubles(h->g) + (size_t)h->g.nz * 16 + 64;
+  if (need < glasma::gaugefix_scratch_doubles()) need = glasma::gaugefix_scratch_doubles();
   if (h->scratch_doubles >= need) return GLASMA_OK;
   if (h->scratch) {
     cudaStreamSynchronize(h->stream);
@@ -724,6 +725,38 @@ int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double to
   std::string err;
   int n = 0;
   st = glasma::gaugefix_run(&h->gf, a, alpha, max_iters, tol, flags, log, &n, &err);
+  if (iterations) *iterations = n;
+  if (st != GLASMA_OK) return fail(st, err);
+  return GLASMA_OK;
+}
+
+int glasma_coulomb_fix_algorithm(glasma_lattice* h, int algorithm, double param, unsigned long long seed, int max_iters,
+                                 double tol, unsigned flags, double* log, int* iterations) {
+  GLASMA_CHECK_HANDLE(h);
+  if (algorithm == GLASMA_GF_FOURIER) return glasma_coulomb_fix(h, param, max_iters, tol, flags, log, iterations);
+  if (algorithm != GLASMA_GF_LOS_ALAMOS && algorithm != GLASMA_GF_JACOBI)
+    return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown gauge-fixing algorithm");
+  if (max_iters < 0) return fail(GLASMA_ERR_INVALID_ARGUMENT, "max_iters < 0");
+  if (flags) return fail(GLASMA_ERR_INVALID_ARGUMENT, "gauge-fixing flags apply to the Fourier update only");
+  int st;
+  for (int f : {GLASMA_FIELD_G, GLASMA_FIELD_UG, GLASMA_FIELD_EG})
+    if ((st = ensure_field(h, f))) return st;
+  if ((st = ensure_scratch(h))) return st;
+  glasma::GaugeFixArgs a = {};
+  a.g = h->g;
+  a.precision = h->precision;
+  a.a_scale = h->a_scale;
+  a.stream = h->stream;
+  a.U = h->f[GLASMA_FIELD_U];
+  a.E = h->f[GLASMA_FIELD_E];
+  a.G = h->f[GLASMA_FIELD_G];
+  a.UG = h->f[GLASMA_FIELD_UG];
+  a.EG = h->f[GLASMA_FIELD_EG];
+  a.scratch = h->scratch;
+  a.scratch_doubles = h->scratch_doubles;
+  std::string err;
+  int n = 0;
+  st = glasma::gaugefix_run_local(a, algorithm, param, seed, max_iters, tol, log, &n, &err);
   if (iterations) *iterations = n;
   if (st != GLASMA_OK) return fail(st, err);
   return GLASMA_OK;

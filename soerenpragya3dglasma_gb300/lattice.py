@@ -263,14 +263,18 @@ class Lattice:
         return v.value, out
 
     # -- Coulomb gauge fixing (S/GAUGETRANSFORMATION)
-    def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False, fft_fp32=False):
-        """Fourier-accelerated Coulomb gauge fixing; returns the per-iteration log rows
-        (n, max dev, avg dev, max step, avg step, min functional, functional / V)."""
+    def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False, fft_fp32=False,
+                    algorithm="fourier", seed=0):
+        """Coulomb gauge fixing; returns the per-iteration log rows (n, max dev, avg dev, max step,
+        avg step, min functional, functional / V).  algorithm: "fourier" (alpha = the step size of the
+        Fourier-accelerated update), "los_alamos" (alpha = the over-relaxation probability; seed picks
+        the draws) or "jacobi" (alpha = the step size)."""
         log = np.zeros((max(int(max_iters), 1), 7))
         n = ctypes.c_int()
         flags = (_lib.GF_PROJECT_ZERO_MODE if project_zero_mode else 0) | (_lib.GF_FFT_FP32 if fft_fp32 else 0)
-        check(self.lib.glasma_coulomb_fix(self.h, float(alpha), int(max_iters), float(tol), flags,
-                                          log.ctypes.data_as(_lib._D), ctypes.byref(n)))
+        check(self.lib.glasma_coulomb_fix_algorithm(self.h, _lib.GF_ALGORITHMS[algorithm], float(alpha), int(seed),
+                                                    int(max_iters), float(tol), flags,
+                                                    log.ctypes.data_as(_lib._D), ctypes.byref(n)))
         return log[: n.value]
 
     def fft3d(self, X, inverse=False):
@@ -294,6 +298,30 @@ class Lattice:
         complex floats with fp32)."""
         fn = self.lib.glasma_fft3d_f32 if fp32 else self.lib.glasma_fft3d
         check(fn(self.h, ctypes.c_void_p(int(in_ptr)), ctypes.c_void_p(int(out_ptr)), int(inverse)))
+
+    # -- configuration files
+    def save_text(self, links=None, efield=None, currents=None):
+        """The reference's text files (IO::SaveConfiguration / SaveConfigurationJ); any path may be None."""
+        from .checkpoint import _io_check, _path
+
+        _io_check(self.lib, self.lib.glasma_save_text(self.h, _path(links), _path(efield), _path(currents)))
+
+    def load_text(self, links=None, efield=None, currents=None):
+        """Read the reference's text files into the lattice (IO::LoadConfiguration)."""
+        from .checkpoint import _io_check, _path
+
+        _io_check(self.lib, self.lib.glasma_load_text(self.h, _path(links), _path(efield), _path(currents)))
+
+    def save_binary(self, path):
+        """Bit-exact restart file of U, UOld, E and the four currents."""
+        from .checkpoint import _io_check, _path
+
+        _io_check(self.lib, self.lib.glasma_save_binary(self.h, _path(path)))
+
+    def load_binary(self, path):
+        from .checkpoint import _io_check, _path
+
+        _io_check(self.lib, self.lib.glasma_load_binary(self.h, _path(path)))
 
     def gauge_reset(self):
         check(self.lib.glasma_gauge_reset(self.h))

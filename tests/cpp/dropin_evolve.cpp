@@ -2,7 +2,9 @@
 // compiled against include/glasma_gb300_reference_api.hpp instead of the reference's modules.
 // Usage: dropin_evolve Nx Ny Nz dt nsteps in_prefix out_prefix
 // Reads <in_prefix>.{U,E,Jp,Jm,JpStat,JmStat}.bin (reference host layout, FP64), evolves, writes
-// <out_prefix>.{U,UOld,E,Jp,Jm,JpStat,JmStat}.bin and prints the bulk energy and Gauss law.
+// <out_prefix>.{U,UOld,E,Jp,Jm,JpStat,JmStat}.bin, the reference's text configuration files
+// <out_prefix>.{U,E,J}ID<seed>.txt (IO::SaveConfiguration / SaveConfigurationJ) and prints the bulk
+// energy and Gauss law.
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -60,6 +62,9 @@ int main(int argc, char** argv) {
     write_from(out + ".Jm.bin", SUNcChargeDensity::Jm->Get(0, 0, -1, 0), 8 * S);
     write_from(out + ".JpStat.bin", SUNcChargeDensity::JpStat->Get(0, 0, -1, 0), 8 * S);
     write_from(out + ".JmStat.bin", SUNcChargeDensity::JmStat->Get(0, 0, -1, 0), 8 * S);
+    IO::OutputDirectory = out + ".";
+    IO::SaveConfiguration("U", "E");
+    IO::SaveConfigurationJ("J");
   } catch (const glasma_dropin::Error& e) {
     std::fprintf(stderr, "glasma error %d: %s\n", e.status, e.what());
     return 3;

@@ -17,6 +17,15 @@ Fixtures (npz, float64/complex128, reference host layout with ghost slices):
   expi.npz              MatrixIExp known answers
   mv_collision.npz      MV collision initial state on 4x4x16 (injected Gaussian
                         charges), observables at t=0 and after 8 steps
+  config_text.npz       the reference's text configuration files (IO::SaveConfiguration,
+                        SaveConfigurationJ) of seeded fields on 3x2x2, and what its
+                        IO::LoadConfiguration reads back from them
+  coulomb_local.npz     4x3x5 anisotropic lattice, weak field in a random gauge: the
+                        reference's Los Alamos update (over-relaxation probability 0, and
+                        0.5 with the draws injected into its rng()) and its Jacobi update,
+                        run single-threaded (log at full precision, G, gauge-fixed U and E)
+
+    python tests/golden/make_golden.py config_text     # only the named cases
 """
 import multiprocessing as mp
 import os
@@ -128,6 +137,75 @@ def mv_case(q):
     q.put(res)
 
 
+CONFIG = dict(N=(3, 2, 2), a=(1.0, 1.0, 1.0), seed=77)
+
+
+def config_fields():
+    """Seeded fields with a spread of magnitudes (exponent formats, a negative zero)."""
+    c = CONFIG
+    f = O.random_fields(c["N"], c["seed"])
+    f["E"].reshape(-1)[::7] *= 1e-9
+    f["E"].reshape(-1)[3::11] *= 1e7
+    f["Jp"].reshape(-1)[5] = -0.0
+    f["JmStat"].reshape(-1)[::5] *= 1e-12
+    return f
+
+
+def config_case(q):
+    c = CONFIG
+    N = c["N"]
+    f = config_fields()
+    ref = O.Reference(N, c["a"])
+    ref.set_fields(f)
+    paths = ref.save_configuration()
+    res = {"in_" + k: v for k, v in f.items()}
+    for name, path in zip(("links", "efield", "currents"), paths):
+        res["file_" + name] = np.frombuffer(open(path, "rb").read(), dtype=np.uint8)
+    # load into fields holding a sentinel, to show what the reference's loader fills
+    sentinel = {k: np.full_like(v, 7.0) for k, v in f.items()}
+    ref.set_fields(sentinel)
+    ref.load_configuration(*paths)
+    for k, v in ref.get_fields().items():
+        res["loaded_" + k] = v
+    q.put(res)
+
+
+LOCAL = dict(N=(4, 3, 5), a=(1.0, 0.9, 0.8), seed=21, iters=4, draw_seed=11)
+LOCAL_RUNS = (("la0", "los_alamos", 0.0), ("la5", "los_alamos", 0.5), ("jac", "jacobi", 0.3))
+
+
+def local_case(q):
+    """LosAlamosAlgorithm / JacobiAlgorithm::UpdateGaugeTransformation of the reference, one fresh
+    lattice per run, one thread (so that its rng() calls come in site order)."""
+    c = LOCAL
+    N = c["N"]
+    res = {}
+    oracle = O.Oracle()
+    for tag, alg, param in LOCAL_RUNS:
+        f = mild_gauge_config(N, c["seed"])
+        ref = O.Reference(N, c["a"], threads=1)
+        ref.set_fields(f)
+        u = oracle.gf_uniforms_in_site_order(N, c["draw_seed"], c["iters"]) if alg == "los_alamos" else ()
+        res[tag + "_log"] = ref.coulomb_fix_local(alg, param, c["iters"], u)
+        for k in ("G", "UG", "EG"):
+            res[tag + "_" + k] = ref.get(k)
+        if tag == "la0":
+            res["U"], res["E"] = f["U"], f["E"]
+    q.put(res)
+
+
+# fixture name -> (case function, configuration stored beside it); the functions run in spawned
+# children, so they are named here rather than passed as closures
+CASES = {
+    "leapfrog_random": ("leapfrog_case", LEAPFROG),
+    "coulomb_mild": ("coulomb_case", COULOMB),
+    "expi": ("expi_case", {}),
+    "mv_collision": ("mv_case", MV),
+    "config_text": ("config_case", CONFIG),
+    "coulomb_local": ("local_case", LOCAL),
+}
+
+
 def run(fn):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
@@ -138,23 +216,21 @@ def run(fn):
     return res
 
 
-def main():
+def main(cases):
     from oracle import build
 
     if build.build_reference() is None:
         raise SystemExit("reference sources not found; fixtures can only be generated where they exist")
-    r = run(leapfrog_case)
-    np.savez_compressed(os.path.join(HERE, "leapfrog_random.npz"), **r, **{"cfg_" + k: np.array(v) for k, v in LEAPFROG.items()})
-    r = run(coulomb_case)
-    np.savez_compressed(os.path.join(HERE, "coulomb_mild.npz"), **r, **{"cfg_" + k: np.array(v) for k, v in COULOMB.items()})
-    r = run(expi_case)
-    np.savez_compressed(os.path.join(HERE, "expi.npz"), **r)
-    r = run(mv_case)
-    np.savez_compressed(os.path.join(HERE, "mv_collision.npz"), **r, **{"cfg_" + k: np.array(v) for k, v in MV.items()})
+    for name in cases or list(CASES):
+        if name not in CASES:
+            raise SystemExit("unknown case " + name)
+        fn, cfg = CASES[name]
+        r = run(globals()[fn])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **r, **{"cfg_" + k: np.array(v) for k, v in cfg.items()})
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

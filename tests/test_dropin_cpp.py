@@ -8,6 +8,7 @@ import pytest
 
 from oracle import oracle as O
 from soerenpragya3dglasma_gb300 import build
+from soerenpragya3dglasma_gb300.checkpoint import read_text
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "dropin_evolve.cpp")
@@ -46,3 +47,11 @@ def test_dropin_driver_matches_oracle(tmp_path, oracle):
     assert abs(vals["T00"][0] - bulk[9]) / abs(bulk[9]) < 1e-12
     assert np.allclose(vals["GAUSS"], oracle.gauss(ref, N, (1.0, 1.0, 1.0)), rtol=1e-12)
     assert abs(vals["TIME"][0] - steps * dt) < 1e-12
+    # the reference's text configuration files, written through IO::SaveConfiguration(J)
+    txt = read_text(N, links=tmp_path / "out.UID0.txt", efield=tmp_path / "out.EID0.txt",
+                    currents=tmp_path / "out.JID0.txt")
+    for k in ("U", "E", "Jp", "Jm", "JpStat", "JmStat"):
+        got = np.fromfile(str(tmp_path / ("out.%s.bin" % k)), dtype=ref[k].dtype).reshape(ref[k].shape)
+        x = got.view(np.float64) if np.iscomplexobj(got) else got
+        y = txt[k].view(np.float64) if np.iscomplexobj(txt[k]) else txt[k]
+        assert np.all(np.abs(y - x) <= 6e-15 * np.abs(x)), k  # 15 significant digits, then a parse

@@ -73,3 +73,23 @@ def test_mv_collision_evolution_matches_reference(oracle, golden_dir):
     assert np.allclose(oracle.bulk(f, N, a), g["t8_bulk"], rtol=1e-11, atol=1e-11)
     assert np.allclose(oracle.gauss(f, N, a), g["t8_gauss"], rtol=1e-10, atol=1e-15)
     assert np.allclose(oracle.emt_map(f, N, a), g["t8_emt"], rtol=1e-10, atol=1e-14)
+
+
+@pytest.mark.parametrize("tag,alg,param", [("la0", "los_alamos", 0.0), ("la5", "los_alamos", 0.5),
+                                           ("jac", "jacobi", 0.3)])
+def test_local_gauge_fixers_match_reference(oracle, golden_dir, tag, alg, param):
+    """Los Alamos (with and without over-relaxation draws) and Jacobi against the reference's own
+    LosAlamosAlgorithm / JacobiAlgorithm::UpdateGaugeTransformation (tests/golden/coulomb_local.npz)."""
+    g = _load(golden_dir, "coulomb_local.npz")
+    N, a = tuple(int(v) for v in g["cfg_N"]), tuple(g["cfg_a"])
+    f = {"U": g["U"].copy(), "E": g["E"].copy()}
+    G = O.identity_gauge(N)
+    st, log, UG, EG = oracle.coulomb_fix_local(f, G, N, a, alg, param, int(g["cfg_iters"]),
+                                               seed=int(g["cfg_draw_seed"]))
+    assert st == 0 and len(log) == len(g[tag + "_log"])
+    # Los Alamos: the same operations in the same order; Jacobi: exp(i t.a) by Cayley-Hamilton here,
+    # by eigen-decomposition in the reference (the step sizes 3 - tr differ in their last digits)
+    tol = 1e-14 if alg == "los_alamos" else 1e-13
+    assert np.allclose(log, g[tag + "_log"], rtol=1e-10, atol=1e-14)
+    for k, v in (("G", G), ("UG", UG), ("EG", EG)):
+        assert np.max(np.abs(v - g[tag + "_" + k])) < tol, k
