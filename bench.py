@@ -659,6 +659,51 @@ def run_fft(args):
     print(json.dumps(line), flush=True)
 
 
+def run_tmd(args):
+    """The TMD / Glauber initial state of SimulationmitPC::Run at the reference's parameters: 128x128x2048,
+    Au nuclei (A = 197, Lorentz factor 250) centred on slices 785 and 1261, seeded noise and nucleon
+    draws.  Times glasma_tmd_init end to end (noise uploads and the host profile tables included) and
+    checks the state: links unitary, Gauss law."""
+    import numpy as np
+    import torch
+
+    from soerenpragya3dglasma_gb300 import Lattice, build, glauber_sample
+
+    build.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    N = tuple(int(v) for v in args.lattice.split(",")) if args.lattice else (128, 128, 2048)
+    rng = np.random.Generator(np.random.PCG64(4242))
+    noise = [rng.standard_normal(8 * N[0] * N[1] * N[2]) for _ in range(2)]
+    uni = rng.random(400000)
+    left, used = glauber_sample(197, uni)
+    right, _ = glauber_sample(197, uni[used:])
+    times = []
+    with Lattice(N, stream=stream) as lat:
+        for i in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lat.tmd_init(noise[0], noise[1], left, right, dt=0.125)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i > 0:
+                times.append(e0.elapsed_time(e1))
+        umax, _ = lat.unitarity()
+        gmax, gavg = lat.gauss()
+        t00 = lat.bulk()[9]
+    ms = float(np.median(times))
+    line = {"metric": "TMD initial state: lattice sites per second", "value": N[0] * N[1] * N[2] / (ms * 1e-3),
+            "unit": "sites/s", "n_gpus": 1, "steps": len(times), "warmup": 1, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "seeded N(0,1) noise and uniform nucleon draws (numpy PCG64 seed 4242)",
+            "config": {"workload": "TMD/Glauber initial state %dx%dx%d, A=197, reference parameters" % N,
+                       "lattice": list(N)},
+            "ms_per_init": ms, "unitarity_max": umax, "gauss_max": gmax, "gauss_avg": gavg, "t00": t00}
+    print(json.dumps(line), flush=True)
+
+
 def run_adjoint(args):
     """The adjoint workload: a 64x64x256 MV collision (g^2 mu = 0.5, m = 0.2, sigma_z = 4, centres
     128 -+ 24, seeded charges), FP64, 400 steps at dt = 0.125, objective P_L/P_T over the central 32
@@ -765,9 +810,10 @@ def main():
                     help="which precisions to run (profiling runs); the JSON line needs both")
     ap.add_argument("--lattice", default=None, help="Nx,Ny,Nz instead of the workload's (profiling runs)")
     ap.add_argument("--event-shape", default=None, help="NX,NY,NZ for every batched event (profiling runs)")
-    ap.add_argument("--workload", default="production", choices=["production", "batched", "adjoint", "fft"],
+    ap.add_argument("--workload", default="production", choices=["production", "batched", "adjoint", "fft", "tmd"],
                     help="production: the headline 128x128x512 line; batched: 64 uneven events in one launch; "
-                         "adjoint: the gradient of P_L/P_T on a 64x64x256 collision; fft: the 3D FFT alone")
+                         "adjoint: the gradient of P_L/P_T on a 64x64x256 collision; fft: the 3D FFT alone; "
+                         "tmd: the TMD/Glauber initial state at 128x128x2048")
     ap.add_argument("--adj-steps", type=int, default=400)
     ap.add_argument("--fd-dirs", type=int, default=2)
     ap.add_argument("--events", type=int, default=64)
@@ -786,6 +832,8 @@ def main():
         run_adjoint(args)
     elif args.workload == "fft":
         run_fft(args)
+    elif args.workload == "tmd":
+        run_tmd(args)
     else:
         run_ours(args)
 

@@ -200,6 +200,42 @@ int glasma_mv_init(glasma_lattice* h, int single_left, const double* zeta_left, 
                    double meff, double dt);
 const char* glasma_mv_last_error(void);
 
+/* Parameters of the TMD / Glauber initial state, under the reference's names (S/LATTICE/Parameters.cpp
+ * and the nuclear centres of S/TMDNUCLEUS/TMDbased.cpp:41-50); the reference's values in brackets for
+ * a = 1.  glasma_tmd_default_params fills them. */
+typedef struct {
+  int atomic_number;   /* Parameters::AtomicNumber [197]; 16, 54, 197 or 208 (NuclearData.cpp) */
+  double qs0a;         /* Parameters::Qs0A, lattice units [0.33] */
+  double meff;         /* Parameters::MEff, infrared cut-off of the 2D filter [Qs0A] */
+  double ax_fm, ay_fm; /* Parameters::aXInFm, aYInFm [Qs0A 0.197 / 0.5] */
+  double az_fm;        /* Parameters::aZInFm [aXInFm / (Qs0A 512)] */
+  double com_energy;   /* Parameters::CoMEnergy in fm^-1 [500 / 0.197]; Lorentz factor = com_energy 0.197 / 2 */
+  int center_left;     /* slice of the left nucleus' centre [785] */
+  int center_right;    /* slice of the right nucleus' centre [1261] */
+  double dt;           /* Dynamics::dTStep of the first step (SingleSheet) */
+} glasma_tmd_params;
+
+void glasma_tmd_default_params(glasma_tmd_params* p, double dt);
+
+/* The Woods-Saxon nucleus of Nucleus::SetNucleonPositions (S/TMDNUCLEUS/GBWSampling.cpp:20-84):
+ * rejection sampling of A nucleons from the uniform draws the reference takes from rng() (four per
+ * trial: x, y, z in [-4R, 4R), acceptance), then the centre of mass moved to the origin.  positions:
+ * A x 3 doubles in fm; used (may be NULL): draws consumed.  Host only.  GLASMA_ERR_INVALID_ARGUMENT
+ * when A has no Woods-Saxon entry or the draws run out. */
+int glasma_glauber_sample(int A, const double* uniforms, long n_uniforms, double* positions, long* used);
+
+/* The TMD / Glauber initial state of SimulationmitPC::Run (S/SimulationmitPC.cpp:315-367): per nucleus
+ * ChargeDistributions::ChargeFluctuation (S/TMDNUCLEUS/CorrelationFunction.cpp:23-97) from the injected
+ * noise, TmdBasedCollision::SetWilsonLines (S/TMDNUCLEUS/TMDbased.cpp:243-291) with the given nucleons,
+ * then InitialConditions::SingleSheet for both nuclei and the ghost syncs.  noise_left / noise_right:
+ * 8 Nx Ny Nz N(0,1) numbers each, in the order the reference draws them (index a + 8 (x + Nx (y + Ny z)));
+ * nucleons_left / nucleons_right: A x 3 positions (glasma_glauber_sample).  rho_left / rho_right (may be
+ * NULL): receive the filtered densities SUNcChargeDensity::rhoL / rhoR (8 doubles per site, ghost slices
+ * included).  Host arrays. */
+int glasma_tmd_init(glasma_lattice* h, const double* noise_left, const double* noise_right,
+                    const double* nucleons_left, const double* nucleons_right, const glasma_tmd_params* params,
+                    double* rho_left, double* rho_right);
+
 /* Configuration files in the reference's text format: IO::SaveConfiguration and
  * IO::SaveConfigurationJ (S/IO/SaveConfiguration.cpp:6-93) write the links, E and the four currents
  * one entry per line, ghost slices included, with 15 significant digits; IO::LoadConfiguration

@@ -285,7 +285,8 @@ LOCAL_GAUGE_ALGORITHMS = {"los_alamos": 1, "jacobi": 2}
 
 
 # ----------------------------------------------------------------- the reference itself
-_FIELD_ID = {"U": 0, "UOld": 1, "E": 2, "Jp": 3, "Jm": 4, "JpStat": 5, "JmStat": 6, "G": 7, "UG": 8, "EG": 9}
+_FIELD_ID = {"U": 0, "UOld": 1, "E": 2, "Jp": 3, "Jm": 4, "JpStat": 5, "JmStat": 6, "G": 7, "UG": 8, "EG": 9,
+             "rhoL": 10, "rhoR": 11, "CFL": 12, "CFR": 13, "RhoLT1": 14, "RhoRT1": 15, "VLeft": 16, "VRight": 17}
 
 
 class Reference:
@@ -319,6 +320,9 @@ class Reference:
         L.ref_set_threads.argtypes = [ctypes.c_int]
         L.ref_save_configuration.argtypes = [ctypes.c_char_p] * 3
         L.ref_load_configuration.argtypes = [ctypes.c_char_p] * 3
+        L.ref_tmd_init.argtypes = [_dp, ctypes.c_long, _dp, ctypes.c_long, ctypes.c_double, ctypes.c_int] + \
+            [ctypes.c_double] * 6
+        L.ref_uniforms_used.restype = ctypes.c_long
         L.ref_mv_init.argtypes = [_dp, ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]
         self._tmp = tempfile.mkdtemp(prefix="glasma_ref_")
@@ -348,7 +352,7 @@ class Reference:
             out = np.zeros(shape_links(N), dtype=np.complex128)
         elif name in ("E", "EG"):
             out = zero_efield(N)
-        elif name == "G":
+        elif name in ("G", "VLeft", "VRight"):
             out = identity_gauge(N)
         else:
             out = zero_current(N)
@@ -404,6 +408,14 @@ class Reference:
         out = np.zeros(9, dtype=np.complex128)
         self.lib.ref_expi(c, _ptr(np.ascontiguousarray(alpha, dtype=np.float64)), _ptr(out))
         return out.reshape(3, 3).T
+
+    def tmd_init(self, gauss, uniforms, dt, A, qs0a, meff, ax_fm, ay_fm, az_fm, com_energy):
+        """SimulationmitPC::Run's initial state; gauss / uniforms replay Gauss() / rng().  Returns the
+        number of uniforms the nucleon sampling consumed."""
+        g = np.ascontiguousarray(gauss, dtype=np.float64)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        self.lib.ref_tmd_init(_ptr(g), g.size, _ptr(u), u.size, dt, int(A), qs0a, meff, ax_fm, ay_fm, az_fm, com_energy)
+        return self.lib.ref_uniforms_used()
 
     def mv_init(self, gauss, dt, qs_left, qs_right, center_left, center_right, sigma, lam, meff, single_left=False):
         g = np.ascontiguousarray(gauss, dtype=np.float64)

@@ -140,6 +140,10 @@ void SUNcMatrix(DOUBLE Amplitude, SU_Nc_FUNDAMENTAL_FORMAT* V) {
 #include "FFT/FFT2D.cpp"
 #include "FFT/FFT3D.cpp"
 #include "COLLIDINGOBJECTS/CollidingObjects.cpp"
+#include "TMDNUCLEUS/NuclearData.cpp"
+#include "TMDNUCLEUS/GBWSampling.cpp"
+#include "TMDNUCLEUS/CorrelationFunction.cpp"
+#include "TMDNUCLEUS/TMDbased.cpp"
 #include "INITIALCONDITIONS/SUNCCURRENTS/RevSingleNucleus.cpp"
 #include "IO/SaveConfiguration.cpp"
 #include "IO/LoadConfiguration.cpp"
@@ -168,6 +172,15 @@ void* FieldPointer(int which, long* n_doubles) {
     case 7: *n_doubles = 2 * 9 * S; return GaugeTransformation::G->G;
     case 8: *n_doubles = 2 * 27 * S; return GaugeFixedVariables::U->U;
     case 9: *n_doubles = 24 * S; return GaugeFixedVariables::E->E;
+    // the initial-condition intermediates (S/LATTICE/SUNcVariables.cpp:41-60)
+    case 10: *n_doubles = 8 * S; return SUNcChargeDensity::rhoL->J;
+    case 11: *n_doubles = 8 * S; return SUNcChargeDensity::rhoR->J;
+    case 12: *n_doubles = 8 * S; return SUNcChargeDensity::CFL->J;
+    case 13: *n_doubles = 8 * S; return SUNcChargeDensity::CFR->J;
+    case 14: *n_doubles = 8 * S; return SUNcChargeDensity::RhoLT1->J;
+    case 15: *n_doubles = 8 * S; return SUNcChargeDensity::RhoRT1->J;
+    case 16: *n_doubles = 2 * 9 * S; return SUNcWilsonLines::VLeft->V;
+    case 17: *n_doubles = 2 * 9 * S; return SUNcWilsonLines::VRight->V;
     default: *n_doubles = 0; return nullptr;
   }
 }
@@ -393,5 +406,52 @@ void ref_mv_init(const double* gauss, long n_gauss, double dt, double qsL, doubl
   SUNcGaugeLinks::UOld->SynchronizeGhostCells();
   SUNcElectricFields::E->SynchronizeGhostCells();
 }
+
+// The TMD / Glauber initial state of SimulationmitPC::Run (S/SimulationmitPC.cpp:315-367): per nucleus
+// ChargeDistributions::ChargeFluctuation (S/TMDNUCLEUS/CorrelationFunction.cpp:23-97) and
+// TmdBasedCollision::SetWilsonLines (S/TMDNUCLEUS/TMDbased.cpp:243-291, its Nucleus sampled as in
+// S/TMDNUCLEUS/GBWSampling.cpp), left first; then SingleSheet for both nuclei and the ghost syncs.
+// gauss: the Gauss() values in call order (8 Nx Ny Nz per nucleus); uniforms: the rng() values (the
+// nucleon positions).  The Parameters the reference derives at static initialisation are set here.
+void ref_tmd_init(const double* gauss, long n_gauss, const double* uniforms, long n_uniforms, double dt, int A,
+                  double qs0a, double meff, double ax_fm, double ay_fm, double az_fm, double com_energy) {
+  RandomNumberGenerator::Injected.assign(gauss, gauss + n_gauss);
+  RandomNumberGenerator::Cursor = 0;
+  RandomNumberGenerator::Uniforms.assign(uniforms, uniforms + n_uniforms);
+  RandomNumberGenerator::UniformCursor = 0;
+  Dynamics::dTStep = dt;
+  Dynamics::Reset();
+  Parameters::AtomicNumber = A;
+  Parameters::Qs0A = qs0a;
+  Parameters::MEff = meff;
+  Parameters::aXInFm = ax_fm;
+  Parameters::aYInFm = ay_fm;
+  Parameters::aZInFm = az_fm;
+  Parameters::CoMEnergy = com_energy;
+  ChargeDistributions::ChargeFluctuation(SUNcChargeDensity::CFL, 'L');
+  SUNcChargeDensity::CFL->SynchronizeGhostCells();
+  TmdBasedCollision::SetWilsonLines(SUNcChargeDensity::rhoL, SUNcChargeDensity::CFL, SUNcWilsonLines::VLeft, 'L');
+  SUNcChargeDensity::rhoL->SynchronizeGhostCells();
+  ChargeDistributions::ChargeFluctuation(SUNcChargeDensity::CFR, 'R');
+  SUNcChargeDensity::CFR->SynchronizeGhostCells();
+  TmdBasedCollision::SetWilsonLines(SUNcChargeDensity::rhoR, SUNcChargeDensity::CFR, SUNcWilsonLines::VRight, 'R');
+  SUNcChargeDensity::rhoR->SynchronizeGhostCells();
+  InitialConditions::SingleSheet::SingleSheet(SUNcChargeDensity::rhoL, 0, (Lattice::N[2] - 2) / 2,
+                                              SUNcChargeDensity::RhoLT1, SUNcWilsonLines::VLeft, 'L',
+                                              SUNcChargeDensity::JpStat, SUNcChargeDensity::Jp);
+  InitialConditions::SingleSheet::SingleSheet(SUNcChargeDensity::rhoR, Lattice::N[2] / 2, Lattice::N[2] - 1,
+                                              SUNcChargeDensity::RhoRT1, SUNcWilsonLines::VRight, 'R',
+                                              SUNcChargeDensity::JmStat, SUNcChargeDensity::Jm);
+  SUNcChargeDensity::JpStat->SynchronizeGhostCells();
+  SUNcChargeDensity::Jp->SynchronizeGhostCells();
+  SUNcChargeDensity::JmStat->SynchronizeGhostCells();
+  SUNcChargeDensity::Jm->SynchronizeGhostCells();
+  SUNcGaugeLinks::U->SynchronizeGhostCells();
+  SUNcGaugeLinks::UOld->SynchronizeGhostCells();
+  SUNcElectricFields::E->SynchronizeGhostCells();
+}
+
+// How many rng() values the last run consumed (the rejection sampling's count is not known in advance).
+long ref_uniforms_used() { return (long)RandomNumberGenerator::UniformCursor; }
 
 }  // extern "C"

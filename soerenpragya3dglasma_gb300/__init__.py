@@ -10,6 +10,7 @@ Observables::Bulk, ...) over the same handle.
 """
 from ._lib import GlasmaError, load  # noqa: F401
 from .batch import Batch  # noqa: F401
-from .lattice import DYNAMICAL_FIELDS, Lattice, empty_field, field_shape  # noqa: F401
+from .lattice import DYNAMICAL_FIELDS, Lattice, empty_field, field_shape, glauber_sample, tmd_default_params  # noqa: F401
 
-__all__ = ["Lattice", "Batch", "GlasmaError", "load", "field_shape", "empty_field", "DYNAMICAL_FIELDS"]
+__all__ = ["Lattice", "Batch", "GlasmaError", "load", "field_shape", "empty_field", "DYNAMICAL_FIELDS",
+           "glauber_sample", "tmd_default_params"]

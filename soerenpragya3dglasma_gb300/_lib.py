@@ -21,6 +21,16 @@ GF_PROJECT_ZERO_MODE = 0x1
 GF_FFT_FP32 = 0x2
 GF_ALGORITHMS = {"fourier": 0, "los_alamos": 1, "jacobi": 2}
 
+
+
+class TmdParams(ctypes.Structure):
+    """glasma_tmd_params (include/glasma_gb300.h)."""
+    _fields_ = [("atomic_number", ctypes.c_int), ("qs0a", ctypes.c_double), ("meff", ctypes.c_double),
+                ("ax_fm", ctypes.c_double), ("ay_fm", ctypes.c_double), ("az_fm", ctypes.c_double),
+                ("com_energy", ctypes.c_double), ("center_left", ctypes.c_int), ("center_right", ctypes.c_int),
+                ("dt", ctypes.c_double)]
+
+
 # (name, restype, argtypes) for every symbol declared in include/glasma_gb300.h
 _H = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
@@ -59,6 +69,9 @@ SIGNATURES = [
     ("glasma_mv_init", ctypes.c_int, [_H, ctypes.c_int, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("glasma_mv_last_error", ctypes.c_char_p, []),
+    ("glasma_tmd_default_params", None, [ctypes.POINTER(TmdParams), ctypes.c_double]),
+    ("glasma_glauber_sample", ctypes.c_int, [ctypes.c_int, _D, ctypes.c_long, _D, ctypes.POINTER(ctypes.c_long)]),
+    ("glasma_tmd_init", ctypes.c_int, [_H, _D, _D, _D, _D, ctypes.POINTER(TmdParams), _D, _D]),
     ("glasma_fill_synthetic", ctypes.c_int, [_H, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_double]),
     ("glasma_autotune", ctypes.c_int, [_H, ctypes.c_double, _I]),

@@ -60,6 +60,28 @@ def _address(arr, n_doubles):
     return arr.data_ptr()
 
 
+def tmd_default_params(dt=0.125):
+    """The reference's TMD parameters for unit lattice spacing (glasma_tmd_default_params)."""
+    lib = _lib.load()
+    p = _lib.TmdParams()
+    lib.glasma_tmd_default_params(ctypes.byref(p), float(dt))
+    return p
+
+
+def glauber_sample(A, uniforms):
+    """Nucleon positions (A, 3) in fm from the reference's rng() draws, and the number of draws used
+    (Nucleus::SetNucleonPositions; host only)."""
+    lib = _lib.load()
+    u = np.ascontiguousarray(uniforms, dtype=np.float64)
+    pos = np.zeros((A, 3))
+    used = ctypes.c_long()
+    st = lib.glasma_glauber_sample(int(A), u.ctypes.data_as(_lib._D), u.size, pos.ctypes.data_as(_lib._D),
+                                   ctypes.byref(used))
+    if st:
+        raise _lib.GlasmaError(st, lib.glasma_mv_last_error().decode(errors="replace"))
+    return pos, used.value
+
+
 class Lattice:
     """One lattice resident in GPU memory (the reference's global field singletons,
     S/LATTICE/SUNcVariables.cpp:4-90, become one handle)."""
@@ -117,6 +139,28 @@ class Lattice:
                                      float(meff), float(dt))
         if st:
             raise _lib.GlasmaError(st, self.lib.glasma_mv_last_error().decode(errors="replace"))
+
+    def tmd_init(self, noise_left, noise_right, nucleons_left, nucleons_right, dt=0.125, return_densities=False,
+                 **params):
+        """TMD / Glauber initial state on the GPU (SimulationmitPC::Run).  noise_*: 8*Nx*Ny*Nz N(0,1)
+        numbers in the order a + 8*(x + Nx*(y + Ny*z)); nucleons_*: (A, 3) positions in fm (glauber_sample).
+        params override tmd_default_params(dt) by field name.  With return_densities, returns the
+        filtered densities (rhoL, rhoR) in the reference's ChargeDensity layout."""
+        p = tmd_default_params(dt)
+        for k, v in params.items():
+            setattr(p, k, v)
+        N = self.N
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (noise_left, noise_right, nucleons_left,
+                                                                     nucleons_right)]
+        assert arrs[0].size == arrs[1].size == 8 * N[0] * N[1] * N[2]
+        assert arrs[2].size == arrs[3].size == 3 * p.atomic_number
+        rho = [np.zeros((N[2] + 2, N[1], N[0], 8)) for _ in range(2)] if return_densities else [None, None]
+        ptrs = [a.ctypes.data_as(_lib._D) for a in arrs]
+        rptr = [r.ctypes.data_as(_lib._D) if r is not None else None for r in rho]
+        st = self.lib.glasma_tmd_init(self.h, *ptrs, ctypes.byref(p), *rptr)
+        if st:
+            raise _lib.GlasmaError(st, self.lib.glasma_mv_last_error().decode(errors="replace"))
+        return tuple(rho) if return_densities else None
 
     def fill_synthetic(self, seed, link_amp=0.3, e_amp=0.1, j_amp=0.02):
         """Seeded synthetic fields generated on the device (links exp(i link_amp t.r), Gaussian E, J)."""

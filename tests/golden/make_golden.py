@@ -20,6 +20,11 @@ Fixtures (npz, float64/complex128, reference host layout with ghost slices):
   config_text.npz       the reference's text configuration files (IO::SaveConfiguration,
                         SaveConfigurationJ) of seeded fields on 3x2x2, and what its
                         IO::LoadConfiguration reads back from them
+  tmd_glauber.npz       the TMD / Glauber initial state of SimulationmitPC::Run on 4x4x1024
+                        (Lorentz factor 5.2, so that no slice's nuclear profile falls into
+                        the subnormal range where the reference's eigen-decomposition exp
+                        fails): per-slice sums of squares of every field, and the full
+                        fields on ten slices; inputs regenerated from PCG64 seeds
   coulomb_local.npz     4x3x5 anisotropic lattice, weak field in a random gauge: the
                         reference's Los Alamos update (over-relaxation probability 0, and
                         0.5 with the draws injected into its rng()) and its Jacobi update,
@@ -194,6 +199,49 @@ def local_case(q):
     q.put(res)
 
 
+TMD = dict(N=(4, 4, 1024), seed=2024, dt=0.125, A=197, qs0a=0.33, com_energy=2 * 5.2 / 0.197,
+           slices=(0, 1, 255, 510, 511, 512, 513, 770, 1022, 1023))
+TMD_FIELDS = ("U", "UOld", "E", "Jp", "Jm", "JpStat", "JmStat", "rhoL", "rhoR")
+
+
+def tmd_inputs(c):
+    """Gaussian noise for both nuclei (the reference's Gauss() stream) and uniforms (its rng() stream)."""
+    N = c["N"]
+    rng = np.random.Generator(np.random.PCG64(c["seed"]))
+    gauss = rng.standard_normal(2 * 8 * N[0] * N[1] * N[2])
+    uniforms = rng.random(400000)
+    return gauss, uniforms
+
+
+def tmd_params(c):
+    ax = c["qs0a"] * 0.197 / 0.5
+    return dict(qs0a=c["qs0a"], meff=c["qs0a"], ax_fm=ax, ay_fm=ax, az_fm=ax / (c["qs0a"] * 512),
+                com_energy=c["com_energy"])
+
+
+def slice_sums(name, v):
+    """Per-slice (ghosts included) sum of squares; links measured from the identity."""
+    if name in ("U", "UOld"):
+        v = v - np.eye(3)
+    return np.sum(np.abs(v.reshape(v.shape[0], -1)) ** 2, axis=1)
+
+
+def tmd_case(q):
+    c = TMD
+    gauss, uniforms = tmd_inputs(c)
+    ref = O.Reference(c["N"], (1.0, 1.0, 1.0))
+    pr = tmd_params(c)
+    used = ref.tmd_init(gauss, uniforms, c["dt"], c["A"], pr["qs0a"], pr["meff"], pr["ax_fm"], pr["ay_fm"],
+                        pr["az_fm"], pr["com_energy"])
+    res = {"uniforms_used": np.array(used), "gauss_check": np.array([gauss.sum(), gauss[:4].sum(), uniforms.sum()])}
+    sl = np.array(c["slices"]) + 1  # ghost slice first
+    for k in TMD_FIELDS:
+        v = ref.get(k)
+        res["sums_" + k] = slice_sums(k, v)
+        res["win_" + k] = v[sl]
+    q.put(res)
+
+
 # fixture name -> (case function, configuration stored beside it); the functions run in spawned
 # children, so they are named here rather than passed as closures
 CASES = {
@@ -203,6 +251,7 @@ CASES = {
     "mv_collision": ("mv_case", MV),
     "config_text": ("config_case", CONFIG),
     "coulomb_local": ("local_case", LOCAL),
+    "tmd_glauber": ("tmd_case", TMD),
 }
 
 

@@ -108,4 +108,5 @@ def test_invalid_arguments_return_a_status():
         assert lat.lib.glasma_coulomb_fix_algorithm(lat.h, 7, 0.5, 0, 3, 1e-15, 0, None, None) == 1
         with pytest.raises(GlasmaError, match="Fourier update only"):
             lat.coulomb_fix(0.0, 3, algorithm="los_alamos", fft_fp32=True)
-        assert len(lat.coulomb_fix(0.0, 2, algorithm="los_alamos")) == 2
+        # identity links are already in Coulomb gauge: a negative tolerance forces both iterations
+        assert len(lat.coulomb_fix(0.0, 2, tol=-1.0, algorithm="los_alamos")) == 2
