@@ -17,9 +17,6 @@
 // SUNcDynamics.cpp:181-183) regrouped by linearity of ReTr(i t^a .) and the identity
 // ReTr(i t^a W^dagger) = -ReTr(i t^a W).  Ghost slices are written by the threads that own
 // slice 0 and slice Nz-1, which is the reference's SynchronizeGhostCells after each sub-step.
-#include <cstdlib>
-
-#include "efield_tile.cuh"
 #include "leapfrog_sites.cuh"
 
 namespace glasma {
@@ -129,42 +126,9 @@ void prefer_l1(K kernel) {
   }
 }
 
-// FP32 K1 with the block's links staged in shared memory (efield_tile.cuh): bit-identical to the
-// untiled kernel, used where the lattice is wide enough for its 32 x 4 tiles.  GLASMA_K1_TILE=0 in the
-// environment selects the untiled kernel (for comparisons).
-constexpr int kTileX = 32, kTileY = 4;
-inline bool tile_k1_enabled() {
-  static const bool on = [] {
-    const char* v = std::getenv("GLASMA_K1_TILE");
-    return !(v && v[0] == '0');
-  }();
-  return on;
-}
-template <typename T>
-bool launch_tiled_efield(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, cudaStream_t stream,
-                         cudaError_t* err) {
-  if (sizeof(T) != 4 || !tile_k1_enabled() || g.nx < kTileX + 2 || g.ny < kTileY + 2) return false;
-  const size_t bytes = sizeof(cx<T>) * (tile_link_elems<kTileX, kTileY>() + StapleShare<T>::kSlots * 9 * kThreads);
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(efield_tile_kernel<T, kTileX, kTileY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bytes) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    attr = true;
-  }
-  const long long tiles = (long long)((g.nx + kTileX - 1) / kTileX) * ((g.ny + kTileY - 1) / kTileY) * g.nz;
-  efield_tile_kernel<T, kTileX, kTileY><<<(unsigned)tiles, kThreads, bytes, stream>>>(g, f, p);
-  *err = cudaGetLastError();
-  return true;
-}
-
 template <typename T>
 cudaError_t launch_efield_kernel(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, int tile_x,
                                  cudaStream_t stream) {
-  cudaError_t terr;
-  if (launch_tiled_efield<T>(g, f, p, stream, &terr)) return terr;
   if (tile_x <= 0 || tile_x > kThreads || kThreads % tile_x) tile_x = kThreads;
   const TileMap tm = TileMap::make(g.nx, g.ny, tile_x, kThreads);
   const unsigned grid = (unsigned)tm.tiles(g.nz);
