@@ -298,7 +298,8 @@ int glasma_gauss_noalloc(const double* U, const double* E, const double* JpStat,
                          int nz, double ax, double ay, double az, double a_scale, double* result, double* zprofile,
                          void* stream);
 
-/* ---- Adjoint leapfrog (FP64 lattices).  No reference counterpart.
+/* ---- Adjoint leapfrog, in the lattice's precision (FP64 or FP32 arithmetic and storage; the
+ * objective's slice sums are reduced in FP64 either way).  No reference counterpart.
  * Objective on the state after nsteps: L = N(q)/D(q), q = (e0,e1,e2,b0,b1,b2) summed over the slices
  * z in [z_begin, z_end), e_mu = cE_mu sum E_mu^2, b_i = cB_i sum 4 ReTr(1 - P_jk) with the bulk
  * observables' constants (S/OBSERVABLES/BulkObservables.cpp:22-97); N = num.q, D = den.q (D = 1 if

@@ -249,14 +249,14 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
     // Without a use for U(t+dt/2) (UOld, the z-link J transport), the two half steps are one:
     // exp(i c t.E)^2 = exp(2i c t.E), one matmul less (equal up to rounding).
     if (p.do_second && !p.save_uold && !(mu == 2 && p.do_j)) {
-      expi(T(2) * pick3(p.cU, mu), e, X);
-      mul_nn(X, u, uh);
+      link_exp(T(2) * pick3(p.cU, mu), e, X);
+      link_apply(X, u, uh);
       store_link(f.U, S, mu, s, uh);
       if (sg >= 0) store_link(f.U, S, mu, sg, uh);
       continue;
     }
-    expi(pick3(p.cU, mu), e, X);
-    mul_nn(X, u, uh);
+    link_exp(pick3(p.cU, mu), e, X);
+    link_apply(X, u, uh);
     if (p.save_uold) {
       store_link(f.UOld, S, mu, s, uh);
       if (sg >= 0) store_link(f.UOld, S, mu, sg, uh);
@@ -280,7 +280,7 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
       if (sg >= 0) store_alg(f.Jm, S, 0, sg, j);
     }
     if (p.do_second) {
-      mul_nn(X, uh, u);
+      link_apply(X, uh, u);
     } else {
       u = uh;
     }
@@ -408,21 +408,21 @@ __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>
     }
     Mat<T> X, uh;
     if (!pl.save_uold && mu != 2) {  // one exp at twice the angle, as in links_site
-      expi(T(2) * pick3(pl.cU, mu), e, X);
-      mul_nn(X, u, w);
+      link_exp(T(2) * pick3(pl.cU, mu), e, X);
+      link_apply(X, u, w);
       if (!dry) {
         store_link(out.U, S, mu, s, w);
         if (sg >= 0) store_link(out.U, S, mu, sg, w);
       }
       continue;
     }
-    expi(pick3(pl.cU, mu), e, X);
-    mul_nn(X, u, uh);
+    link_exp(pick3(pl.cU, mu), e, X);
+    link_apply(X, u, uh);
     if (pl.save_uold && !dry) {
       store_link(in.UOld, S, mu, s, uh);
       if (sg >= 0) store_link(in.UOld, S, mu, sg, uh);
     }
-    mul_nn(X, uh, w);
+    link_apply(X, uh, w);
     if (!dry) {
       store_link(out.U, S, mu, s, w);
       if (sg >= 0) store_link(out.U, S, mu, sg, w);

@@ -12,9 +12,12 @@
 // Every reduction is two-pass and deterministic: a fixed grid writes FP64 block partials
 // (warp shuffles, then shared memory), a one-block pass sums them in a fixed order.
 // Site arithmetic runs in FP64, except the magnetic term of the bulk energy on FP32 lattices,
-// which uses the identity (exact for any matrices)
+// which uses the identity
 //   3 - ReTr(a b c^d d^d) = 1/2 ||A - B||^2 - 1/2 (n(a) + n(b) + n(c) + n(d)),
-//   A = a b, B = d c, n(u) = ||u||_F^2 - 3  (zero for unitary u):
+//   A = a b, B = d c, n(u) = ||u||_F^2 - 3  (zero for unitary u),
+// exact with n(A) + n(B) in place of the four link terms and equal to it to first order in the links'
+// departure from unitarity (~1e-7 for FP32-rounded links, so the difference is ~1e-14); the link
+// terms are preferred because the products' own FP32 rounding never enters them:
 // A, B and ||A - B||^2 are formed in FP32, whose rounding then costs about 1e-7 ||A - B|| per
 // plaquette instead of 1e-7 (no cancellation against 3, so weak fields keep their digits), and the
 // norm terms are summed in FP64 per link (each link's n counted for the plaquettes it belongs to).

@@ -311,9 +311,10 @@ struct Trig<float> {
   static __device__ __forceinline__ float taylor_c1() { return 1e-3f; }
 };
 
-// X = exp(i c t^a al^a), Cayley-Hamilton form exp(iQ) = f0 + f1 Q + f2 Q^2.
-template <typename T>
-__device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
+// X = exp(i c t^a al^a), Cayley-Hamilton form exp(iQ) = f0 + f1 Q + f2 Q^2.  kMinusOne: X - 1
+// instead, with f0 - 1 formed directly (expi_m1 below).
+template <typename T, bool kMinusOne = false>
+__device__ __forceinline__ void expi_impl(T c, const Alg<T>& al, Mat<T>& X) {
   Alg<T> sc;
 #pragma unroll
   for (int a = 0; a < 8; a++) sc.a[a] = c * al.a[a];
@@ -336,7 +337,7 @@ __device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
   c0 *= T(1) / T(3);
   cx<T> f0, f1, f2;
   if (c1 < Trig<T>::taylor_c1()) {
-    f0 = mk<T>(T(1) - c0 * c0 / T(720), -c0 / T(6) + c1 * c0 / T(120));
+    f0 = mk<T>(kMinusOne ? -(c0 * c0 / T(720)) : T(1) - c0 * c0 / T(720), -c0 / T(6) + c1 * c0 / T(120));
     f1 = mk<T>(c0 / T(24) - c0 * c1 / T(360), T(1) - c1 / T(6) + c1 * c1 / T(120));
     f2 = mk<T>(T(-0.5) + c1 / T(24) - c1 * c1 / T(720), c0 / T(120));
   } else {
@@ -385,6 +386,7 @@ __device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
       f1.re = -f1.re;
       f2.im = -f2.im;
     }
+    if (kMinusOne) f0.re -= T(1);
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) {
@@ -399,6 +401,68 @@ __device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
   X.e[4].im += f0.im;
   X.e[8].re += f0.re;
   X.e[8].im += f0.im;
+}
+template <typename T>
+__device__ __forceinline__ void expi(T c, const Alg<T>& al, Mat<T>& X) {
+  expi_impl<T, false>(c, al, X);
+}
+// exp(i c t.al) - 1.  Near the identity the diagonal of exp(iQ) is 1 - (Q^2)_ii/2 + ..., and in FP32 a
+// deviation below ~3e-8 vanishes when it is added to 1, every step the same way: the links' norms then
+// grow by ~tr Q^2 per step (measured: unitarity defect 2.9e-5 after 400 steps of an MV collision).
+// Formed as X - 1 the small terms keep their relative precision; the link update U + (X - 1) U rounds
+// once, at a point that moves from step to step, so they survive on average.
+template <typename T>
+__device__ __forceinline__ void expi_m1(T c, const Alg<T>& al, Mat<T>& Xm1) {
+  expi_impl<T, true>(c, al, Xm1);
+}
+// a + b rounded stochastically: to the FP32 neighbour of the exact sum with probability equal to the
+// fraction of the gap, so the rounding is unbiased.  The exact residual comes from TwoSum; the random
+// number is a hash of the operands' bits (they change from step to step, so it needs no counter and
+// gives the same bits in every launch path).
+__device__ __forceinline__ float add_stochastic(float a, float b, unsigned salt) {
+  const float s = a + b, bb = s - a;
+  const float r = (a - (s - bb)) + (b - bb);
+  if (r == 0.f) return s;
+  const float t = nextafterf(s, r > 0.f ? 3.0e38f : -3.0e38f);
+  const float p = fabsf(r / (t - s));
+  unsigned h = (__float_as_uint(a) * 0x9E3779B1u) ^ (__float_as_uint(b) * 0x85EBCA77u) ^ salt;
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  h *= 0x297A2D39u;
+  h ^= h >> 15;
+  return (float)(h >> 8) * (1.f / 16777216.f) < p ? t : s;
+}
+// out = (1 + Xm1) u.  In FP32 the real parts of the diagonal are added with stochastic rounding: near
+// the identity they receive only the second-order -(Q^2)_ii/2 per step (the first-order i Q u is
+// imaginary there), which round-to-nearest would drop in the same direction every step, growing the
+// links' norms between reunitarisations.
+template <typename T>
+__device__ __forceinline__ void mul_near_identity(const Mat<T>& Xm1, const Mat<T>& u, Mat<T>& out) {
+  mul_nn(Xm1, u, out);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    if (sizeof(T) == 4 && (k == 0 || k == 4 || k == 8))
+      out.e[k].re = (T)add_stochastic((float)u.e[k].re, (float)out.e[k].re, (unsigned)k);
+    else
+      out.e[k].re += u.e[k].re;
+    out.e[k].im += u.e[k].im;
+  }
+}
+// The link update's exponential and its application: FP32 keeps X - 1 (expi_m1), FP64 forms X.
+template <typename T>
+__device__ __forceinline__ void link_exp(T c, const Alg<T>& al, Mat<T>& X) {
+  if (sizeof(T) == 4)
+    expi_m1(c, al, X);
+  else
+    expi(c, al, X);
+}
+template <typename T>
+__device__ __forceinline__ void link_apply(const Mat<T>& X, const Mat<T>& u, Mat<T>& out) {
+  if (sizeof(T) == 4)
+    mul_near_identity(X, u, out);
+  else
+    mul_nn(X, u, out);
 }
 
 // ||V V^dagger - 1||_F  (S/SUNc/SU3/GroupOperations.cpp:337-349)
@@ -489,37 +553,58 @@ __device__ __forceinline__ void reunitarize_newton(Mat<T>& V) {
   }
 }
 
-// Same projection for FP32 links in FP32 arithmetic: Newton-Schulz steps U <- U (3 - U^d U) / 2, which
-// converge quadratically to the same polar factor without an inverse (U = W (1 + e), e Hermitian,
-// becomes W (1 - e^2)), then the determinant's phase is divided out.  Links that drifted far from
-// SU(3) (||1 - U^d U|| > 0.25, outside the fast-convergence region) take the FP64 Newton path.
+// Same projection for FP32 links, kept unbiased.  A link within ~1e-6 of SU(3) is U = W (1 + e) with
+// W the projection and e Hermitian and small; U W-ward is U (1 - e) to first order, and e = (U^d U - 1)/2.
+// Everything small is formed as a small number: the diagonal of U^d U - 1 exactly (error-free FMA
+// products, then the exact subtraction of 1), its off-diagonal in FP32 (no cancellation against 1
+// there), the determinant's phase theta from an FP32 determinant, and the link is corrected as
+// U + U M, M = -e - i theta/3, with one rounding.  Forming 1.5 - H/2 and U (1.5 - H/2) in FP32 instead
+// (plain Newton-Schulz) rounds the ~1e-8 corrections at 1 and was measured to shrink the links' norms
+// by 2e-8 on average, raising a weak-field plaquette energy by 1.8e-3.  Links that drifted far from
+// SU(3) (||U^d U - 1|| > 1e-4) take the FP64 Newton path.
+__device__ __forceinline__ float two_prod_sq_err(float a) { return fmaf(a, a, -a * a); }
 __device__ __forceinline__ void reunitarize_f32(Mat<float>& U) {
-  Mat<float> H, K, X;
-  mul_dn(U, U, H);
-  float dev = 0.f;
+  // e = (U^d U - 1)/2: the diagonal from exact squares, summed with their error terms
+  float d[3];
 #pragma unroll
-  for (int k = 0; k < 9; k++) {
-    const float d = H.e[k].re - ((k % 4 == 0) ? 1.f : 0.f);
-    dev = fmaf(d, d, fmaf(H.e[k].im, H.e[k].im, dev));
+  for (int j = 0; j < 3; j++) {
+    float hi = 0.f, lo = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const cx<float> u = U.e[k + 3 * j];
+      const float pr = u.re * u.re, pi = u.im * u.im;
+      lo += two_prod_sq_err(u.re) + two_prod_sq_err(u.im);
+      // TwoSum of hi + pr and of that + pi
+      float s = hi + pr, bb = s - hi;
+      lo += (hi - (s - bb)) + (pr - bb);
+      hi = s;
+      s = hi + pi;
+      bb = s - hi;
+      lo += (hi - (s - bb)) + (pi - bb);
+      hi = s;
+    }
+    d[j] = (hi - 1.f) + lo;  // hi - 1 is exact for hi in [0.5, 2]
   }
-  if (!(dev <= 0.0625f)) {
+  cx<float> h01 = mk<float>(0, 0), h02 = mk<float>(0, 0), h12 = mk<float>(0, 0);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    cfma_cn(h01, U.e[k], U.e[k + 3]);
+    cfma_cn(h02, U.e[k], U.e[k + 6]);
+    cfma_cn(h12, U.e[k + 3], U.e[k + 6]);
+  }
+  const float dev = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] +
+                    2.f * (h01.re * h01.re + h01.im * h01.im + h02.re * h02.re + h02.im * h02.im +
+                           h12.re * h12.re + h12.im * h12.im);
+  // ||U^d U - 1||^2 <= 1e-8: the first-order correction leaves |e|^2 < 3e-9, below FP32 rounding
+  if (!(dev <= 1e-8f)) {
     reunitarize_newton(U);
     return;
   }
-#pragma unroll 1
-  for (int it = 0; it < 2; it++) {
-    if (it > 0) mul_dn(U, U, H);
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      K.e[k].re = ((k % 4 == 0) ? 1.5f : 0.f) - 0.5f * H.e[k].re;
-      K.e[k].im = -0.5f * H.e[k].im;
-    }
-    mul_nn(U, K, X);
-    U = X;
-  }
-  cx<float> det = mk<float>(0, 0);
+  // the determinant's phase (~1e-7 for a link this close to SU(3)); its FP32 rounding is random in sign,
+  // so the correction it drives is unbiased
+  float theta;
   {
-    cx<float> c0 = mk<float>(0, 0), c1 = mk<float>(0, 0), c2 = mk<float>(0, 0);
+    cx<float> c0 = mk<float>(0, 0), c1 = mk<float>(0, 0), c2 = mk<float>(0, 0), det = mk<float>(0, 0);
     cfma(c0, U.e[4], U.e[8]);
     cfma(c0, mk<float>(-U.e[7].re, -U.e[7].im), U.e[5]);
     cfma(c1, U.e[5], U.e[6]);
@@ -529,15 +614,25 @@ __device__ __forceinline__ void reunitarize_f32(Mat<float>& U) {
     cfma(det, U.e[0], c0);
     cfma(det, U.e[1], c1);
     cfma(det, U.e[2], c2);
+    theta = atan2f(det.im, det.re);
   }
-  float sp, cp;
-  sincosf(-atan2f(det.im, det.re) * (1.f / 3.f), &sp, &cp);
-  const cx<float> ph = mk<float>(cp, sp);
+  // M = -e - i theta/3 (e Hermitian: e_ij = h_ij / 2 off the diagonal, d_j / 2 on it)
+  Mat<float> M, C;
+  const float t3 = theta * (1.f / 3.f);
+  M.e[0] = mk<float>(-0.5f * d[0], -t3);
+  M.e[4] = mk<float>(-0.5f * d[1], -t3);
+  M.e[8] = mk<float>(-0.5f * d[2], -t3);
+  M.e[3] = mk<float>(-0.5f * h01.re, -0.5f * h01.im);  // (0,1)
+  M.e[6] = mk<float>(-0.5f * h02.re, -0.5f * h02.im);  // (0,2)
+  M.e[7] = mk<float>(-0.5f * h12.re, -0.5f * h12.im);  // (1,2)
+  M.e[1] = mk<float>(M.e[3].re, -M.e[3].im);
+  M.e[2] = mk<float>(M.e[6].re, -M.e[6].im);
+  M.e[5] = mk<float>(M.e[7].re, -M.e[7].im);
+  mul_nn(U, M, C);
 #pragma unroll
   for (int k = 0; k < 9; k++) {
-    cx<float> w = mk<float>(0, 0);
-    cfma(w, U.e[k], ph);
-    U.e[k] = w;
+    U.e[k].re += C.e[k].re;
+    U.e[k].im += C.e[k].im;
   }
 }
 

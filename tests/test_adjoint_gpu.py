@@ -79,3 +79,43 @@ def test_checkpoint_spacing_does_not_change_gradient():
         scale = np.max(np.abs(out[0][k]))
         assert np.max(np.abs(out[1][k] - out[0][k])) <= 1e-10 * scale, k
         assert np.max(np.abs(out[2][k] - out[0][k])) <= 1e-9 * scale, k
+
+
+def _rel_l2(a, b):
+    return float(np.linalg.norm(a[1:-1] - b[1:-1]) / np.linalg.norm(b[1:-1]))
+
+
+def test_fp32_adjoint_follows_the_fp64_adjoint():
+    """On an FP32 lattice the adjoint runs in FP32 end to end (forward, time-reversed reconstruction,
+    vector-Jacobian products).  Started from the same fields (rounded to FP32 for both), its objective
+    and gradients agree with the FP64 adjoint's to FP32 accuracy."""
+    f0 = initial()
+    f32 = {k: (v.astype(np.complex64).astype(np.complex128) if np.iscomplexobj(v)
+               else v.astype(np.float32).astype(np.float64)) for k, v in f0.items()}
+    res = {}
+    for prec in ("fp64", "fp32"):
+        with Lattice(N, A, precision=prec) as lat:
+            lat.upload_fields(f32)
+            res[prec] = lat.adjoint(DT, STEPS, Z0, Z1, Lattice.PL_OVER_PT, checkpoint_every=3)
+    (l64, g64), (l32, g32) = res["fp64"], res["fp32"]
+    assert abs(l32 - l64) <= 1e-5 * abs(l64)
+    errs = {k: _rel_l2(g32[k], g64[k]) for k in GRAD_FIELDS}
+    assert all(e < 2e-4 for e in errs.values()), errs
+
+
+@pytest.mark.parametrize("link_amp", [0.25, 1e-3])
+def test_fp32_objective_matches_fp64_measurement(link_amp):
+    """The objective of the same fields on both lattices.  Weak fields (links within 1e-3 of the
+    identity, as in the dilute central region of a late collision) are the hard case for FP32: the
+    plaquette term is formed without cancellation against 3 (the bulk energy's identity)."""
+    f0 = O.random_fields(N, 555, link_amp=link_amp, e_amp=0.3 * link_amp, j_amp=0.1)
+    f32 = {k: (v.astype(np.complex64).astype(np.complex128) if np.iscomplexobj(v)
+               else v.astype(np.float32).astype(np.float64)) for k, v in f0.items()}
+    vals = []
+    for prec in ("fp64", "fp32"):
+        with Lattice(N, A, precision=prec) as lat:
+            lat.upload_fields(f32)
+            vals.append(lat.objective(Z0, Z1, Lattice.PL_OVER_PT))
+    # weak fields: the plaquette differences A - B (~1e-3) carry FP32 rounding of ~1e-7
+    tol = 1e-5 if link_amp > 0.1 else 1e-3
+    assert abs(vals[1] - vals[0]) <= tol * abs(vals[0]), vals
