@@ -306,17 +306,27 @@ __global__ void split_filter_kernel(double2* X, double2* Y, L n, int nx, int ny,
 
 // Path-ordered Wilson lines (SetNewWilsonLines, TMDbased.cpp:176-221 / CollidingObjects.cpp:180-226):
 // per transverse site W <- exp(i c t.Phi(z)) W over the slices in order ('R' from z = 0 up with
-// c = +1/sqrt2, 'L' from the top slice down with c = -1/sqrt2), V(z) = W.  Phi = real part of P[a][site];
-// V[k][site] complex, k = i + 3j.  One thread per transverse site walks all slices, so the launch uses
-// small blocks (64 threads) to spread the Nx Ny threads over every SM.
-__global__ void path_order_kernel(const double2* P, int nx, int ny, int nz, int up, double c, double2* V) {
+// c = +1/sqrt2, 'L' from the top slice down with c = -1/sqrt2), V(z) = W; Phi = real part of P[a][site],
+// V[k][site] complex, k = i + 3j.  A walk over all slices per transverse site leaves the GPU nearly idle
+// (one thread per site), so the product is a chunked scan: the ordered slices are cut into chunks of
+// kPathChunk; per (site, chunk) the exponentials are
+// stored in V and their ordered product in `prod` (phase 1); per site a prefix over the chunks turns
+// `prod` into each chunk's incoming product (phase 2); per (site, chunk) the incoming product is carried
+// through the stored exponentials into V (phase 3).  prod[q][chunk][col], nch chunks.
+constexpr int kPathChunk = 32;
+__global__ void path_chunk_kernel(const double2* P, int nx, int ny, int nz, int up, double c, double2* V,
+                                  double2* prod) {
   const L plane = (L)nx * ny, vol = plane * nz;
-  const L col = (L)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= plane) return;
+  const int nch = (nz + kPathChunk - 1) / kPathChunk;
+  const L i = (L)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= plane * nch) return;
+  const int ch = (int)(i / plane);
+  const L col = i - (L)ch * plane;
   M3 W;
   set_zero(W);
   W.e[0].re = W.e[4].re = W.e[8].re = 1.0;
-  for (int k = 0; k < nz; k++) {
+  const int k1 = min(nz, (ch + 1) * kPathChunk);
+  for (int k = ch * kPathChunk; k < k1; k++) {
     const int z = up ? k : nz - 1 - k;
     const L site = col + plane * z;
     A8 phi;
@@ -324,6 +334,55 @@ __global__ void path_order_kernel(const double2* P, int nx, int ny, int nz, int 
     for (int a = 0; a < 8; a++) phi.a[a] = P[(L)a * vol + site].x;
     M3 X, Wn;
     expi(c, phi, X);
+#pragma unroll
+    for (int q = 0; q < 9; q++) V[(L)q * vol + site] = make_double2(X.e[q].re, X.e[q].im);
+    mul_nn(X, W, Wn);
+    W = Wn;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) prod[((L)q * nch + ch) * plane + col] = make_double2(W.e[q].re, W.e[q].im);
+}
+__global__ void path_prefix_kernel(double2* prod, L plane, int nch) {
+  const L col = (L)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= plane) return;
+  M3 In;
+  set_zero(In);
+  In.e[0].re = In.e[4].re = In.e[8].re = 1.0;
+  for (int ch = 0; ch < nch; ch++) {
+    M3 Pc, Wn;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      double2* p = prod + ((L)q * nch + ch) * plane + col;
+      Pc.e[q] = mk<double>(p->x, p->y);
+      *p = make_double2(In.e[q].re, In.e[q].im);
+    }
+    mul_nn(Pc, In, Wn);
+    In = Wn;
+  }
+}
+__global__ void path_apply_kernel(int nx, int ny, int nz, int up, const double2* prod, double2* V) {
+  const L plane = (L)nx * ny, vol = plane * nz;
+  const int nch = (nz + kPathChunk - 1) / kPathChunk;
+  const L i = (L)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= plane * nch) return;
+  const int ch = (int)(i / plane);
+  const L col = i - (L)ch * plane;
+  M3 W;
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const double2 v = prod[((L)q * nch + ch) * plane + col];
+    W.e[q] = mk<double>(v.x, v.y);
+  }
+  const int k1 = min(nz, (ch + 1) * kPathChunk);
+  for (int k = ch * kPathChunk; k < k1; k++) {
+    const int z = up ? k : nz - 1 - k;
+    const L site = col + plane * z;
+    M3 X, Wn;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      const double2 v = V[(L)q * vol + site];
+      X.e[q] = mk<double>(v.x, v.y);
+    }
     mul_nn(X, W, Wn);
     W = Wn;
 #pragma unroll
@@ -618,8 +677,8 @@ extern "C" const char* glasma_mv_last_error(void) { return g_mv_error.c_str(); }
 //   field (CollidingObjects::SetWilsonLinesForFirstStep), U from V', E = ILog(U UOld^d)/coff, JStat
 //   from the Gauss law, J from JStat by the z filter.
 // Unlike the MV state the density differs from slice to slice, so every slice gets its own Poisson
-// field: the 2D transforms run batched over all 8 Nz planes at once and only the path ordering walks
-// the slices, one thread per transverse site.
+// field: the 2D transforms run batched over all 8 Nz planes at once, and the path ordering is a
+// chunked scan over the slices.
 namespace {
 const double kTmdBG = 4.0 * 0.197 * 0.197;  // nucleon width^2 in fm^2 (GBWSampling.cpp:4)
 
@@ -665,6 +724,17 @@ static int tmd_impl(glasma_lattice* h, const double* const noise[2], const doubl
     return e;
   };
   auto fftz = [&](double2* buf, int inverse) { return fft_lines(buf, nz, plane, 8 * vol, inverse, tw[2], st); };
+  // path-ordered Wilson lines: the chunked scan (small per-chunk products keep every SM busy)
+  const int nch = (nz + kPathChunk - 1) / kPathChunk;
+  Dev chunk;
+  if (!chunk.alloc(sizeof(double2) * 9 * (size_t)nch * plane)) return mvfail(GLASMA_ERR_OUT_OF_MEMORY, "path chunks");
+  auto path_scan = [&](const double2* Pin, int up, double c, double2* Vout) {
+    double2* pr = static_cast<double2*>(chunk.p);
+    const L n = plane * nch;
+    path_chunk_kernel<<<g1(n), 256, 0, st>>>(Pin, nx, ny, nz, up, c, Vout, pr);
+    path_prefix_kernel<<<(unsigned)((plane + 63) / 64), 64, 0, st>>>(pr, plane, nch);
+    path_apply_kernel<<<g1(n), 256, 0, st>>>(nx, ny, nz, up, pr, Vout);
+  };
   // every field starts from Lattice::Init's state: identity links, zero E and currents
   for (int f : {GLASMA_FIELD_U, GLASMA_FIELD_UOLD})
     identity_links_kernel<T><<<g1(27 * g.S), 256, 0, st>>>(static_cast<cx<T>*>(h->f[f]), g.S);
@@ -730,7 +800,7 @@ static int tmd_impl(glasma_lattice* h, const double* const noise[2], const doubl
     }
     const int up = D == 'R' ? 1 : 0;
     const double c = D == 'R' ? inv_sqrt2 : -inv_sqrt2;
-    path_order_kernel<<<(unsigned)((plane + 63) / 64), 64, 0, st>>>(Y, nx, ny, nz, up, c, V);
+    path_scan(Y, up, c, V);
     // ---- SingleSheet: the density shifted by dt, its per-slice Poisson field, V'
     {
       std::vector<double2> ph(nz);
@@ -752,7 +822,7 @@ static int tmd_impl(glasma_lattice* h, const double* const noise[2], const doubl
     filter2d_kernel<<<g1(8 * vol), 256, 0, st>>>(X, 8 * vol, nx, ny, g.a[0], g.a[1], 1.0, 0.0, 1);
     if (e == cudaSuccess) e = fft2(X, 1);
     if (e != cudaSuccess) return mvfail(GLASMA_ERR_CUDA, std::string("TMD first step: ") + cudaGetErrorString(e));
-    path_order_kernel<<<(unsigned)((plane + 63) / 64), 64, 0, st>>>(X, nx, ny, nz, up, c, Vp);
+    path_scan(X, up, c, Vp);
     const double coff0 = -p.dt * g.a[0] * g.a[0] / a3, coff1 = -p.dt * g.a[1] * g.a[1] / a3;
     sheet_links_v_kernel<T><<<g1(plane * (zhi - zlo + 1)), 256, 0, st>>>(
         g, V, Vp, zlo, zhi, coff0, coff1, static_cast<cx<T>*>(h->f[GLASMA_FIELD_U]),
