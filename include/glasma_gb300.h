@@ -100,6 +100,19 @@ int glasma_upload(glasma_lattice* h, int field, const double* host);
 int glasma_download(glasma_lattice* h, int field, double* host);
 /* Same, from / to a device buffer holding the host layout. */
 int glasma_upload_device(glasma_lattice* h, int field, const double* device_aos);
+/* Uploads that overlap the handle's kernels: glasma_upload_begin starts copying `host` (reference
+ * layout, as for glasma_upload) into a staging area on the handle's own transfer stream and returns;
+ * glasma_upload_finish orders the handle's stream after every begun copy and converts them into the
+ * fields (on that stream, without waiting on the host).  Kernels enqueued before finish still see the
+ * old fields, so the next step's inputs can travel while the current step runs:
+ *   begin(inputs 0); finish(); for k: { begin(inputs k+1); step(); read result; finish(); }
+ * The host buffers must stay unchanged until the handle's stream has passed finish's conversion (after
+ * any synchronising call: an observable, a download, glasma_synchronize); page-locked buffers let the
+ * copy run without the CPU.  A begin waits on the device for the previous finish's conversion to have
+ * read the staging.
+ * No reference counterpart (the reference's fields live on the host). */
+int glasma_upload_begin(glasma_lattice* h, int field, const double* host);
+int glasma_upload_finish(glasma_lattice* h);
 int glasma_download_device(glasma_lattice* h, int field, double* device_aos);
 
 /* nsteps x Dynamics::SUNc::Update (S/DYNAMICS/SUNcDynamics.cpp:353-378) with time step dt.

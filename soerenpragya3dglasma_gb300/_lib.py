@@ -62,6 +62,8 @@ SIGNATURES = [
     ("glasma_emt_map", ctypes.c_int, [_H, _D]),
     ("glasma_pressure_anisotropy", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _D, _D, _D]),
     ("glasma_reunitarize", ctypes.c_int, [_H]),
+    ("glasma_upload_begin", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p]),
+    ("glasma_upload_finish", ctypes.c_int, [_H]),
     ("glasma_coulomb_fix", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
     ("glasma_coulomb_fix_algorithm", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong,
                                                     ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),

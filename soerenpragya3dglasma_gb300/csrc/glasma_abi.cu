@@ -349,6 +349,12 @@ int glasma_destroy(glasma_lattice* h) {
   }
   if (h->staging) cudaFree(h->staging);
   if (h->scratch) cudaFree(h->scratch);
+  if (h->xfer_stream) cudaStreamSynchronize(h->xfer_stream);
+  for (int i = 0; i < 10; i++)
+    if (h->stage_f[i]) cudaFree(h->stage_f[i]);
+  if (h->xfer_done) cudaEventDestroy(h->xfer_done);
+  if (h->stage_free) cudaEventDestroy(h->stage_free);
+  if (h->xfer_stream) cudaStreamDestroy(h->xfer_stream);
   glasma::gaugefix_destroy(h->gf);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
@@ -448,6 +454,54 @@ static int download_common(glasma_lattice* h, int field, double* dst, cudaMemcpy
   if (e != cudaSuccess) return cuda_fail(e, "soa_to_aos");
   GLASMA_CUDA(cudaMemcpyAsync(dst, h->staging, bytes, kind, h->stream), "download copy");
   GLASMA_CUDA(cudaStreamSynchronize(h->stream), "download sync");
+  return GLASMA_OK;
+}
+
+int glasma_upload_begin(glasma_lattice* h, int field, const double* host) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!valid_field(field)) return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown field");
+  if (!host) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null source");
+  int st = ensure_field(h, field);
+  if (st) return st;
+  if (!h->xfer_stream) {
+    GLASMA_CUDA(cudaStreamCreateWithFlags(&h->xfer_stream, cudaStreamNonBlocking), "transfer stream");
+    GLASMA_CUDA(cudaEventCreateWithFlags(&h->xfer_done, cudaEventDisableTiming), "transfer event");
+    GLASMA_CUDA(cudaEventCreateWithFlags(&h->stage_free, cudaEventDisableTiming), "staging event");
+  }
+  const size_t bytes = (size_t)h->g.S * host_doubles_per_site(field) * sizeof(double);
+  if (!h->stage_f[field]) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GLASMA_ERR_OUT_OF_MEMORY, std::string("cudaMalloc upload staging: ") + cudaGetErrorString(e));
+    }
+    h->stage_f[field] = static_cast<double*>(p);
+  }
+  // the previous finish's conversion must have read this staging area before it is overwritten (an
+  // event never recorded is complete)
+  GLASMA_CUDA(cudaStreamWaitEvent(h->xfer_stream, h->stage_free, 0), "wait for staging");
+  GLASMA_CUDA(cudaMemcpyAsync(h->stage_f[field], host, bytes, cudaMemcpyHostToDevice, h->xfer_stream),
+              "upload copy");
+  h->pending |= 1u << field;
+  return GLASMA_OK;
+}
+
+int glasma_upload_finish(glasma_lattice* h) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!h->pending) return GLASMA_OK;
+  GLASMA_CUDA(cudaEventRecord(h->xfer_done, h->xfer_stream), "record transfers");
+  GLASMA_CUDA(cudaStreamWaitEvent(h->stream, h->xfer_done, 0), "wait for transfers");
+  for (int f = 0; f < 10; f++) {
+    if (!(h->pending & (1u << f))) continue;
+    const int P = host_doubles_per_site(f);
+    cudaError_t e = h->precision == GLASMA_FP64
+                        ? glasma::launch_aos_to_soa<double>(h->stage_f[f], static_cast<double*>(h->f[f]), h->g.S, P, h->stream)
+                        : glasma::launch_aos_to_soa<float>(h->stage_f[f], static_cast<float*>(h->f[f]), h->g.S, P, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "aos_to_soa of staged upload");
+  }
+  GLASMA_CUDA(cudaEventRecord(h->stage_free, h->stream), "record staging read");
+  h->pending = 0;
   return GLASMA_OK;
 }
 

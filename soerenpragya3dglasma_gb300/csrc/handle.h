@@ -27,6 +27,12 @@ struct glasma_lattice {
   int step_method;    // GLASMA_STEP_ONE_PASS / GLASMA_STEP_TWO_PASS
   int last_method;    // method the last glasma_step used
   unsigned long long swaps;  // buffer swaps so far (batched launches rebuild their tables on change)
+  // asynchronous uploads (glasma_upload_begin / glasma_upload_finish)
+  cudaStream_t xfer_stream;  // copies host -> staging, overlapping the handle's kernels (first use)
+  cudaEvent_t xfer_done;     // recorded on xfer_stream at finish: every begun copy has landed
+  cudaEvent_t stage_free;    // recorded on the handle's stream at finish: the staging has been read
+  double* stage_f[10];       // per-field staging areas in the reference's host layout
+  unsigned pending;          // fields begun and not yet finished (bit per glasma_field)
 };
 
 namespace glasma {

@@ -129,13 +129,17 @@ __device__ __forceinline__ void decode_vol(const Geometry& g, long long idx, int
   y = (int)(r - (long long)z * g.ny);
 }
 
-// C = A B C^d D^d as the reference's UUDD grouping
-__device__ __forceinline__ void plaq_uudd(const Mat<double>& a, const Mat<double>& b, const Mat<double>& c,
-                                          const Mat<double>& d, Mat<double>& out) {
-  Mat<double> t1, t2;
-  mul_nn(a, b, t1);
-  mul_dd(c, d, t2);
-  mul_nn(t1, t2, out);
+// Re tr(a b c^d d^d) = Re sum_ij (a b)_ij conj((d c)_ij): two products and a dot product instead of
+// the three products of the full plaquette (the bulk energy needs only its trace)
+__device__ __forceinline__ double retr_plaq(const Mat<double>& a, const Mat<double>& b, const Mat<double>& c,
+                                           const Mat<double>& d) {
+  Mat<double> A, B;
+  mul_nn(a, b, A);
+  mul_nn(d, c, B);
+  double t = 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) t = fma(A.e[k].re, B.e[k].re, fma(A.e[k].im, B.e[k].im, t));
+  return t;
 }
 
 // ||A - B||^2 of the plaquette a b (d c)^d in the (j,k) plane, A = U_j(x) U_k(x+j), B = U_k(x) U_j(x+k), FP32
@@ -195,28 +199,25 @@ __global__ void __launch_bounds__(kRedThreads) bulk_kernel(Geometry g, FieldPtrs
       v[0] += 2.0 * (double)plaq_sqdiff_f(f.U, S, 1, 2, s, syp, szp) - 2.0 * (2.0 * nz + wz * ny + gy);
       v[1] += 2.0 * (double)plaq_sqdiff_f(f.U, S, 2, 0, s, szp, sxp) - 2.0 * (2.0 * nz + wz * nx + gx);
     } else {
-      Mat<double> a, b, c, d, P;
+      Mat<double> a, b, c, d;
       // Uxy = U_x(x) U_y(x+x) U_x^d(x+y) U_y^d(x)
       load_link_d(f.U, S, 0, s, a);
       load_link_d(f.U, S, 1, sxp, b);
       load_link_d(f.U, S, 0, syp, c);
       load_link_d(f.U, S, 1, s, d);
-      plaq_uudd(a, b, c, d, P);
-      v[2] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
+      v[2] += 4.0 * (3.0 - retr_plaq(a, b, c, d));
       // Uyz = U_y(x) U_z(x+y) U_y^d(x+z) U_z^d(x)
       load_link_d(f.U, S, 1, s, a);
       load_link_d(f.U, S, 2, syp, b);
       load_link_d(f.U, S, 1, szp, c);
       load_link_d(f.U, S, 2, s, d);
-      plaq_uudd(a, b, c, d, P);
-      v[0] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
+      v[0] += 4.0 * (3.0 - retr_plaq(a, b, c, d));
       // Uzx = U_z(x) U_x(x+z) U_z^d(x+x) U_x^d(x)
       load_link_d(f.U, S, 2, s, a);
       load_link_d(f.U, S, 0, szp, b);
       load_link_d(f.U, S, 2, sxp, c);
       load_link_d(f.U, S, 0, s, d);
-      plaq_uudd(a, b, c, d, P);
-      v[1] += 4.0 * (3.0 - P.e[0].re - P.e[4].re - P.e[8].re);
+      v[1] += 4.0 * (3.0 - retr_plaq(a, b, c, d));
     }
     for (int mu = 0; mu < 3; mu++) {
       Alg<double> e;

@@ -191,6 +191,20 @@ class Lattice:
         check(self.lib.glasma_download(self.h, _lib.FIELDS[name], _address(out, self.field_doubles(name))))
         return out
 
+    def upload_begin(self, name, arr):
+        """Start copying a host field on the handle's transfer stream (glasma_upload_begin); the array
+        is kept alive here until upload_finish."""
+        check(self.lib.glasma_upload_begin(self.h, _lib.FIELDS[name], _address(arr, self.field_doubles(name))))
+        self._in_flight = getattr(self, "_in_flight", []) + [arr]
+
+    def upload_finish(self):
+        """Order the handle's stream after the begun copies and convert them into the fields.  The copies
+        may still be reading the host arrays when this returns: they are kept alive until the next
+        upload_finish (by then a synchronising call has passed in any sensible loop)."""
+        check(self.lib.glasma_upload_finish(self.h))
+        self._finished = getattr(self, "_in_flight", [])
+        self._in_flight = []
+
     def upload_device(self, name, dev_ptr):
         check(self.lib.glasma_upload_device(self.h, _lib.FIELDS[name], ctypes.c_void_p(int(dev_ptr))))
 
