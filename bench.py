@@ -38,12 +38,15 @@ SEED = 1002
 LINK_AMP, E_AMP, J_AMP = 0.3, 0.1, 0.02
 INPUT_FIELDS = ("U", "E", "Jp", "Jm", "JpStat", "JmStat")
 # compulsory HBM bytes per site of each kernel (read + write of what it must touch once)
+# ("fp32_l12": FP32 with 12-real links, rows 0 and 1 of each link read and written, 144 B per site)
 KERNEL_BYTES = {
-    "efield_jstat": {"fp64": 432 + 2 * 192 + 128 + 2 * 128, "fp32": 216 + 2 * 96 + 64 + 2 * 64},
-    "links_j": {"fp64": 192 + 2 * 432 + 128 + 2 * 128, "fp32": 96 + 2 * 216 + 64 + 2 * 64},
-    "fused_step": {"fp64": 1760, "fp32": 880},  # one pass: every per-site state array read and written once
+    "efield_jstat": {"fp64": 432 + 2 * 192 + 128 + 2 * 128, "fp32": 216 + 2 * 96 + 64 + 2 * 64,
+                     "fp32_l12": 144 + 2 * 96 + 64 + 2 * 64},
+    "links_j": {"fp64": 192 + 2 * 432 + 128 + 2 * 128, "fp32": 96 + 2 * 216 + 64 + 2 * 64,
+                "fp32_l12": 96 + 2 * 144 + 64 + 2 * 64},
+    "fused_step": {"fp64": 1760, "fp32": 880, "fp32_l12": 736},  # one pass: every per-site array read and written once
 }
-STEP_BYTES = {"fp64": 1760, "fp32": 880}  # every per-site state array read and written once
+STEP_BYTES = {"fp64": 1760, "fp32": 880, "fp32_l12": 736}  # every per-site state array read and written once
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -283,18 +286,19 @@ def run_ours(args):
 
     tiles = {}
 
-    def make_lattice(precision):
+    def make_lattice(precision, link_reals=18):
         lat = Lattice(N, A_WORK, precision=precision, reunitarize_every=16 if precision == "fp32" else 0,
                       stream=stream)
         lat.set_step_method(args.step_method)
+        lat.link_reals = link_reals
         for k in INPUT_FIELDS:
             lat.upload_device(k, inputs[k].data_ptr())
         lat.upload_device("UOld", inputs["U"].data_ptr())
         if args.tile:
             lat.set_tile(args.tile)
-            tiles[precision] = args.tile
-        else:
-            tiles[precision] = lat.autotune(DT)  # untimed: picks the electric-field kernel's block tile
+            tiles[precision + ("_l12" if link_reals == 12 else "")] = args.tile
+        else:  # untimed: picks the electric-field kernel's block tile
+            tiles[precision + ("_l12" if link_reals == 12 else "")] = lat.autotune(DT)
         return lat
 
     peak, peak_kind = hbm_peak()
@@ -341,9 +345,9 @@ def run_ours(args):
     # holds its share of reunitarisations whatever the alignment.
     steps32 = 16 * max(1, -(-args.steps // 16))
 
-    def timed_run(precision, sampler=None, nsteps=None):
+    def timed_run(precision, sampler=None, nsteps=None, link_reals=18):
         nsteps = nsteps or args.steps
-        lat = make_lattice(precision)
+        lat = make_lattice(precision, link_reals)
         lat.step(DT, args.warmup, save_uold=False)
         torch.cuda.synchronize()
         barrier()
@@ -485,6 +489,18 @@ def run_ours(args):
                 "observables_ms": obs32,
                 "roofline": roofline(dom32, "fp32", k32[dom32])}
         del lat32
+        # ---- FP32 with 12-real links (rows 0 and 1 stored, row 2 = conj(row0 x row1)), same inputs
+        lat12, ms12, k12 = timed_run("fp32", None, steps32, link_reals=12)
+        e12 = lat12.bulk()
+        dom12 = max(k12, key=k12.get)
+        fp32["links12"] = {
+            "value": world * vol / (ms12 * 1e-3), "ms_per_step": ms12,
+            "step_bytes_per_site": STEP_BYTES["fp32_l12"],
+            "step_hbm_frac": STEP_BYTES["fp32_l12"] * vol / (ms12 * 1e-3) / 1e9 / peak,
+            "energy_rel_err_vs_fp64": (abs(e12[9] - e64[9]) / abs(e64[9])) if e64 is not None else None,
+            "kernel_ms": k12, "roofline": roofline(dom12, "fp32_l12", k12[dom12]),
+            "note": "one row-2 completion pass per step() call is inside ms_per_step"}
+        del lat12
 
     if fp32 is not None and run64 and not args.no_gauge:
         # ---- FP32 against FP64 on a physical state: a 64x64x256 MV collision (seeded charges), 200 steps
@@ -501,8 +517,9 @@ def run_ours(args):
         fr = {k: (v.astype(np.complex64).astype(np.complex128) if np.iscomplexobj(v)
                   else v.astype(np.float32).astype(np.float64)) for k, v in fp.items()}
         vals = {}
-        for prec in ("fp64", "fp32"):
-            with Lattice(Np, precision=prec, reunitarize_every=16 if prec == "fp32" else 0, stream=stream) as lp:
+        for prec, reals in (("fp64", 18), ("fp32", 18), ("fp32_l12", 12)):
+            with Lattice(Np, precision=prec[:4], reunitarize_every=16 if prec != "fp64" else 0, stream=stream) as lp:
+                lp.link_reals = reals
                 lp.upload_fields(fr)
                 lp.step(DT, stepsp, save_uold=False)
                 vals[prec] = (lp.bulk()[9], lp.objective(112, 144, Lattice.PL_OVER_PT), lp.unitarity()[0])
@@ -511,7 +528,9 @@ def run_ours(args):
                      "reunitarised every 16 steps, both from the same FP32-rounded fields" % stepsp,
             "energy_rel_err_vs_fp64": abs(vals["fp32"][0] - vals["fp64"][0]) / abs(vals["fp64"][0]),
             "pl_over_pt_central_fp64": vals["fp64"][1], "pl_over_pt_central_fp32": vals["fp32"][1],
-            "fp32_unitarity_max": vals["fp32"][2]}
+            "fp32_unitarity_max": vals["fp32"][2],
+            "links12_energy_rel_err_vs_fp64": abs(vals["fp32_l12"][0] - vals["fp64"][0]) / abs(vals["fp64"][0]),
+            "links12_pl_over_pt_central": vals["fp32_l12"][1], "links12_unitarity_max": vals["fp32_l12"][2]}
 
     e2e = None
     if lat is not None and not args.no_e2e:

@@ -133,6 +133,17 @@ int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags);
 int glasma_set_step_method(glasma_lattice* h, int method);
 int glasma_get_step_method(glasma_lattice* h, int* method);
 
+/* Link storage of the leapfrog step (FP32 handles): 18 reals per link (default) or 12, rows 0 and 1
+ * of each link, with row 2 formed in registers as the unitary complement conj(row0 x row1).  With 12
+ * the step kernels and the in-step reunitarisation read and write two thirds of the link bytes; at the
+ * end of every glasma_step call row 2 is written back, so every other call sees full links.  Rows 0
+ * and 1 are taken as the link: a link that is not in SU(3) when the call starts is replaced by the
+ * SU(3)-completion of its first two rows.  GLASMA_ERR_UNSUPPORTED for 12 on FP64 handles (their
+ * kernels are bound by the FP64 pipe, which the reconstruction would load further).
+ * No reference counterpart (the reference stores full links, S/LATTICE/GaugeLinks.cpp). */
+int glasma_set_link_storage(glasma_lattice* h, int reals_per_link);
+int glasma_get_link_storage(glasma_lattice* h, int* reals_per_link);
+
 /* glasma_step with CUDA events recorded on the handle's stream around the kernels of every
  * step; kernel_ms[0] / kernel_ms[1] receive the summed milliseconds of the electric-field/JStat
  * kernel and of the link/J kernel (two-pass), or of the one-pass kernel and 0 (one-pass).

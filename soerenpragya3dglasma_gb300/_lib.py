@@ -51,6 +51,8 @@ SIGNATURES = [
     ("glasma_step_profiled", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_uint, _D]),
     ("glasma_set_step_method", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_get_step_method", ctypes.c_int, [_H, _I]),
+    ("glasma_set_link_storage", ctypes.c_int, [_H, ctypes.c_int]),
+    ("glasma_get_link_storage", ctypes.c_int, [_H, _I]),
     ("glasma_update_efield", ctypes.c_int, [_H, ctypes.c_double]),
     ("glasma_update_jstat", ctypes.c_int, [_H, ctypes.c_double]),
     ("glasma_update_links", ctypes.c_int, [_H, ctypes.c_double]),

@@ -220,6 +220,16 @@ int copy_results_to_host(glasma_lattice* h, const double* dev, double* host, siz
   return GLASMA_OK;
 }
 
+// 12-real links: the step kernels left row 2 of every link stale; write it from rows 0 and 1 so that
+// every other kernel and the downloads see full links between calls.
+template <typename T>
+int complete_links(glasma_lattice* h) {
+  if (h->link_rows != 2) return GLASMA_OK;
+  cudaError_t e = glasma::launch_complete_links<T>(h->g, static_cast<cx<T>*>(h->f[GLASMA_FIELD_U]), h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "complete links");
+  return GLASMA_OK;
+}
+
 // When `ev` is non-null it holds 3 events per step (before K1, between K1 and K2, after K2),
 // recorded on the handle's stream.
 template <typename T>
@@ -234,7 +244,8 @@ int step_impl(glasma_lattice* h, double dt, int nsteps, unsigned flags, cudaEven
     for (int n = 0; n < nsteps; n++) {
       if (ev) cudaEventRecord(ev[3 * n], h->stream);
       const bool save = (flags & GLASMA_STEP_SAVE_UOLD) && (n == nsteps - 1);
-      e = glasma::launch_fused_step<T>(h->g, ptrs<T>(h), alt_ptrs<T>(h), dt, save, h->tile_x, false, h->stream);
+      e = glasma::launch_fused_step<T>(h->g, ptrs<T>(h), alt_ptrs<T>(h), dt, save, h->tile_x, false, h->stream,
+                                       h->link_rows);
       if (e != cudaSuccess) return cuda_fail(e, "fused step");
       if (ev) {
         cudaEventRecord(ev[3 * n + 1], h->stream);
@@ -243,29 +254,29 @@ int step_impl(glasma_lattice* h, double dt, int nsteps, unsigned flags, cudaEven
       swap_buffers(h);
       h->steps_done++;
       if (h->reunit_every > 0 && h->steps_done % h->reunit_every == 0) {
-        e = glasma::launch_reunitarize<T>(h->g, static_cast<cx<T>*>(h->f[GLASMA_FIELD_U]), h->stream);
+        e = glasma::launch_reunitarize<T>(h->g, static_cast<cx<T>*>(h->f[GLASMA_FIELD_U]), h->stream, h->link_rows);
         if (e != cudaSuccess) return cuda_fail(e, "reunitarize");
       }
     }
-    return GLASMA_OK;
+    return complete_links<T>(h);
   }
   h->last_method = GLASMA_STEP_TWO_PASS;
   for (int n = 0; n < nsteps; n++) {
     if (ev) cudaEventRecord(ev[3 * n], h->stream);
-    e = glasma::launch_efield_jstat<T>(h->g, p, dt, h->tile_x, h->stream);
+    e = glasma::launch_efield_jstat<T>(h->g, p, dt, h->tile_x, h->stream, h->link_rows);
     if (e != cudaSuccess) return cuda_fail(e, "efield_jstat");
     if (ev) cudaEventRecord(ev[3 * n + 1], h->stream);
     const bool save = (flags & GLASMA_STEP_SAVE_UOLD) && (n == nsteps - 1);
-    e = glasma::launch_links_j<T>(h->g, p, dt, save, true, true, h->stream);
+    e = glasma::launch_links_j<T>(h->g, p, dt, save, true, true, h->stream, h->link_rows);
     if (e != cudaSuccess) return cuda_fail(e, "links_j");
     if (ev) cudaEventRecord(ev[3 * n + 2], h->stream);
     h->steps_done++;
     if (h->reunit_every > 0 && h->steps_done % h->reunit_every == 0) {
-      e = glasma::launch_reunitarize<T>(h->g, p.U, h->stream);
+      e = glasma::launch_reunitarize<T>(h->g, p.U, h->stream, h->link_rows);
       if (e != cudaSuccess) return cuda_fail(e, "reunitarize");
     }
   }
-  return GLASMA_OK;
+  return complete_links<T>(h);
 }
 
 }  // namespace
@@ -315,6 +326,7 @@ int glasma_create(int nx, int ny, int nz, double ax, double ay, double az, int p
   h->real_bytes = precision == GLASMA_FP64 ? 8 : 4;
   h->tile_x = glasma::default_tile_x(nx);
   h->step_method = GLASMA_STEP_TWO_PASS;  // faster on GB300 while the step is bound by arithmetic issue
+  h->link_rows = 3;
   h->last_method = GLASMA_STEP_TWO_PASS;
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
@@ -538,6 +550,23 @@ int glasma_set_step_method(glasma_lattice* h, int method) {
       h->alt[f] = nullptr;
     }
   }
+  return GLASMA_OK;
+}
+
+int glasma_set_link_storage(glasma_lattice* h, int reals_per_link) {
+  GLASMA_CHECK_HANDLE(h);
+  if (reals_per_link != 18 && reals_per_link != 12)
+    return fail(GLASMA_ERR_INVALID_ARGUMENT, "reals_per_link must be 18 or 12");
+  if (reals_per_link == 12 && h->precision != GLASMA_FP32)
+    return fail(GLASMA_ERR_UNSUPPORTED, "12-real links are built for FP32 handles only");
+  h->link_rows = reals_per_link == 12 ? 2 : 3;
+  return GLASMA_OK;
+}
+
+int glasma_get_link_storage(glasma_lattice* h, int* reals_per_link) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!reals_per_link) return fail(GLASMA_ERR_INVALID_ARGUMENT, "reals_per_link is null");
+  *reals_per_link = h->link_rows == 2 ? 12 : 18;
   return GLASMA_OK;
 }
 
@@ -870,9 +899,10 @@ int glasma_autotune(glasma_lattice* h, double dt, int* tile_x) {
           one_pass ? GLASMA_DISPATCH(h, glasma::launch_fused_step<double>(h->g, ptrs<double>(h), alt_ptrs<double>(h), dt,
                                                                           false, tx, true, h->stream),
                                      glasma::launch_fused_step<float>(h->g, ptrs<float>(h), alt_ptrs<float>(h), dt, false,
-                                                                      tx, true, h->stream))
+                                                                      tx, true, h->stream, h->link_rows))
                    : GLASMA_DISPATCH(h, glasma::launch_efield_dry<double>(h->g, ptrs<double>(h), dt, tx, h->stream),
-                                     glasma::launch_efield_dry<float>(h->g, ptrs<float>(h), dt, tx, h->stream));
+                                     glasma::launch_efield_dry<float>(h->g, ptrs<float>(h), dt, tx, h->stream,
+                                                                      h->link_rows));
       cudaEventRecord(e1, h->stream);
       if (e != cudaSuccess) {
         cudaEventDestroy(e0);

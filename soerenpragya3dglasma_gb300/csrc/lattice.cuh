@@ -56,6 +56,51 @@ __device__ __forceinline__ void store_link(cx<T>* __restrict__ U, I S, int mu, I
 #pragma unroll
   for (int k = 0; k < 9; k++) p[(I)k * S] = m.e[k];
 }
+// 12-real links: the leapfrog kernels of a handle in two-row storage read and write rows 0 and 1 of
+// each link only (k = 0,1,3,4,6,7: 12 reals of 18) and form row 2 in registers as the unitary
+// complement with unit determinant, row2 = conj(row0 x row1): for U in SU(3) the rows are orthonormal
+// and det U = row2 . (row0 x row1) = 1 fix it.  R = rows stored (3 = full, 2 = two-row).
+template <typename T>
+__device__ __forceinline__ void complete_row2(Mat<T>& m) {
+  // m(0,j) = e[3j], m(1,j) = e[3j+1], m(2,j) = e[3j+2]
+  auto cross = [](const cx<T>& a, const cx<T>& b, const cx<T>& c, const cx<T>& d) {
+    // conj(a b - c d)
+    cx<T> r;
+    r.re = fma(a.re, b.re, fma(-a.im, b.im, fma(-c.re, d.re, c.im * d.im)));
+    r.im = -fma(a.re, b.im, fma(a.im, b.re, fma(-c.re, d.im, -(c.im * d.re))));
+    return r;
+  };
+  m.e[2] = cross(m.e[3], m.e[7], m.e[6], m.e[4]);
+  m.e[5] = cross(m.e[6], m.e[1], m.e[0], m.e[7]);
+  m.e[8] = cross(m.e[0], m.e[4], m.e[3], m.e[1]);
+}
+template <int R, typename T, typename I>
+__device__ __forceinline__ void load_link_r(const cx<T>* __restrict__ U, I S, int mu, I s, Mat<T>& m) {
+  if constexpr (R == 3) {
+    load_link(U, S, mu, s, m);
+  } else {
+    const cx<T>* p = U + ((I)(mu * 9) * S + s);
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      m.e[3 * j] = p[(I)(3 * j) * S];
+      m.e[3 * j + 1] = p[(I)(3 * j + 1) * S];
+    }
+    complete_row2(m);
+  }
+}
+template <int R, typename T, typename I>
+__device__ __forceinline__ void store_link_r(cx<T>* __restrict__ U, I S, int mu, I s, const Mat<T>& m) {
+  if constexpr (R == 3) {
+    store_link(U, S, mu, s, m);
+  } else {
+    cx<T>* p = U + ((I)(mu * 9) * S + s);
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      p[(I)(3 * j) * S] = m.e[3 * j];
+      p[(I)(3 * j + 1) * S] = m.e[3 * j + 1];
+    }
+  }
+}
 template <typename T, typename I>
 __device__ __forceinline__ void load_alg(const T* __restrict__ F, I S, int base, I s, Alg<T>& v) {
   const T* p = F + ((I)base * S + s);
@@ -75,23 +120,30 @@ inline bool use_32bit_index(const Geometry& g) { return g.S * 27 < (1LL << 31) -
 // All launches go to `stream`.  Return cudaGetLastError() of the launch.
 // tile_x: sites along x per K1 block tile (kThreads/tile_x along y); chosen by the autotuner.
 template <typename T>
-cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream);
+cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream,
+                                int link_rows = 3);
 // K1 computing everything and storing nothing: timing runs of the autotuner.
 template <typename T>
-cudaError_t launch_efield_dry(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream);
+cudaError_t launch_efield_dry(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream,
+                              int link_rows = 3);
 template <typename T>
 cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second_half,
-                           cudaStream_t stream);
+                           cudaStream_t stream, int link_rows = 3);
 // The whole step in one launch: reads U, J, JStat of time t from `in`, writes those of t+dt to `out`
 // (distinct buffers), E in place in in.E, UOld (when save_uold) in in.UOld.  Bit-identical to
 // launch_efield_jstat followed by launch_links_j.  dry: compute, store nothing (autotuner).
 template <typename T>
 cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, double dt, bool save_uold,
-                              int tile_x, bool dry, cudaStream_t stream);
+                              int tile_x, bool dry, cudaStream_t stream, int link_rows = 3);
 template <typename T>
 cudaError_t launch_sync_ghosts(const Geometry& g, T* base, int components, cudaStream_t stream);
 template <typename T>
-cudaError_t launch_reunitarize(const Geometry& g, cx<T>* U, cudaStream_t stream);
+cudaError_t launch_reunitarize(const Geometry& g, cx<T>* U, cudaStream_t stream, int link_rows = 3);
+// link_rows (3 = full links, 2 = 12-real two-row storage, FP32 only) selects the link accessors of the
+// leapfrog and reunitarisation kernels above; complete_links writes row 2 of every link from rows 0
+// and 1, which returns a two-row array to full matrices for every other kernel.
+template <typename T>
+cudaError_t launch_complete_links(const Geometry& g, cx<T>* U, cudaStream_t stream);
 
 // Sub-step kernels with the reference's exact sub-step boundaries.
 template <typename T>

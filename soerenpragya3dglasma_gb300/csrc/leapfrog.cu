@@ -23,30 +23,31 @@ namespace glasma {
 
 namespace {
 
-template <typename T, typename I>
+// R: rows of each link the kernel reads and writes (3 full, 2 for 12-real links).
+template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
     efield_jstat_kernel(Geometry g, FieldPtrs<T> f, EParams<T> p, TileMap tm) {
   __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   int x, y, z;
   if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
-  efield_site<T, I>(g, f, p, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
+  efield_site<T, I, R>(g, f, p, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
 }
 
-template <typename T, typename I>
+template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
     links_j_kernel(Geometry g, FieldPtrs<T> f, LParams<T> p) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
   if (idx >= (I)g.vol) return;
-  links_site<T, I>(g, f, p, idx);
+  links_site<T, I, R>(g, f, p, idx);
 }
 
-template <typename T, typename I>
+template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kFusedMinBlocks)
     fused_step_kernel(Geometry g, FieldPtrs<T> in, FieldPtrs<T> out, EParams<T> pe, LParams<T> pl, TileMap tm) {
   __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   int x, y, z;
   if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
-  fused_site<T, I>(g, in, out, pe, pl, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
+  fused_site<T, I, R>(g, in, out, pe, pl, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
 }
 
 template <typename T, typename I>
@@ -90,16 +91,30 @@ __global__ void sync_ghosts_kernel(E* base, long long S, long long plane, int nz
   p[(long long)(nz + 1) * plane + r] = p[(long long)nz * plane + r];  // z=Nz <- z=Nz-1
 }
 
-template <typename T>
+template <typename T, int R>
 __global__ void reunitarize_kernel(Geometry g, cx<T>* U) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.S * 3) return;
   const int mu = (int)(i / g.S);
   const long long s = i - (long long)mu * g.S;
   Mat<T> u;
-  load_link<T, long long>(U, g.S, mu, s, u);
+  load_link_r<R, T, long long>(U, g.S, mu, s, u);
   reunitarize(u);
-  store_link<T, long long>(U, g.S, mu, s, u);
+  store_link_r<R, T, long long>(U, g.S, mu, s, u);
+}
+
+// Row 2 of every link (ghost slices included) from rows 0 and 1: two-row storage back to full links.
+template <typename T>
+__global__ void complete_links_kernel(Geometry g, cx<T>* U) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.S * 3) return;
+  const int mu = (int)(i / g.S);
+  const long long s = i - (long long)mu * g.S;
+  Mat<T> u;
+  load_link_r<2, T, long long>(U, g.S, mu, s, u);
+  cx<T>* p = U + (long long)(mu * 9) * g.S + s;
+#pragma unroll
+  for (int j = 0; j < 3; j++) p[(long long)(3 * j + 2) * g.S] = u.e[3 * j + 2];
 }
 
 template <typename E>
@@ -126,19 +141,38 @@ void prefer_l1(K kernel) {
   }
 }
 
+// Two-row (12-real) link storage is built for FP32 only: the FP64 kernels are bound by the FP64 pipe,
+// and the row reconstruction would add FP64 work to save bytes that do not bound them.
+template <typename T>
+bool two_row(int link_rows) {
+  return sizeof(T) == 4 && link_rows == 2;
+}
+
+template <typename T, int R>
+void launch_efield_rows(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, const TileMap& tm, unsigned grid,
+                        cudaStream_t stream) {
+  if (use_32bit_index(g)) {
+    prefer_l1<T>(efield_jstat_kernel<T, int, R>);
+    efield_jstat_kernel<T, int, R><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
+  } else {
+    prefer_l1<T>(efield_jstat_kernel<T, long long, R>);
+    efield_jstat_kernel<T, long long, R><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
+  }
+}
+
 template <typename T>
 cudaError_t launch_efield_kernel(const Geometry& g, FieldPtrs<T> f, const EParams<T>& p, int tile_x,
-                                 cudaStream_t stream) {
+                                 cudaStream_t stream, int link_rows = 3) {
   if (tile_x <= 0 || tile_x > kThreads || kThreads % tile_x) tile_x = kThreads;
   const TileMap tm = TileMap::make(g.nx, g.ny, tile_x, kThreads);
   const unsigned grid = (unsigned)tm.tiles(g.nz);
-  if (use_32bit_index(g)) {
-    prefer_l1<T>(efield_jstat_kernel<T, int>);
-    efield_jstat_kernel<T, int><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
-  } else {
-    prefer_l1<T>(efield_jstat_kernel<T, long long>);
-    efield_jstat_kernel<T, long long><<<grid, kThreads, 0, stream>>>(g, f, p, tm);
+  if constexpr (sizeof(T) == 4) {
+    if (two_row<T>(link_rows)) {
+      launch_efield_rows<T, 2>(g, f, p, tm, grid, stream);
+      return cudaGetLastError();
+    }
   }
+  launch_efield_rows<T, 3>(g, f, p, tm, grid, stream);
   return cudaGetLastError();
 }
 
@@ -163,13 +197,15 @@ EParams<T> make_eparams(const Geometry& g, double dt, int do_e, int do_jstat, in
 }  // namespace
 
 template <typename T>
-cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream) {
-  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 1, 1, 0), tile_x, stream);
+cudaError_t launch_efield_jstat(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream,
+                                int link_rows) {
+  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 1, 1, 0), tile_x, stream, link_rows);
 }
 
 template <typename T>
-cudaError_t launch_efield_dry(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream) {
-  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 1, 1, 1), tile_x, stream);
+cudaError_t launch_efield_dry(const Geometry& g, FieldPtrs<T> f, double dt, int tile_x, cudaStream_t stream,
+                              int link_rows) {
+  return launch_efield_kernel<T>(g, f, make_eparams<T>(g, dt, 1, 1, 1), tile_x, stream, link_rows);
 }
 
 template <typename T>
@@ -194,32 +230,55 @@ LParams<T> make_lparams(const Geometry& g, double dt, bool save_uold, bool do_j,
   return p;
 }
 
+template <typename T, int R>
+void launch_fused_rows(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, const EParams<T>& pe,
+                       const LParams<T>& pl, const TileMap& tm, unsigned grid, cudaStream_t stream) {
+  if (use_32bit_index(g)) {
+    prefer_l1<T>(fused_step_kernel<T, int, R>);
+    fused_step_kernel<T, int, R><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
+  } else {
+    prefer_l1<T>(fused_step_kernel<T, long long, R>);
+    fused_step_kernel<T, long long, R><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
+  }
+}
+
 template <typename T>
 cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, double dt, bool save_uold,
-                              int tile_x, bool dry, cudaStream_t stream) {
+                              int tile_x, bool dry, cudaStream_t stream, int link_rows) {
   if (tile_x <= 0 || tile_x > kThreads || kThreads % tile_x) tile_x = kThreads;
   const TileMap tm = TileMap::make(g.nx, g.ny, tile_x, kThreads);
   const unsigned grid = (unsigned)tm.tiles(g.nz);
   const EParams<T> pe = make_eparams<T>(g, dt, 1, 1, dry ? 1 : 0);
   const LParams<T> pl = make_lparams<T>(g, dt, save_uold, true, true);
-  if (use_32bit_index(g)) {
-    prefer_l1<T>(fused_step_kernel<T, int>);
-    fused_step_kernel<T, int><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
-  } else {
-    prefer_l1<T>(fused_step_kernel<T, long long>);
-    fused_step_kernel<T, long long><<<grid, kThreads, 0, stream>>>(g, in, out, pe, pl, tm);
+  if constexpr (sizeof(T) == 4) {
+    if (two_row<T>(link_rows)) {
+      launch_fused_rows<T, 2>(g, in, out, pe, pl, tm, grid, stream);
+      return cudaGetLastError();
+    }
   }
+  launch_fused_rows<T, 3>(g, in, out, pe, pl, tm, grid, stream);
   return cudaGetLastError();
+}
+
+template <typename T, int R>
+void launch_links_rows(const Geometry& g, FieldPtrs<T> f, const LParams<T>& p, cudaStream_t stream) {
+  if (use_32bit_index(g))
+    links_j_kernel<T, int, R><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+  else
+    links_j_kernel<T, long long, R><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
 }
 
 template <typename T>
 cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, int link_rows) {
   const LParams<T> p = make_lparams<T>(g, dt, save_uold, do_j, do_second);
-  if (use_32bit_index(g))
-    links_j_kernel<T, int><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
-  else
-    links_j_kernel<T, long long><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
+  if constexpr (sizeof(T) == 4) {
+    if (two_row<T>(link_rows)) {
+      launch_links_rows<T, 2>(g, f, p, stream);
+      return cudaGetLastError();
+    }
+  }
+  launch_links_rows<T, 3>(g, f, p, stream);
   return cudaGetLastError();
 }
 
@@ -246,8 +305,20 @@ cudaError_t launch_sync_ghosts(const Geometry& g, T* base, int components, cudaS
 }
 
 template <typename T>
-cudaError_t launch_reunitarize(const Geometry& g, cx<T>* U, cudaStream_t stream) {
-  reunitarize_kernel<T><<<grid_for(g.S * 3, kThreads), kThreads, 0, stream>>>(g, U);
+cudaError_t launch_reunitarize(const Geometry& g, cx<T>* U, cudaStream_t stream, int link_rows) {
+  if constexpr (sizeof(T) == 4) {
+    if (two_row<T>(link_rows)) {
+      reunitarize_kernel<T, 2><<<grid_for(g.S * 3, kThreads), kThreads, 0, stream>>>(g, U);
+      return cudaGetLastError();
+    }
+  }
+  reunitarize_kernel<T, 3><<<grid_for(g.S * 3, kThreads), kThreads, 0, stream>>>(g, U);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_complete_links(const Geometry& g, cx<T>* U, cudaStream_t stream) {
+  complete_links_kernel<T><<<grid_for(g.S * 3, 256), 256, 0, stream>>>(g, U);
   return cudaGetLastError();
 }
 
@@ -260,15 +331,17 @@ cudaError_t launch_copy_links(const Geometry& g, const cx<T>* src, cx<T>* dst, c
 
 #define GLASMA_INSTANTIATE(T)                                                                                   \
   template cudaError_t launch_fused_step<T>(const Geometry&, FieldPtrs<T>, FieldPtrs<T>, double, bool, int, bool, \
-                                            cudaStream_t);                                                      \
-  template cudaError_t launch_efield_jstat<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);       \
-  template cudaError_t launch_efield_dry<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);         \
+                                            cudaStream_t, int);                                                 \
+  template cudaError_t launch_efield_jstat<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t, int);  \
+  template cudaError_t launch_efield_dry<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t, int);    \
   template cudaError_t launch_efield_only<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);        \
   template cudaError_t launch_jstat_only<T>(const Geometry&, FieldPtrs<T>, double, int, cudaStream_t);         \
-  template cudaError_t launch_links_j<T>(const Geometry&, FieldPtrs<T>, double, bool, bool, bool, cudaStream_t); \
+  template cudaError_t launch_links_j<T>(const Geometry&, FieldPtrs<T>, double, bool, bool, bool, cudaStream_t,  \
+                                         int);                                                                  \
   template cudaError_t launch_links_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);              \
   template cudaError_t launch_j_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);                  \
-  template cudaError_t launch_reunitarize<T>(const Geometry&, cx<T>*, cudaStream_t);                           \
+  template cudaError_t launch_reunitarize<T>(const Geometry&, cx<T>*, cudaStream_t, int);                      \
+  template cudaError_t launch_complete_links<T>(const Geometry&, cx<T>*, cudaStream_t);                        \
   template cudaError_t launch_copy_links<T>(const Geometry&, const cx<T>*, cx<T>*, cudaStream_t);              \
   template cudaError_t launch_sync_ghosts<T>(const Geometry&, T*, int, cudaStream_t);                          \
   template cudaError_t launch_sync_ghosts<cx<T>>(const Geometry&, cx<T>*, int, cudaStream_t);

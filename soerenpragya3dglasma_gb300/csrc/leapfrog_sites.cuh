@@ -83,8 +83,9 @@ struct StapleShare {
 };
 enum StapleMode { kStapleCompute = 0, kStapleStore = 1, kStapleReuse = 2 };
 
-// Staples of link mu at x in the (mu,nu) plane, weighted by c, added to acc.
-template <typename T, typename I>
+// Staples of link mu at x in the (mu,nu) plane, weighted by c, added to acc.  R: rows of each link
+// stored (3 full, 2 for 12-real links, see load_link_r).
+template <typename T, typename I, int R = 3>
 __device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, I S, int mu, int nu, I s, I s_pmu, I s_pnu,
                                             I s_pmu_mnu, I s_mnu, T c, Mat<T>& acc, cx<T>* sh = nullptr,
                                             int mode = kStapleCompute, int slot = 0) {
@@ -99,8 +100,8 @@ __device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, I S, in
         t.e[i + 3 * j] = mk<T>(v.re, -v.im);
       }
   } else {
-    load_link(U, S, nu, s_pmu, a);
-    load_link(U, S, mu, s_pnu, b);
+    load_link_r<R>(U, S, nu, s_pmu, a);
+    load_link_r<R>(U, S, mu, s_pnu, b);
     mul_nd(a, b, t);
     if (sh && mode == kStapleStore) {
       cx<T>* q = sh + (slot * 9) * kThreads + threadIdx.x;
@@ -108,12 +109,12 @@ __device__ __forceinline__ void add_staples(const cx<T>* __restrict__ U, I S, in
       for (int k = 0; k < 9; k++) q[k * kThreads] = t.e[k];
     }
   }
-  load_link(U, S, nu, s, a);
+  load_link_r<R>(U, S, nu, s, a);
   add_mul_nd(t, a, c, acc);
-  load_link(U, S, nu, s_pmu_mnu, a);
-  load_link(U, S, mu, s_mnu, b);
+  load_link_r<R>(U, S, nu, s_pmu_mnu, a);
+  load_link_r<R>(U, S, mu, s_mnu, b);
   mul_dd(a, b, t);
-  load_link(U, S, nu, s_mnu, a);
+  load_link_r<R>(U, S, nu, s_mnu, a);
   add_mul_nn(t, a, c, acc);
 }
 
@@ -128,7 +129,7 @@ struct EParams {
 };
 
 // The electric-field and JStat update of one site (K1's per-site body).
-template <typename T, typename I>
+template <typename T, typename I, int R = 3>
 __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T>& f, const EParams<T>& p, int x, int y,
                                             int z, cx<T>* sh = nullptr) {
   const I S = (I)g.S, plane = (I)g.plane;
@@ -144,17 +145,17 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
       Mat<T> acc;
       set_zero(acc);
       if (mu == 0) {
-        add_staples(f.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc, sh, kStapleStore, 0);
-        add_staples(f.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc, sh, kStapleStore, 1);
+        add_staples<T, I, R>(f.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, p.cnu[1], acc, sh, kStapleStore, 0);
+        add_staples<T, I, R>(f.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, p.cnu[2], acc, sh, kStapleStore, 1);
       } else if (mu == 1) {
-        add_staples(f.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc, sh, kStapleReuse, 0);
-        add_staples(f.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc, sh, kStapleStore, 0);
+        add_staples<T, I, R>(f.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, p.cnu[0], acc, sh, kStapleReuse, 0);
+        add_staples<T, I, R>(f.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, p.cnu[2], acc, sh, kStapleStore, 0);
       } else {
-        add_staples(f.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc, sh, kStapleReuse, 1);
-        add_staples(f.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc, sh, kStapleReuse, 0);
+        add_staples<T, I, R>(f.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, p.cnu[0], acc, sh, kStapleReuse, 1);
+        add_staples<T, I, R>(f.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, p.cnu[1], acc, sh, kStapleReuse, 0);
       }
       Mat<T> u, P;
-      load_link(f.U, S, mu, s, u);
+      load_link_r<R>(f.U, S, mu, s, u);
       mul_nn_traceless(u, acc, P);
       Alg<T> force, e;
       retr_itg(P, pick3(p.gc, mu), force);
@@ -177,7 +178,7 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
   if (p.do_jstat) {
     const I szm = s - plane;
     Mat<T> uzm;
-    load_link(f.U, S, 2, szm, uzm);
+    load_link_r<R>(f.U, S, 2, szm, uzm);
     Alg<T> down, jc, st;
     load_alg(f.Jp, S, 0, szm, jc);
     inv_adj_mul(uzm, jc, down);
@@ -233,7 +234,7 @@ struct LParams {
 };
 
 // K2's per-site body: links to t+dt (two applications of one exp), UOld, J transport.
-template <typename T, typename I>
+template <typename T, typename I, int R = 3>
 __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>& f, const LParams<T>& p, I idx) {
   const I S = (I)g.S, plane = (I)g.plane;
   const I s = idx + plane;
@@ -245,14 +246,14 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
     Alg<T> e;
     load_alg(f.E, S, mu * 8, s, e);
     Mat<T> X, u, uh;
-    load_link(f.U, S, mu, s, u);
+    load_link_r<R>(f.U, S, mu, s, u);
     // Without a use for U(t+dt/2) (UOld, the z-link J transport), the two half steps are one:
     // exp(i c t.E)^2 = exp(2i c t.E), one matmul less (equal up to rounding).
     if (p.do_second && !p.save_uold && !(mu == 2 && p.do_j)) {
       link_exp(T(2) * pick3(p.cU, mu), e, X);
       link_apply(X, u, uh);
-      store_link(f.U, S, mu, s, uh);
-      if (sg >= 0) store_link(f.U, S, mu, sg, uh);
+      store_link_r<R>(f.U, S, mu, s, uh);
+      if (sg >= 0) store_link_r<R>(f.U, S, mu, sg, uh);
       continue;
     }
     link_exp(pick3(p.cU, mu), e, X);
@@ -284,8 +285,8 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
     } else {
       u = uh;
     }
-    store_link(f.U, S, mu, s, u);
-    if (sg >= 0) store_link(f.U, S, mu, sg, u);
+    store_link_r<R>(f.U, S, mu, s, u);
+    if (sg >= 0) store_link_r<R>(f.U, S, mu, sg, u);
   }
 }
 
@@ -300,14 +301,14 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
 //   Uh            = exp(i cU E_mu(x)) U_mu(x)                        UpdateGaugeLinks(dt/2)
 //   J(x)         += -/+ cj (Uh_z J Stat(x+z) Uh_z^d - JStat(x))     UpdateJ
 //   U_mu(x; t+dt) = exp(i cU E_mu(x)) Uh                             UpdateGaugeLinks(dt/2)
-template <typename T, typename I>
+template <typename T, typename I, int R = 3>
 __device__ __forceinline__ void fused_currents(const FieldPtrs<T>& in, const FieldPtrs<T>& out, I S, I plane, I s,
                                                I sg, bool hi, const Mat<T>& uz, const Mat<T>& uhz, T cj, bool dry) {
   const I szm = s - plane, szp = s + plane;
   Alg<T> jc, down, sp, sm;
   {
     Mat<T> w;
-    load_link(in.U, S, 2, szm, w);
+    load_link_r<R>(in.U, S, 2, szm, w);
     load_alg(in.Jp, S, 0, szm, jc);
     inv_adj_mul(w, jc, down);
     load_alg(in.Jp, S, 0, s, jc);
@@ -361,7 +362,7 @@ __device__ __forceinline__ void fused_currents(const FieldPtrs<T>& in, const Fie
   }
 }
 
-template <typename T, typename I>
+template <typename T, typename I, int R = 3>
 __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>& in, const FieldPtrs<T>& out,
                                            const EParams<T>& pe, const LParams<T>& pl, int x, int y, int z,
                                            cx<T>* sh = nullptr) {
@@ -378,17 +379,17 @@ __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>
     Mat<T> acc;
     set_zero(acc);
     if (mu == 0) {
-      add_staples(in.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, pe.cnu[1], acc, sh, kStapleStore, 0);
-      add_staples(in.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, pe.cnu[2], acc, sh, kStapleStore, 1);
+      add_staples<T, I, R>(in.U, S, 0, 1, s, sxp, syp, nb<I>(g, x, y, z, 1, -1, 0), sym, pe.cnu[1], acc, sh, kStapleStore, 0);
+      add_staples<T, I, R>(in.U, S, 0, 2, s, sxp, szp, nb<I>(g, x, y, z, 1, 0, -1), szm, pe.cnu[2], acc, sh, kStapleStore, 1);
     } else if (mu == 1) {
-      add_staples(in.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, pe.cnu[0], acc, sh, kStapleReuse, 0);
-      add_staples(in.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, pe.cnu[2], acc, sh, kStapleStore, 0);
+      add_staples<T, I, R>(in.U, S, 1, 0, s, syp, sxp, nb<I>(g, x, y, z, -1, 1, 0), sxm, pe.cnu[0], acc, sh, kStapleReuse, 0);
+      add_staples<T, I, R>(in.U, S, 1, 2, s, syp, szp, nb<I>(g, x, y, z, 0, 1, -1), szm, pe.cnu[2], acc, sh, kStapleStore, 0);
     } else {
-      add_staples(in.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, pe.cnu[0], acc, sh, kStapleReuse, 1);
-      add_staples(in.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, pe.cnu[1], acc, sh, kStapleReuse, 0);
+      add_staples<T, I, R>(in.U, S, 2, 0, s, szp, sxp, nb<I>(g, x, y, z, -1, 0, 1), sxm, pe.cnu[0], acc, sh, kStapleReuse, 1);
+      add_staples<T, I, R>(in.U, S, 2, 1, s, szp, syp, nb<I>(g, x, y, z, 0, -1, 1), sym, pe.cnu[1], acc, sh, kStapleReuse, 0);
     }
     Mat<T> u, w;
-    load_link(in.U, S, mu, s, u);
+    load_link_r<R>(in.U, S, mu, s, u);
     mul_nn_traceless(u, acc, w);
     Alg<T> force, e;
     retr_itg(w, pick3(pe.gc, mu), force);
@@ -411,8 +412,8 @@ __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>
       link_exp(T(2) * pick3(pl.cU, mu), e, X);
       link_apply(X, u, w);
       if (!dry) {
-        store_link(out.U, S, mu, s, w);
-        if (sg >= 0) store_link(out.U, S, mu, sg, w);
+        store_link_r<R>(out.U, S, mu, s, w);
+        if (sg >= 0) store_link_r<R>(out.U, S, mu, sg, w);
       }
       continue;
     }
@@ -424,10 +425,10 @@ __device__ __forceinline__ void fused_site(const Geometry& g, const FieldPtrs<T>
     }
     link_apply(X, uh, w);
     if (!dry) {
-      store_link(out.U, S, mu, s, w);
-      if (sg >= 0) store_link(out.U, S, mu, sg, w);
+      store_link_r<R>(out.U, S, mu, s, w);
+      if (sg >= 0) store_link_r<R>(out.U, S, mu, sg, w);
     }
-    if (mu == 2) fused_currents<T, I>(in, out, S, plane, s, sg, hi, u, uh, pl.cj, dry);
+    if (mu == 2) fused_currents<T, I, R>(in, out, S, plane, s, sg, hi, u, uh, pl.cj, dry);
   }
 }
 

@@ -236,6 +236,18 @@ class Lattice:
         check(self.lib.glasma_get_step_method(self.h, ctypes.byref(m)))
         return {v: k for k, v in self.STEP_METHODS.items()}[m.value]
 
+    @property
+    def link_reals(self):
+        """Reals per link the leapfrog step reads and writes: 18, or 12 (rows 0 and 1 of each link,
+        row 2 formed as conj(row0 x row1); FP32 handles only)."""
+        m = ctypes.c_int()
+        check(self.lib.glasma_get_link_storage(self.h, ctypes.byref(m)))
+        return m.value
+
+    @link_reals.setter
+    def link_reals(self, reals):
+        check(self.lib.glasma_set_link_storage(self.h, int(reals)))
+
     def step_profiled(self, dt, nsteps=1, save_uold=False):
         """Like step(); returns the summed CUDA-event milliseconds of (efield_jstat, links_j) for the
         two-pass method, (one-pass kernel, 0) for the one-pass method."""
