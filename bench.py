@@ -639,22 +639,30 @@ def run_batched(args):
     shapes = ([tuple(int(v) for v in args.event_shape.split(","))] * args.events if args.event_shape
               else batched_shapes(args.events))
     sites = sum(a * b * c for a, b, c in shapes)
-    with Batch(shapes, precision="fp32", reunitarize_every=16, stream=stream) as b:
-        for i, ev in enumerate(b.events):
-            ev.fill_synthetic(2000 + i, LINK_AMP, E_AMP, J_AMP)
-        tiles = b.autotune(0.1)
-        b.step(0.1, max(args.warmup, 16), use_graph=True)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        clk = ClockSampler(0)
-        clk.__enter__()
-        e0.record(stream)
-        b.step(0.1, args.steps, use_graph=True)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        clk.__exit__(None, None, None)
-        ms = e0.elapsed_time(e1) / args.steps
-        energy = b.energy()
+    clk = ClockSampler(0)
+
+    def timed_batch(reals, sampler=None):
+        with Batch(shapes, precision="fp32", reunitarize_every=16, stream=stream) as b:
+            b.set_link_reals(reals)
+            for i, ev in enumerate(b.events):
+                ev.fill_synthetic(2000 + i, LINK_AMP, E_AMP, J_AMP)
+            tiles = b.autotune(0.1)
+            b.step(0.1, max(args.warmup, 16), use_graph=True)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if sampler is not None:
+                sampler.__enter__()
+            e0.record(stream)
+            b.step(0.1, args.steps, use_graph=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if sampler is not None:
+                sampler.__exit__(None, None, None)
+            return e0.elapsed_time(e1) / args.steps, b.energy(), tiles
+
+    ms, energy, tiles = timed_batch(18, clk)
+    # the same events with 12-real links (rows 0 and 1 stored; one row-2 pass per event per call)
+    ms12, energy12, _ = timed_batch(12)
     peak, peak_kind = hbm_peak()
     line = {
         "metric": "batched leapfrog site-updates/s",
@@ -676,6 +684,9 @@ def run_batched(args):
         "peak_kind": peak_kind,
         "tiles_by_shape": sorted(set((s[0], t) for s, t in zip(shapes, tiles))),
         "energy_finite": bool(all(abs(x) < float("inf") for x in energy)),
+        "links12": {"value": sites / (ms12 * 1e-3), "ms_per_step": ms12,
+                    "step_hbm_frac": STEP_BYTES["fp32_l12"] * sites / (ms12 * 1e-3) / 1e9 / peak,
+                    "max_energy_rel_diff_vs_18_real": max(abs(x - y) / abs(y) for x, y in zip(energy12, energy))},
         "clocks": clk.summary(),
         "gpu_launches": 2 * args.steps + (args.steps // 16) * len(shapes),
     }

@@ -364,6 +364,10 @@ int glasma_batch_step(glasma_batch* b, double dt, int nsteps, int use_graph);
 #define GLASMA_BATCH_PERSISTENT 0
 #define GLASMA_BATCH_TILE_GRID 1
 int glasma_batch_set_launch(glasma_batch* b, int mode);
+/* 12-real links for every event of an FP32 batch (see glasma_set_link_storage): the batched step
+ * kernels read and write rows 0 and 1 of each link; row 2 is written back at the end of every
+ * glasma_batch_step call. */
+int glasma_batch_set_link_storage(glasma_batch* b, int reals_per_link);
 /* Per-event T00 (volume sum, FP64 reductions), n_events doubles. */
 int glasma_batch_energy(glasma_batch* b, double* t00);
 int glasma_batch_synchronize(glasma_batch* b);

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("glasma_batch_autotune", ctypes.c_int, [_H, ctypes.c_double, _I]),
     ("glasma_batch_step", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int]),
     ("glasma_batch_set_launch", ctypes.c_int, [_H, ctypes.c_int]),
+    ("glasma_batch_set_link_storage", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_batch_energy", ctypes.c_int, [_H, _D]),
     ("glasma_batch_synchronize", ctypes.c_int, [_H]),
     ("glasma_batch_last_error", ctypes.c_char_p, []),

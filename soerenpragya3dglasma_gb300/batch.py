@@ -57,6 +57,11 @@ class Batch:
         tile list); both cover all events in one launch per kernel and give the same fields."""
         _bcheck(self.lib, self.lib.glasma_batch_set_launch(self.b, {"persistent": 0, "tile_grid": 1}[mode]))
 
+    def set_link_reals(self, reals):
+        """18 (default) or 12 reals per link in the batched step (FP32 batches; rows 0 and 1 of each
+        link stored, row 2 formed as conj(row0 x row1)); every event follows the setting."""
+        _bcheck(self.lib, self.lib.glasma_batch_set_link_storage(self.b, int(reals)))
+
     def step(self, dt, nsteps, use_graph=True):
         _bcheck(self.lib, self.lib.glasma_batch_step(self.b, float(dt), int(nsteps), int(bool(use_graph))))
 

@@ -36,7 +36,8 @@ struct EventDesc {
   long long k2_begin;  // first 128-site chunk of this event
 };
 
-template <typename T, typename I>
+// R: rows of each link read and written (3 full, 2 for 12-real links).
+template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
     efield_batch_kernel(const EventDesc<T>* __restrict__ ev, const unsigned short* __restrict__ tile_ev, long long total) {
   __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
@@ -49,11 +50,11 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
     const EParams<T> ep = ev[e].ep;
     const TileMap tm = ev[e].tm;
     int x, y, z;
-    if (tm.site(t - ev[e].k1_begin, threadIdx.x, g.nx, g.ny, x, y, z)) efield_site<T, I>(g, f, ep, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
+    if (tm.site(t - ev[e].k1_begin, threadIdx.x, g.nx, g.ny, x, y, z)) efield_site<T, I, R>(g, f, ep, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
   }
 }
 
-template <typename T, typename I>
+template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
     links_batch_kernel(const EventDesc<T>* __restrict__ ev, const unsigned short* __restrict__ tile_ev, long long total) {
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
@@ -62,7 +63,7 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
     const FieldPtrs<T> f = ev[e].f;
     const LParams<T> lp = ev[e].lp;
     const long long idx = (t - ev[e].k2_begin) * kThreads + threadIdx.x;
-    if (idx < g.vol) links_site<T, I>(g, f, lp, (I)idx);
+    if (idx < g.vol) links_site<T, I, R>(g, f, lp, (I)idx);
   }
 }
 
@@ -83,6 +84,7 @@ struct glasma_batch {
   bool idx32 = true;
   int grid1 = 0, grid2 = 0;
   int launch_mode = GLASMA_BATCH_TILE_GRID;
+  int link_rows = 3;  // 2: 12-real links (FP32), as glasma_set_link_storage
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_dt = NAN;
@@ -109,6 +111,18 @@ glasma::FieldPtrs<T> handle_ptrs(glasma_lattice* h) {
   p.JpStat = static_cast<T*>(h->f[GLASMA_FIELD_JPSTAT]);
   p.JmStat = static_cast<T*>(h->f[GLASMA_FIELD_JMSTAT]);
   return p;
+}
+
+template <typename T, int R>
+void batch_occupancy(const glasma_batch* b, int& per1, int& per2) {
+  using namespace glasma;
+  if (b->idx32) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, int, R>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, int, R>, kThreads, 0);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, long long, R>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, long long, R>, kThreads, 0);
+  }
 }
 
 // (Re)build the device event table for time step dt.
@@ -187,13 +201,12 @@ int build_descriptors(glasma_batch* b, double dt) {
   int dev = 0, sms = 0, per1 = 0, per2 = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (b->idx32) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, int>, kThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, int>, kThreads, 0);
-  } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, long long>, kThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, long long>, kThreads, 0);
-  }
+  bool two_row = false;
+  if constexpr (sizeof(T) == 4) two_row = b->link_rows == 2;
+  if (two_row)
+    batch_occupancy<T, 2>(b, per1, per2);
+  else
+    batch_occupancy<T, 3>(b, per1, per2);
   if (b->launch_mode == GLASMA_BATCH_TILE_GRID && k1 < (1LL << 31) && k2 < (1LL << 31)) {
     b->grid1 = (int)k1;
     b->grid2 = (int)k2;
@@ -205,17 +218,29 @@ int build_descriptors(glasma_batch* b, double dt) {
   return GLASMA_OK;
 }
 
-template <typename T>
-cudaError_t launch_batch_step(glasma_batch* b) {
+template <typename T, int R>
+void launch_batch_rows(glasma_batch* b) {
   using namespace glasma;
   const EventDesc<T>* ev = static_cast<const EventDesc<T>*>(b->d_desc);
   if (b->idx32) {
-    efield_batch_kernel<T, int><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
-    links_batch_kernel<T, int><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total, b->k2_total);
+    efield_batch_kernel<T, int, R><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
+    links_batch_kernel<T, int, R><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total, b->k2_total);
   } else {
-    efield_batch_kernel<T, long long><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
-    links_batch_kernel<T, long long><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total, b->k2_total);
+    efield_batch_kernel<T, long long, R><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
+    links_batch_kernel<T, long long, R><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total,
+                                                                              b->k2_total);
   }
+}
+
+template <typename T>
+cudaError_t launch_batch_step(glasma_batch* b) {
+  if constexpr (sizeof(T) == 4) {
+    if (b->link_rows == 2) {
+      launch_batch_rows<T, 2>(b);
+      return cudaGetLastError();
+    }
+  }
+  launch_batch_rows<T, 3>(b);
   return cudaGetLastError();
 }
 
@@ -223,7 +248,19 @@ cudaError_t reunitarize_all(glasma_batch* b) {
   for (glasma_lattice* h : b->ev) {
     cudaError_t e = b->precision == GLASMA_FP64
                         ? glasma::launch_reunitarize<double>(h->g, static_cast<glasma::cx<double>*>(h->f[GLASMA_FIELD_U]), b->stream)
-                        : glasma::launch_reunitarize<float>(h->g, static_cast<glasma::cx<float>*>(h->f[GLASMA_FIELD_U]), b->stream);
+                        : glasma::launch_reunitarize<float>(h->g, static_cast<glasma::cx<float>*>(h->f[GLASMA_FIELD_U]), b->stream,
+                                                            b->link_rows);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// 12-real links: row 2 of every event's links from rows 0 and 1 (full links between calls).
+cudaError_t complete_all(glasma_batch* b) {
+  if (b->link_rows != 2) return cudaSuccess;
+  for (glasma_lattice* h : b->ev) {
+    cudaError_t e =
+        glasma::launch_complete_links<float>(h->g, static_cast<glasma::cx<float>*>(h->f[GLASMA_FIELD_U]), b->stream);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -382,6 +419,27 @@ int glasma_batch_step(glasma_batch* b, double dt, int nsteps, int use_graph) {
     if ((e = one_step(b)) != cudaSuccess) return bcuda(e, "batch step");
     done++;
   }
+  if ((e = complete_all(b)) != cudaSuccess) return bcuda(e, "complete links");
+  return GLASMA_OK;
+}
+
+int glasma_batch_set_link_storage(glasma_batch* b, int reals_per_link) {
+  if (!b) return bfail(GLASMA_ERR_INVALID_ARGUMENT, "null batch");
+  if (reals_per_link != 18 && reals_per_link != 12)
+    return bfail(GLASMA_ERR_INVALID_ARGUMENT, "reals_per_link must be 18 or 12");
+  if (reals_per_link == 12 && b->precision != GLASMA_FP32)
+    return bfail(GLASMA_ERR_UNSUPPORTED, "12-real links are built for FP32 batches only");
+  const int rows = reals_per_link == 12 ? 2 : 3;
+  if (rows != b->link_rows) {
+    b->link_rows = rows;
+    b->desc_dt = NAN;  // persistent grids are sized for the kernels of this storage
+    if (b->graph) {
+      cudaStreamSynchronize(b->stream);
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
+  for (glasma_lattice* h : b->ev) glasma_set_link_storage(h, reals_per_link);  // events stepped alone
   return GLASMA_OK;
 }
 

@@ -39,6 +39,36 @@ def test_batch_equals_individual_events(precision):
             assert np.array_equal(got[i][k], ref[k]), (i, k)
 
 
+@pytest.mark.parametrize("mode", ["tile_grid", "persistent"])
+def test_batch_links12_equals_individual_events(mode):
+    """12-real links in the batched kernels: bit-identical to each event stepped alone with 12-real
+    links, in both launch modes; full links after the call."""
+    fields = [O.random_fields(N, 340 + i) for i, N in enumerate(SHAPES)]
+    dt, steps = 0.1, 37
+    with Batch(SHAPES, precision="fp32", reunitarize_every=16) as b:
+        b.set_launch(mode)
+        b.set_link_reals(12)
+        tiles = b.autotune(dt)
+        for ev, f in zip(b.events, fields):
+            ev.upload_fields(f)
+        b.step(dt, steps, use_graph=True)
+        got = [ev.download_fields(("U", "E", "Jp", "Jm", "JpStat", "JmStat")) for ev in b.events]
+        umax = max(ev.unitarity()[0] for ev in b.events)
+    assert umax < 1e-5
+    for i, (N, f) in enumerate(zip(SHAPES, fields)):
+        with Lattice(N, precision="fp32", reunitarize_every=16) as lat:
+            lat.link_reals = 12
+            lat.set_tile(tiles[i])
+            lat.upload_fields(f)
+            lat.step(dt, steps, save_uold=False)
+            ref = lat.download_fields(("U", "E", "Jp", "Jm", "JpStat", "JmStat"))
+        for k in ref:
+            assert np.array_equal(got[i][k], ref[k]), (i, k)
+    with Batch(SHAPES, precision="fp64") as b:
+        with pytest.raises(Exception):
+            b.set_link_reals(12)
+
+
 def test_batch_launch_modes_agree():
     """One block per tile and the persistent grid run the same per-site arithmetic."""
     fields = [O.random_fields(N, 330 + i) for i, N in enumerate(SHAPES)]
