@@ -1,10 +1,12 @@
 // batch.cu -- many independent lattices ("events") of uneven sizes advanced together.
 //
 // Each event is an ordinary lattice handle (its own fields, ghost slices, tile shape).  A step of
-// the whole batch is two launches: the electric-field/JStat kernel walks the list of all events'
-// K1 tiles, the link/J kernel the list of all events' 128-site chunks (one block per tile, or a
-// persistent grid that strides through the list); a block finds its event by binary search over the
-// per-event tile offsets.  The per-site arithmetic is the
+// the whole batch is two launches per group of up to kTableEvents events (one group for the
+// 64-event workload): the electric-field/JStat kernel walks the list of the group's K1 tiles, the
+// link/J kernel the list of its 128-site chunks (one block per tile, or a persistent grid that
+// strides through the list); a block finds its event in a tile -> event table.  The group's event
+// descriptors are a __grid_constant__ kernel parameter, read in place from the constant bank.  The
+// per-site arithmetic is the
 // single-lattice kernels' (leapfrog_sites.cuh), so a batched step is bit-identical to stepping
 // every event on its own.  Blocks of steps are captured once into a CUDA graph and replayed.
 // No reference counterpart: the reference farms independent seeds out as separate jobs
@@ -36,34 +38,44 @@ struct EventDesc {
   long long k2_begin;  // first 128-site chunk of this event
 };
 
-// R: rows of each link read and written (3 full, 2 for 12-real links).
-template <typename T, typename I, int R>
+// Event descriptors of one launch group, passed by value: 96 x 280 B (FP64) stays inside the 32 KB
+// kernel-parameter limit.  As __grid_constant__ the table is read in place from the constant bank;
+// the earlier global-memory table, copied into registers per tile, cost the link kernel 452 B of
+// spill stores per thread (116 B in the single-lattice kernel).
+constexpr int kTableEvents = 96;
+template <typename T>
+struct EventTable {
+  EventDesc<T> ev[kTableEvents];
+  int ev0;         // batch index of ev[0]
+  long long t0;    // the group's tiles (K1) or chunks (K2) are [t0, t1) of the batch's list
+  long long t1;
+};
+
+// R: rows of each link read and written (3 full, 2 for 12-real links).  kStride: the persistent grid
+// strides through the tile list; without it each block takes one tile (the tile grid), and the
+// kernel carries no loop state across the site body (FP32 link kernel: 100 B of spill stores
+// instead of 360, none with 12-real links).
+template <typename T, typename I, int R, bool kStride>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
-    efield_batch_kernel(const EventDesc<T>* __restrict__ ev, const unsigned short* __restrict__ tile_ev, long long total) {
+    efield_batch_kernel(const __grid_constant__ EventTable<T> tab, const unsigned short* __restrict__ tile_ev) {
   __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
-  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-    const int e = tile_ev[t];
-    // Local copies: the site body stores through these pointers, so references into the table
-    // would have to be re-read from global memory after every store.
-    const Geometry g = ev[e].g;
-    const FieldPtrs<T> f = ev[e].f;
-    const EParams<T> ep = ev[e].ep;
-    const TileMap tm = ev[e].tm;
+  for (long long t = tab.t0 + blockIdx.x; t < tab.t1; t += gridDim.x) {
+    const EventDesc<T>& d = tab.ev[tile_ev[t] - tab.ev0];
     int x, y, z;
-    if (tm.site(t - ev[e].k1_begin, threadIdx.x, g.nx, g.ny, x, y, z)) efield_site<T, I, R>(g, f, ep, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
+    if (d.tm.site(t - d.k1_begin, threadIdx.x, d.g.nx, d.g.ny, x, y, z))
+      efield_site<T, I, R>(d.g, d.f, d.ep, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
+    if (!kStride) break;
   }
 }
 
-template <typename T, typename I, int R>
+template <typename T, typename I, int R, bool kStride>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
-    links_batch_kernel(const EventDesc<T>* __restrict__ ev, const unsigned short* __restrict__ tile_ev, long long total) {
-  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-    const int e = tile_ev[t];
-    const Geometry g = ev[e].g;
-    const FieldPtrs<T> f = ev[e].f;
-    const LParams<T> lp = ev[e].lp;
-    const long long idx = (t - ev[e].k2_begin) * kThreads + threadIdx.x;
-    if (idx < g.vol) links_site<T, I, R>(g, f, lp, (I)idx);
+    links_batch_kernel(const __grid_constant__ EventTable<T> tab, const unsigned short* __restrict__ tile_ev) {
+  for (long long t = tab.t0 + blockIdx.x; t < tab.t1; t += gridDim.x) {
+    const EventDesc<T>& d = tab.ev[tile_ev[t] - tab.ev0];
+    const long long idx = (t - d.k2_begin) * kThreads + threadIdx.x;
+    if (idx < d.g.vol) links_site<T, I, R>(d.g, d.f, d.lp, (I)idx);
+    if (!kStride) break;
   }
 }
 
@@ -76,13 +88,16 @@ struct glasma_batch {
   int reunit_every = 0;
   long long steps_done = 0;
   cudaStream_t own_stream = nullptr, stream = nullptr;
-  void* d_desc = nullptr;
+  // launch groups of up to kTableEvents events: the K1 and K2 parameter tables and grid sizes
+  std::vector<glasma::EventTable<float>> tab1_f, tab2_f;
+  std::vector<glasma::EventTable<double>> tab1_d, tab2_d;
+  std::vector<int> grid1, grid2;
   unsigned short* d_tile_ev = nullptr;  // event of every K1 tile, then of every K2 chunk
   long long tile_ev_cap = 0;
   double desc_dt = NAN;
   long long k1_total = 0, k2_total = 0;
   bool idx32 = true;
-  int grid1 = 0, grid2 = 0;
+  bool strided = false;  // some group's grid is smaller than its tile list (strided kernels needed)
   int launch_mode = GLASMA_BATCH_TILE_GRID;
   int link_rows = 3;  // 2: 12-real links (FP32), as glasma_set_link_storage
   cudaGraphExec_t graph = nullptr;
@@ -113,15 +128,28 @@ glasma::FieldPtrs<T> handle_ptrs(glasma_lattice* h) {
   return p;
 }
 
+template <typename T>
+std::vector<glasma::EventTable<T>>& tables1(glasma_batch* b);
+template <>
+std::vector<glasma::EventTable<float>>& tables1<float>(glasma_batch* b) { return b->tab1_f; }
+template <>
+std::vector<glasma::EventTable<double>>& tables1<double>(glasma_batch* b) { return b->tab1_d; }
+template <typename T>
+std::vector<glasma::EventTable<T>>& tables2(glasma_batch* b);
+template <>
+std::vector<glasma::EventTable<float>>& tables2<float>(glasma_batch* b) { return b->tab2_f; }
+template <>
+std::vector<glasma::EventTable<double>>& tables2<double>(glasma_batch* b) { return b->tab2_d; }
+
 template <typename T, int R>
 void batch_occupancy(const glasma_batch* b, int& per1, int& per2) {
   using namespace glasma;
   if (b->idx32) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, int, R>, kThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, int, R>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, int, R, true>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, int, R, true>, kThreads, 0);
   } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, long long, R>, kThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, long long, R>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, long long, R, true>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, long long, R, true>, kThreads, 0);
   }
 }
 
@@ -166,11 +194,6 @@ int build_descriptors(glasma_batch* b, double dt) {
   b->k2_total = k2;
   b->swaps.clear();
   for (glasma_lattice* h : b->ev) b->swaps.push_back(h->swaps);
-  const size_t bytes = sizeof(EventDesc<T>) * d.size();
-  if (!b->d_desc) {
-    cudaError_t e = cudaMalloc(&b->d_desc, bytes);
-    if (e != cudaSuccess) return bfail(GLASMA_ERR_OUT_OF_MEMORY, "cudaMalloc event table");
-  }
   // tile -> event table: one load per block instead of a search through the event table
   std::vector<unsigned short> tev((size_t)(k1 + k2));
   for (size_t i = 0; i < d.size(); i++) {
@@ -194,41 +217,72 @@ int build_descriptors(glasma_batch* b, double dt) {
   }
   cudaError_t e = cudaMemcpyAsync(b->d_tile_ev, tev.data(), sizeof(unsigned short) * tev.size(),
                                   cudaMemcpyHostToDevice, b->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_desc, d.data(), bytes, cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return bcuda(e, "event table upload");
   // persistent grids: as many blocks as fit on the device at once
   int dev = 0, sms = 0, per1 = 0, per2 = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  bool two_row = false;
-  if constexpr (sizeof(T) == 4) two_row = b->link_rows == 2;
-  if (two_row)
-    batch_occupancy<T, 2>(b, per1, per2);
-  else
-    batch_occupancy<T, 3>(b, per1, per2);
-  if (b->launch_mode == GLASMA_BATCH_TILE_GRID && k1 < (1LL << 31) && k2 < (1LL << 31)) {
-    b->grid1 = (int)k1;
-    b->grid2 = (int)k2;
+  if constexpr (sizeof(T) == 4) {
+    if (b->link_rows == 2)
+      batch_occupancy<T, 2>(b, per1, per2);
+    else
+      batch_occupancy<T, 3>(b, per1, per2);
   } else {
-    b->grid1 = (int)std::min<long long>(k1, (long long)sms * std::max(per1, 1));
-    b->grid2 = (int)std::min<long long>(k2, (long long)sms * std::max(per2, 1));
+    batch_occupancy<T, 3>(b, per1, per2);
+  }
+  // launch groups of up to kTableEvents consecutive events, each with its own parameter tables
+  std::vector<EventTable<T>>& tab1 = tables1<T>(b);
+  std::vector<EventTable<T>>& tab2 = tables2<T>(b);
+  tab1.clear();
+  tab2.clear();
+  b->grid1.clear();
+  b->grid2.clear();
+  const bool tile_grid = b->launch_mode == GLASMA_BATCH_TILE_GRID;
+  b->strided = false;
+  for (size_t e0 = 0; e0 < d.size(); e0 += kTableEvents) {
+    const size_t e1 = std::min(d.size(), e0 + (size_t)kTableEvents);
+    EventTable<T> t{};
+    for (size_t i = e0; i < e1; i++) t.ev[i - e0] = d[i];
+    t.ev0 = (int)e0;
+    t.t0 = d[e0].k1_begin;
+    t.t1 = e1 < d.size() ? d[e1].k1_begin : k1;
+    tab1.push_back(t);
+    const long long n1 = t.t1 - t.t0;
+    t.t0 = d[e0].k2_begin;
+    t.t1 = e1 < d.size() ? d[e1].k2_begin : k2;
+    tab2.push_back(t);
+    const long long n2 = t.t1 - t.t0;
+    if (tile_grid && n1 < (1LL << 31) && n2 < (1LL << 31)) {
+      b->grid1.push_back((int)n1);
+      b->grid2.push_back((int)n2);
+    } else {
+      b->grid1.push_back((int)std::min<long long>(n1, (long long)sms * std::max(per1, 1)));
+      b->grid2.push_back((int)std::min<long long>(n2, (long long)sms * std::max(per2, 1)));
+      if (tile_grid) b->strided = true;
+    }
   }
   b->desc_dt = dt;
   return GLASMA_OK;
 }
 
+template <typename T, typename I, int R, bool kStride>
+void launch_batch_group(glasma_batch* b, size_t grp) {
+  using namespace glasma;
+  efield_batch_kernel<T, I, R, kStride><<<b->grid1[grp], kThreads, 0, b->stream>>>(tables1<T>(b)[grp], b->d_tile_ev);
+  links_batch_kernel<T, I, R, kStride><<<b->grid2[grp], kThreads, 0, b->stream>>>(tables2<T>(b)[grp],
+                                                                                  b->d_tile_ev + b->k1_total);
+}
+
 template <typename T, int R>
 void launch_batch_rows(glasma_batch* b) {
-  using namespace glasma;
-  const EventDesc<T>* ev = static_cast<const EventDesc<T>*>(b->d_desc);
-  if (b->idx32) {
-    efield_batch_kernel<T, int, R><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
-    links_batch_kernel<T, int, R><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total, b->k2_total);
-  } else {
-    efield_batch_kernel<T, long long, R><<<b->grid1, kThreads, 0, b->stream>>>(ev, b->d_tile_ev, b->k1_total);
-    links_batch_kernel<T, long long, R><<<b->grid2, kThreads, 0, b->stream>>>(ev, b->d_tile_ev + b->k1_total,
-                                                                              b->k2_total);
+  // the tile grid gives every tile its own block, unless a list outgrew a grid dimension
+  const bool stride = b->launch_mode != GLASMA_BATCH_TILE_GRID || b->strided;
+  for (size_t grp = 0; grp < b->grid1.size(); grp++) {
+    if (b->idx32)
+      stride ? launch_batch_group<T, int, R, true>(b, grp) : launch_batch_group<T, int, R, false>(b, grp);
+    else
+      stride ? launch_batch_group<T, long long, R, true>(b, grp) : launch_batch_group<T, long long, R, false>(b, grp);
   }
 }
 
@@ -316,7 +370,6 @@ int glasma_batch_destroy(glasma_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (glasma_lattice* h : b->ev) glasma_destroy(h);
-  if (b->d_desc) cudaFree(b->d_desc);
   if (b->d_tile_ev) cudaFree(b->d_tile_ev);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;

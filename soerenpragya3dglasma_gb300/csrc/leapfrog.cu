@@ -24,9 +24,14 @@ namespace glasma {
 namespace {
 
 // R: rows of each link the kernel reads and writes (3 full, 2 for 12-real links).
+// The parameter structs are __grid_constant__: the site bodies take them by reference, and without
+// the annotation the compiler copies them to each thread's stack (FP32 K1: 208 B of stack, 304 B of
+// spill stores; with it 88 and 104 B, and none at all with 12-real links), read from the constant
+// bank in place instead.
 template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
-    efield_jstat_kernel(Geometry g, FieldPtrs<T> f, EParams<T> p, TileMap tm) {
+    efield_jstat_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> f,
+                        const __grid_constant__ EParams<T> p, const __grid_constant__ TileMap tm) {
   __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   int x, y, z;
   if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
@@ -35,7 +40,8 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kMinBlocks)
 
 template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
-    links_j_kernel(Geometry g, FieldPtrs<T> f, LParams<T> p) {
+    links_j_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> f,
+                   const __grid_constant__ LParams<T> p) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
   if (idx >= (I)g.vol) return;
   links_site<T, I, R>(g, f, p, idx);
@@ -43,7 +49,9 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
 
 template <typename T, typename I, int R>
 __global__ void __launch_bounds__(kThreads, Occupancy<T>::kFusedMinBlocks)
-    fused_step_kernel(Geometry g, FieldPtrs<T> in, FieldPtrs<T> out, EParams<T> pe, LParams<T> pl, TileMap tm) {
+    fused_step_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> in,
+                      const __grid_constant__ FieldPtrs<T> out, const __grid_constant__ EParams<T> pe,
+                      const __grid_constant__ LParams<T> pl, const __grid_constant__ TileMap tm) {
   __shared__ cx<T> sh[StapleShare<T>::kSlots * 9 * kThreads + 1];
   int x, y, z;
   if (!tm.site(blockIdx.x, threadIdx.x, g.nx, g.ny, x, y, z)) return;
