@@ -45,6 +45,10 @@ KERNEL_BYTES = {
     "links_j": {"fp64": 192 + 2 * 432 + 128 + 2 * 128, "fp32": 96 + 2 * 216 + 64 + 2 * 64,
                 "fp32_l12": 96 + 2 * 144 + 64 + 2 * 64},
     "fused_step": {"fp64": 1760, "fp32": 880, "fp32_l12": 736},  # one pass: every per-site array read and written once
+    # plaquette method: K1 as two-pass plus the 48 contribution reals written per site; K2 as two-pass
+    # plus those reals read and E written
+    "plaquette_forces": {"fp64": 1200 + 384, "fp32": 600 + 192, "fp32_l12": 528 + 192},
+    "links_gather": {"fp64": 1440 + 384 + 192, "fp32": 720 + 192 + 96, "fp32_l12": 576 + 192 + 96},
 }
 STEP_BYTES = {"fp64": 1760, "fp32": 880, "fp32_l12": 736}  # every per-site state array read and written once
 FALLBACK_HBM_GBS = 6800.0
@@ -313,9 +317,10 @@ def run_ours(args):
                "algorithmic_bytes_per_launch": alg, "launch_ms": ms}
         # the pipe that actually limits the kernel, from the ncu capture of the same kernel (the FP64
         # kernels sit at ~95 % of GB300's FP64 pipe, which is why their HBM fraction is small)
-        pa = traffic.get("pipe_active", {}).get("%s_%s" % (name, prec))
+        key = "%s_%s" % (name, prec)
+        pa = traffic.get("pipe_active", {}).get(key)
         if pa:
-            out["pipe_active"] = dict(pa, source="profiles/efield_jstat_links_j_64x64x128_ncu.md")
+            out["pipe_active"] = dict(pa, source=traffic.get("sources", {}).get(key))
         return out
 
     def max_over_ranks(x):
@@ -364,6 +369,8 @@ def run_ours(args):
         ms = max_over_ranks(e0.elapsed_time(e1)) / nsteps
         if lat.last_step_method == "one_pass":
             kern = {"fused_step": kms[0] / nsteps}
+        elif lat.last_step_method == "plaquette":
+            kern = {"plaquette_forces": kms[0] / nsteps, "links_gather": kms[1] / nsteps}
         else:
             kern = {"efield_jstat": kms[0] / nsteps, "links_j": kms[1] / nsteps}
         return lat, ms, kern
@@ -900,7 +907,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-gauge", action="store_true", help="skip the gauge-fixing / FFT leg")
-    ap.add_argument("--step-method", default="two_pass", choices=["one_pass", "two_pass"])
+    ap.add_argument("--step-method", default="plaquette", choices=["one_pass", "two_pass", "plaquette"])
     ap.add_argument("--gauge-evolve", type=int, default=40, help="leapfrog steps of the MV state before gauge fixing")
     ap.add_argument("--gauge-iters", type=int, default=300)
     ap.add_argument("--local-gauge-iters", type=int, default=20,

@@ -144,6 +144,12 @@ cudaError_t launch_reunitarize(const Geometry& g, cx<T>* U, cudaStream_t stream,
 // and 1, which returns a two-row array to full matrices for every other kernel.
 template <typename T>
 cudaError_t launch_complete_links(const Geometry& g, cx<T>* U, cudaStream_t stream);
+// One step by the plaquette method: the force kernel over the plaquette owners, then the link kernel
+// gathering their contributions into E.  `contrib` holds 48 S reals; `between` (optional) is recorded
+// between the two launches.
+template <typename T>
+cudaError_t launch_plaquette_step(const Geometry& g, FieldPtrs<T> f, T* contrib, double dt, bool save_uold,
+                                  cudaStream_t stream, cudaEvent_t between, int link_rows = 3);
 
 // Sub-step kernels with the reference's exact sub-step boundaries.
 template <typename T>

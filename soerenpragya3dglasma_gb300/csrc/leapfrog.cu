@@ -58,6 +58,26 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kFusedMinBlocks)
   fused_site<T, I, R>(g, in, out, pe, pl, x, y, z, StapleShare<T>::kSlots ? sh : nullptr);
 }
 
+// The plaquette method (leapfrog_sites.cuh): K1' over the plaquette owners of slices -1 .. Nz-1,
+// K2' gathering the contributions into E before the link update.
+template <typename T, typename I, int R>
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kPlaqMinBlocks)
+    plaquette_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> f, T* __restrict__ C,
+                     const __grid_constant__ EParams<T> p) {
+  const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+  if (idx >= (I)(g.plane * (g.nz + 1))) return;
+  plaquette_site<T, I, R>(g, f, C, p, idx);
+}
+
+template <typename T, typename I, int R>
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
+    links_gather_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> f,
+                        const T* __restrict__ C, const __grid_constant__ LParams<T> p) {
+  const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
+  if (idx >= (I)g.vol) return;
+  links_site<T, I, R, true>(g, f, p, idx, C);
+}
+
 template <typename T, typename I>
 __global__ void __launch_bounds__(kThreads) j_only_kernel(Geometry g, FieldPtrs<T> f, T cj) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
@@ -276,6 +296,33 @@ void launch_links_rows(const Geometry& g, FieldPtrs<T> f, const LParams<T>& p, c
     links_j_kernel<T, long long, R><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
 }
 
+template <typename T, typename I, int R>
+void launch_plaquette_rows(const Geometry& g, FieldPtrs<T> f, T* C, const EParams<T>& pe, const LParams<T>& pl,
+                           cudaStream_t stream, cudaEvent_t between) {
+  plaquette_kernel<T, I, R><<<grid_for(g.plane * (g.nz + 1), kThreads), kThreads, 0, stream>>>(g, f, C, pe);
+  if (between) cudaEventRecord(between, stream);
+  links_gather_kernel<T, I, R><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, C, pl);
+}
+
+template <typename T>
+cudaError_t launch_plaquette_step(const Geometry& g, FieldPtrs<T> f, T* contrib, double dt, bool save_uold,
+                                  cudaStream_t stream, cudaEvent_t between, int link_rows) {
+  const EParams<T> pe = make_eparams<T>(g, dt, 1, 1, 0);
+  const LParams<T> pl = make_lparams<T>(g, dt, save_uold, true, true);
+  // the contribution buffer has 48 S entries: 32-bit offsets only while that fits
+  const bool i32 = g.S * 48 < (1LL << 31) - 1;
+  if constexpr (sizeof(T) == 4) {
+    if (two_row<T>(link_rows)) {
+      i32 ? launch_plaquette_rows<T, int, 2>(g, f, contrib, pe, pl, stream, between)
+          : launch_plaquette_rows<T, long long, 2>(g, f, contrib, pe, pl, stream, between);
+      return cudaGetLastError();
+    }
+  }
+  i32 ? launch_plaquette_rows<T, int, 3>(g, f, contrib, pe, pl, stream, between)
+      : launch_plaquette_rows<T, long long, 3>(g, f, contrib, pe, pl, stream, between);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_links_j(const Geometry& g, FieldPtrs<T> f, double dt, bool save_uold, bool do_j, bool do_second,
                            cudaStream_t stream, int link_rows) {
@@ -350,6 +397,8 @@ cudaError_t launch_copy_links(const Geometry& g, const cx<T>* src, cx<T>* dst, c
   template cudaError_t launch_j_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);                  \
   template cudaError_t launch_reunitarize<T>(const Geometry&, cx<T>*, cudaStream_t, int);                      \
   template cudaError_t launch_complete_links<T>(const Geometry&, cx<T>*, cudaStream_t);                        \
+  template cudaError_t launch_plaquette_step<T>(const Geometry&, FieldPtrs<T>, T*, double, bool, cudaStream_t,  \
+                                                cudaEvent_t, int);                                              \
   template cudaError_t launch_copy_links<T>(const Geometry&, const cx<T>*, cx<T>*, cudaStream_t);              \
   template cudaError_t launch_sync_ghosts<T>(const Geometry&, T*, int, cudaStream_t);                          \
   template cudaError_t launch_sync_ghosts<cx<T>>(const Geometry&, cx<T>*, int, cudaStream_t);

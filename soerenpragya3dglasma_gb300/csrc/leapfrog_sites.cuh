@@ -24,6 +24,9 @@ constexpr int kThreads = 128;
 #ifndef GLASMA_FP32_FUSED_MIN_BLOCKS
 #define GLASMA_FP32_FUSED_MIN_BLOCKS 4
 #endif
+#ifndef GLASMA_FP32_PLAQ_MIN_BLOCKS
+#define GLASMA_FP32_PLAQ_MIN_BLOCKS 4
+#endif
 template <typename T>
 struct Occupancy;
 template <>
@@ -31,12 +34,14 @@ struct Occupancy<double> {
   static constexpr int kMinBlocks = GLASMA_FP64_MIN_BLOCKS;       // electric-field kernel
   static constexpr int kLinksMinBlocks = GLASMA_FP64_MIN_BLOCKS;  // link/J kernel
   static constexpr int kFusedMinBlocks = GLASMA_FP64_MIN_BLOCKS;  // one-pass step kernel
+  static constexpr int kPlaqMinBlocks = GLASMA_FP64_MIN_BLOCKS;   // plaquette-method force kernel
 };
 template <>
 struct Occupancy<float> {
   static constexpr int kMinBlocks = GLASMA_FP32_MIN_BLOCKS;
   static constexpr int kLinksMinBlocks = GLASMA_FP32_LINKS_MIN_BLOCKS;
   static constexpr int kFusedMinBlocks = GLASMA_FP32_FUSED_MIN_BLOCKS;
+  static constexpr int kPlaqMinBlocks = GLASMA_FP32_PLAQ_MIN_BLOCKS;
 };
 
 template <typename I>
@@ -201,6 +206,171 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
   }
 }
 
+// ---- the plaquette method --------------------------------------------------------------------------
+// The force of UpdateElectricFields is a sum over plaquettes: the plaquette P = a b c^d d^d at y in the
+// plane (p, q), p < q (a = U_p(y), b = U_q(y+p), c = U_p(y+q), d = U_q(y)), with al = ReTr(i t P),
+// enters four links, as the upper or lower staple of each (c_mu = cE[mu], gc_mu = gamma c_mu):
+//   link p at y     +gc_p c_q al                      (U_p(y) S_{+q} = P)
+//   link q at y     -gc_q c_p al                      (U_q(y) S_{+p} = P^d)
+//   link p at y+q   -gc_p c_q InvAdj(d, al)           (U_p(y+q) S_{-q} = d^d P^d d)
+//   link q at y+p   +gc_q c_p InvAdj(a, al)           (U_q(y+p) S_{-p} = a^d P a)
+// using ReTr(i t X^d) = -ReTr(i t X) and ReTr(i t^a V^d X V) = InvAdj(V, ReTr(i t X))_a, the SU(3)
+// InverseAdjointMultiplication.  The same terms as the staple form (K1), regrouped: three plaquettes
+// (three products each) and six adjoint rotations per site instead of twelve staples (two products
+// each, three shared) and three final products: ~18 instead of ~24 matrix products per site.
+// K1' (plaquette_site) runs one thread per plaquette owner y, slices -1 .. Nz-1 (the ghost slice owns
+// the plaquettes whose lower-staple terms reach slice 0): it adds the first two terms and the current
+// source to E at y and stores the last two, already weighted, in a contribution buffer at y.  K2'
+// (links_site with kGather) adds the two contributions each link receives, from y = x-q and x-p, to
+// E before it exponentiates it.  Contribution slots C[(slot*8 + a)*S + y]:
+enum ContribSlot {
+  kC01p = 0,  // plane (0,1), to link 1 at y+x
+  kC01q = 1,  // plane (0,1), to link 0 at y+y
+  kC02p = 2,  // plane (0,2), to link 2 at y+x
+  kC02q = 3,  // plane (0,2), to link 0 at y+z
+  kC12p = 4,  // plane (1,2), to link 2 at y+y
+  kC12q = 5,  // plane (1,2), to link 1 at y+z
+  kCSlots = 6
+};
+
+template <typename T>
+__device__ __forceinline__ void scale_alg(T w, Alg<T>& v) {
+#pragma unroll
+  for (int k = 0; k < 8; k++) v.a[k] *= w;
+}
+
+// al = ReTr(i t^a a b c^d d^d)
+template <typename T>
+__device__ __forceinline__ void plaquette_alg(const Mat<T>& a, const Mat<T>& b, const Mat<T>& c, const Mat<T>& d,
+                                              Alg<T>& al) {
+  Mat<T> ab, dc, P;
+  mul_nn(a, b, ab);
+  mul_nn(d, c, dc);
+  mul_nd_traceless(ab, dc, P);
+  retr_itg(P, T(1), al);
+}
+
+// K1' per owner site: idx = owner site s (slice -1 starts at s = 0); covers (Nz+1) slices.
+template <typename T, typename I, int R>
+__device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtrs<T>& f, T* __restrict__ C,
+                                               const EParams<T>& p, I idx) {
+  const I S = (I)g.S, plane = (I)g.plane;
+  const I s = idx;
+  const int zz = (int)(idx / plane);
+  const int z = zz - 1;
+  const int r = (int)(idx - (I)zz * plane);
+  const int y = r / g.nx, x = r - y * g.nx;
+  const bool interior = z >= 0;
+  const bool below_top = z < g.nz - 1;  // y+z is an interior site
+  const I sxp = nb<I>(g, x, y, z, 1, 0, 0), syp = nb<I>(g, x, y, z, 0, 1, 0), szp = s + plane;
+  const T w01p = p.gc[0] * p.cnu[1], w01q = p.gc[1] * p.cnu[0];  // wp = gc_p c_q, wq = gc_q c_p
+  const T w02p = p.gc[0] * p.cnu[2], w02q = p.gc[2] * p.cnu[0];
+  const T w12p = p.gc[1] * p.cnu[2], w12q = p.gc[2] * p.cnu[1];
+  Alg<T> F0, F1, F2, al, out;
+  Mat<T> u0, u1, u2, b, c;
+  load_link_r<R>(f.U, S, 0, s, u0);
+  load_link_r<R>(f.U, S, 1, s, u1);
+  load_link_r<R>(f.U, S, 2, s, u2);
+  if (interior) {
+    // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
+    load_link_r<R>(f.U, S, 1, sxp, b);
+    load_link_r<R>(f.U, S, 0, syp, c);
+    plaquette_alg(u0, b, c, u1, al);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      F0.a[k] = w01p * al.a[k];
+      F1.a[k] = -w01q * al.a[k];
+    }
+    inv_adj_mul(u1, al, out);  // to link 0 at y+y
+    scale_alg(-w01p, out);
+    if (!p.dry) store_alg(C, S, kC01q * 8, s, out);
+    inv_adj_mul(u0, al, out);  // to link 1 at y+x
+    scale_alg(w01q, out);
+    if (!p.dry) store_alg(C, S, kC01p * 8, s, out);
+  }
+  // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
+  load_link_r<R>(f.U, S, 2, sxp, b);
+  load_link_r<R>(f.U, S, 0, szp, c);
+  plaquette_alg(u0, b, c, u2, al);
+  if (below_top) {
+    inv_adj_mul(u2, al, out);  // to link 0 at y+z
+    scale_alg(-w02p, out);
+    if (!p.dry) store_alg(C, S, kC02q * 8, s, out);
+  }
+  if (interior) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      F0.a[k] += w02p * al.a[k];
+      F2.a[k] = -w02q * al.a[k];
+    }
+    inv_adj_mul(u0, al, out);  // to link 2 at y+x
+    scale_alg(w02q, out);
+    if (!p.dry) store_alg(C, S, kC02p * 8, s, out);
+  }
+  // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
+  load_link_r<R>(f.U, S, 2, syp, b);
+  load_link_r<R>(f.U, S, 1, szp, c);
+  plaquette_alg(u1, b, c, u2, al);
+  if (below_top) {
+    inv_adj_mul(u2, al, out);  // to link 1 at y+z
+    scale_alg(-w12p, out);
+    if (!p.dry) store_alg(C, S, kC12q * 8, s, out);
+  }
+  if (!interior) return;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    F1.a[k] += w12p * al.a[k];
+    F2.a[k] -= w12q * al.a[k];
+  }
+  inv_adj_mul(u1, al, out);  // to link 2 at y+y
+  scale_alg(w12q, out);
+  if (!p.dry) store_alg(C, S, kC12p * 8, s, out);
+  // E += the forces of the plaquettes owned here (+ the current source on E_z); K2' adds the rest
+  Alg<T> e;
+  load_alg(f.E, S, 0, s, e);
+#pragma unroll
+  for (int k = 0; k < 8; k++) e.a[k] += F0.a[k];
+  if (!p.dry) store_alg(f.E, S, 0, s, e);
+  load_alg(f.E, S, 8, s, e);
+#pragma unroll
+  for (int k = 0; k < 8; k++) e.a[k] += F1.a[k];
+  if (!p.dry) store_alg(f.E, S, 8, s, e);
+  {
+    Alg<T> jp, jm;
+    load_alg(f.E, S, 16, s, e);
+    load_alg(f.Jp, S, 0, s, jp);
+    load_alg(f.Jm, S, 0, s, jm);
+#pragma unroll
+    for (int k = 0; k < 8; k++) e.a[k] += F2.a[k] + p.jz * (jp.a[k] - jm.a[k]);
+    if (!p.dry) store_alg(f.E, S, 16, s, e);
+  }
+  // UpdateJStat, as K1
+  const bool lo = (z == 0), hi = (z == g.nz - 1);
+  const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
+  const I szm = s - plane;
+  Mat<T> uzm;
+  load_link_r<R>(f.U, S, 2, szm, uzm);
+  Alg<T> down, jc, st;
+  load_alg(f.Jp, S, 0, szm, jc);
+  inv_adj_mul(uzm, jc, down);
+  load_alg(f.Jp, S, 0, s, jc);
+  load_alg(f.JpStat, S, 0, s, st);
+  axpy_diff(st, -p.cj, jc, down);
+  if (!p.dry) {
+    store_alg(f.JpStat, S, 0, s, st);
+    if (sg >= 0) store_alg(f.JpStat, S, 0, sg, st);
+  }
+  load_alg(f.Jm, S, 0, szm, jc);
+  inv_adj_mul(uzm, jc, down);
+  load_alg(f.Jm, S, 0, s, jc);
+  load_alg(f.JmStat, S, 0, s, st);
+  axpy_diff(st, p.cj, jc, down);
+  if (!p.dry) {
+    store_alg(f.JmStat, S, 0, s, st);
+    if (sg >= 0) store_alg(f.JmStat, S, 0, sg, st);
+  }
+}
+
 // Thread-to-site map of K1: a block of kThreads threads covers a tile of tile_x x (kThreads/tile_x)
 // sites of one z slice, so most y-neighbours a block reads are its own sites (L1 hits).
 struct TileMap {
@@ -233,18 +403,43 @@ struct LParams {
   int save_uold, do_j, do_second;
 };
 
-// K2's per-site body: links to t+dt (two applications of one exp), UOld, J transport.
-template <typename T, typename I, int R = 3>
-__device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>& f, const LParams<T>& p, I idx) {
+// K2's per-site body: links to t+dt (two applications of one exp), UOld, J transport.  kGather (the
+// plaquette method): first E_mu += the two contributions link mu receives from the plaquette owners
+// x-nu (see plaquette_site), stored with its ghost copy.
+template <typename T, typename I, int R = 3, bool kGather = false>
+__device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>& f, const LParams<T>& p, I idx,
+                                           const T* __restrict__ C = nullptr) {
   const I S = (I)g.S, plane = (I)g.plane;
   const I s = idx + plane;
   const int z = (int)(idx / plane);
   const bool lo = (z == 0), hi = (z == g.nz - 1);
   const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
+  I sxm = 0, sym = 0;
+  if constexpr (kGather) {
+    const int r = (int)(idx - (I)z * plane);
+    const int y = r / g.nx, x = r - y * g.nx;
+    sxm = nb<I>(g, x, y, z, -1, 0, 0);
+    sym = nb<I>(g, x, y, z, 0, -1, 0);
+  }
 #pragma unroll 1
   for (int mu = 0; mu < 3; mu++) {
     Alg<T> e;
     load_alg(f.E, S, mu * 8, s, e);
+    if constexpr (kGather) {
+      // link 0: from (0,1) at x-y and (0,2) at x-z; link 1: (0,1) at x-x, (1,2) at x-z;
+      // link 2: (0,2) at x-x, (1,2) at x-y
+      const I s1 = mu == 0 ? sym : sxm;
+      const I s2 = mu == 2 ? sym : s - plane;
+      const int c1 = mu == 0 ? kC01q : (mu == 1 ? kC01p : kC02p);
+      const int c2 = mu == 0 ? kC02q : (mu == 1 ? kC12q : kC12p);
+      Alg<T> a1, a2;
+      load_alg(C, S, c1 * 8, s1, a1);
+      load_alg(C, S, c2 * 8, s2, a2);
+#pragma unroll
+      for (int k = 0; k < 8; k++) e.a[k] += a1.a[k] + a2.a[k];
+      store_alg(f.E, S, mu * 8, s, e);
+      if (sg >= 0) store_alg(f.E, S, mu * 8, sg, e);
+    }
     Mat<T> X, u, uh;
     load_link_r<R>(f.U, S, mu, s, u);
     // Without a use for U(t+dt/2) (UOld, the z-link J transport), the two half steps are one:

@@ -294,6 +294,28 @@ __device__ __forceinline__ void mul_nn_traceless(const Mat<T>& A, const Mat<T>& 
     }
 }
 
+// The entries of C = A B^dagger that retr_itg reads (as mul_nn_traceless, for mul_nd).
+template <typename T>
+__device__ __forceinline__ void mul_nd_traceless(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          acc.im = fma(-A.e[i + 3 * k].re, B.e[j + 3 * k].im, acc.im);
+          acc.im = fma(A.e[i + 3 * k].im, B.e[j + 3 * k].re, acc.im);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma_nc(acc, A.e[i + 3 * k], B.e[j + 3 * k]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+}
+
 template <typename T>
 struct Trig;
 template <>

@@ -222,11 +222,13 @@ class Lattice:
     def step(self, dt, nsteps=1, save_uold=True):
         check(self.lib.glasma_step(self.h, float(dt), int(nsteps), _lib.STEP_SAVE_UOLD if save_uold else 0))
 
-    STEP_METHODS = {"one_pass": 0, "two_pass": 1}
+    STEP_METHODS = {"one_pass": 0, "two_pass": 1, "plaquette": 2}
 
     def set_step_method(self, method):
-        """"two_pass" (default: two kernels per step, in place) or "one_pass" (one kernel per step over
-        two buffer sets, half the HBM traffic).  Both give bit-identical fields."""
+        """"plaquette" (default: the electric force summed plaquette by plaquette, two kernels and a
+        contribution buffer), "two_pass" (two kernels per step, in place, staple form) or "one_pass"
+        (one kernel per step over two buffer sets; bit-identical to two_pass).  The plaquette method
+        equals the other two up to rounding."""
         check(self.lib.glasma_set_step_method(self.h, self.STEP_METHODS[method]))
 
     @property

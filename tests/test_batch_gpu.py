@@ -30,6 +30,7 @@ def test_batch_equals_individual_events(precision):
         energies = b.energy()
     for i, (N, f) in enumerate(zip(SHAPES, fields)):
         with Lattice(N, precision=precision, reunitarize_every=16) as lat:
+            lat.set_step_method("two_pass")  # the batched kernels are the two-pass (staple) kernels
             lat.set_tile(tiles[i])
             lat.upload_fields(f)
             lat.step(dt, steps, save_uold=False)
@@ -57,6 +58,7 @@ def test_batch_links12_equals_individual_events(mode):
     assert umax < 1e-5
     for i, (N, f) in enumerate(zip(SHAPES, fields)):
         with Lattice(N, precision="fp32", reunitarize_every=16) as lat:
+            lat.set_step_method("two_pass")
             lat.link_reals = 12
             lat.set_tile(tiles[i])
             lat.upload_fields(f)
@@ -101,6 +103,7 @@ def test_batch_after_events_stepped_alone():
         got = [ev.download_fields(("U", "E", "Jp", "Jm", "JpStat", "JmStat")) for ev in b.events]
     for i, (N, f) in enumerate(zip(SHAPES, fields)):
         with Lattice(N) as lat:
+            lat.set_step_method("two_pass")
             lat.upload_fields(f)
             lat.step(dt, 2, save_uold=False)
             if i in (1, 2):

@@ -62,13 +62,16 @@ def test_pinned_host_buffers_give_the_same_bytes(precision):
             assert np.array_equal(out_pinned.numpy(), out_pageable.view(np.float64).reshape(out_pinned.shape)), k
 
 
+@pytest.mark.parametrize("method", ["two_pass", "plaquette"])
 @pytest.mark.parametrize("tag,nsteps", [("s1", 1), ("s10", 10)])
-def test_leapfrog_matches_reference_golden(golden_dir, tag, nsteps):
+def test_leapfrog_matches_reference_golden(golden_dir, tag, nsteps, method):
     g = _load(golden_dir, "leapfrog_random.npz")
     N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
     init = {k: g["init_" + k] for k in FIELDS}
     with _gpu(init, N, a) as lat:
+        lat.set_step_method(method)
         lat.step(dt, nsteps)
+        assert lat.last_step_method == method
         out = lat.download_fields()
         for k in FIELDS:
             assert _rel(out[k], g[tag + "_" + k]) < 1e-12, k
@@ -83,11 +86,13 @@ def test_leapfrog_matches_reference_golden(golden_dir, tag, nsteps):
 @pytest.mark.parametrize("N,a,dt,seed", [((6, 5, 8), (1.0, 1.0, 1.0), 0.125, 11),
                                          ((8, 8, 16), (1.0, 1.1, 0.5), 0.05, 12),
                                          ((3, 7, 2), (1.0, 1.0, 1.0), 0.1, 13)])
-def test_leapfrog_matches_oracle(oracle, N, a, dt, seed):
+@pytest.mark.parametrize("method", ["two_pass", "plaquette"])
+def test_leapfrog_matches_oracle(oracle, N, a, dt, seed, method):
     f = O.random_fields(N, seed)
     ref = O.copy_fields(f)
     oracle.update(ref, N, a, dt, 5)
     with _gpu(f, N, a) as lat:
+        lat.set_step_method(method)
         lat.step(dt, 5)
         out = lat.download_fields()
     for k in FIELDS:
@@ -112,6 +117,27 @@ def test_one_pass_equals_two_pass_bit_exact(precision, N):
         assert np.array_equal(outs[0][k], outs[1][k]), k
 
 
+@pytest.mark.parametrize("precision,reals", [("fp64", 18), ("fp32", 18), ("fp32", 12)])
+@pytest.mark.parametrize("N", [(6, 5, 8), (3, 7, 2), (16, 8, 4)])
+def test_plaquette_method_equals_two_pass(precision, reals, N):
+    """The plaquette method sums the same force terms in another order: every field, ghost slices
+    included, equal to the two-pass step up to rounding (FP64 1e-13; FP32 2e-5 after 7 steps of hot
+    random links)."""
+    f = O.random_fields(N, 23)
+    kw = dict(reunitarize_every=3) if precision == "fp32" else {}
+    outs = []
+    for method in ("plaquette", "two_pass"):
+        with _gpu(f, N, (1.0, 1.1, 0.9), precision=precision, **kw) as lat:
+            lat.link_reals = reals
+            lat.set_step_method(method)
+            lat.step(0.1, 7, save_uold=True)
+            assert lat.last_step_method == method
+            outs.append(lat.download_fields())
+    tol = 1e-13 if precision == "fp64" else 2e-5
+    for k in FIELDS:
+        assert _rel(outs[0][k], outs[1][k]) < tol, k
+
+
 def test_step_method_switch_mid_run(oracle):
     """Odd and even step counts with each method, switching between calls, still follow the oracle."""
     N, dt = (6, 6, 10), 0.1
@@ -119,11 +145,14 @@ def test_step_method_switch_mid_run(oracle):
     ref = O.copy_fields(f)
     oracle.update(ref, N, (1.0, 1.0, 1.0), dt, 3, save_uold=False)
     oracle.update(ref, N, (1.0, 1.0, 1.0), dt, 2, save_uold=False)
+    oracle.update(ref, N, (1.0, 1.0, 1.0), dt, 1, save_uold=False)
     oracle.update(ref, N, (1.0, 1.0, 1.0), dt, 1, save_uold=True)
     with _gpu(f, N, (1.0, 1.0, 1.0)) as lat:
         lat.step(dt, 3, save_uold=False)
         lat.set_step_method("two_pass")
         lat.step(dt, 2, save_uold=False)
+        lat.set_step_method("plaquette")
+        lat.step(dt, 1, save_uold=False)
         lat.set_step_method("one_pass")
         lat.step(dt, 1, save_uold=True)
         out = lat.download_fields()
@@ -271,7 +300,8 @@ def test_mv_init_matches_reference_golden(golden_dir):
         assert np.allclose(lat.bulk(), g["t0_bulk"], rtol=1e-10, atol=1e-11)
 
 
-def test_fp32_tracks_fp64_on_a_weak_field_collision():
+@pytest.mark.parametrize("method", ["two_pass", "plaquette"])
+def test_fp32_tracks_fp64_on_a_weak_field_collision(method):
     """An MV collision has dilute regions where the links sit within ~1e-5 of the identity: there FP32
     rounding of the link exponential, of the link stores and of the reunitarisation used to bias the
     state (energy 0.5 % off after a few hundred steps).  From the same FP32-rounded start, FP32 with
@@ -287,6 +317,7 @@ def test_fp32_tracks_fp64_on_a_weak_field_collision():
     out = {}
     for prec in ("fp64", "fp32"):
         with Lattice(N, precision=prec, reunitarize_every=16 if prec == "fp32" else 0) as lat:
+            lat.set_step_method(method)
             lat.upload_fields(f32)
             lat.step(dt, steps, save_uold=False)
             out[prec] = (lat.bulk()[9], lat.unitarity()[0])
