@@ -316,6 +316,28 @@ __device__ __forceinline__ void mul_nd_traceless(const Mat<T>& A, const Mat<T>& 
     }
 }
 
+// The entries of C = A^dagger B that retr_itg reads (as mul_nn_traceless, for mul_dn).
+template <typename T>
+__device__ __forceinline__ void mul_dn_traceless(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<T> acc = mk<T>(0, 0);
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {  // Im conj(A_ki) B_ki
+          acc.im = fma(A.e[k + 3 * i].re, B.e[k + 3 * j].im, acc.im);
+          acc.im = fma(-A.e[k + 3 * i].im, B.e[k + 3 * j].re, acc.im);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma_cn(acc, A.e[k + 3 * i], B.e[k + 3 * j]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+}
+
 template <typename T>
 struct Trig;
 template <>
