@@ -116,11 +116,13 @@ int glasma_upload_finish(glasma_lattice* h);
 int glasma_download_device(glasma_lattice* h, int field, double* device_aos);
 
 /* nsteps x Dynamics::SUNc::Update (S/DYNAMICS/SUNcDynamics.cpp:353-378) with time step dt.
- * With the two-pass method (the default) the electric-field/JStat sub-steps and the link/J
- * sub-steps are two kernels working in place; with the one-pass method each step is one kernel
- * that reads the links and currents of time t from one set of buffers and writes those of t+dt
- * to a second set, which the handle allocates on first use and swaps with the first after every
- * step.  Both give bit-identical fields.  SaveOldLink runs when GLASMA_STEP_SAVE_UOLD is set (for
+ * With the plaquette method (the default) a force kernel over the plaquettes and a link/J kernel
+ * that gathers their contributions into E run per step (equal to the staple form up to rounding);
+ * with the two-pass method the electric-field/JStat sub-steps and the link/J sub-steps are two
+ * kernels working in place; with the one-pass method each step is one kernel that reads the links
+ * and currents of time t from one set of buffers and writes those of t+dt to a second set, which
+ * the handle allocates on first use and swaps with the first after every step.  Two-pass and
+ * one-pass give bit-identical fields.  SaveOldLink runs when GLASMA_STEP_SAVE_UOLD is set (for
  * the last step of the call, which leaves UOld exactly as the reference leaves it). */
 int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags);
 
