@@ -298,7 +298,9 @@ int glasma_fill_synthetic(glasma_lattice* h, unsigned long long seed, double lin
 /* Autotuner: times the step kernel of the handle's step method (the one-pass kernel, or the
  * electric-field kernel of the two-pass method), computing and storing nothing, for each block
  * tile shape tile_x x (128/tile_x) sites of a z slice and keeps the fastest for this lattice;
- * *tile_x (may be NULL) receives it.  glasma_set_tile sets it by hand (tile_x divides 128). */
+ * *tile_x (may be NULL) receives it.  The plaquette method's kernels are pointwise: for it the
+ * current tile is kept and reported without timing.  glasma_set_tile sets it by hand (tile_x
+ * divides 128). */
 int glasma_autotune(glasma_lattice* h, double dt, int* tile_x);
 int glasma_set_tile(glasma_lattice* h, int tile_x);
 

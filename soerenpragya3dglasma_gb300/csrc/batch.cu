@@ -403,7 +403,7 @@ int glasma_batch_autotune(glasma_batch* b, double dt, int* tiles) {
     auto it = chosen.find(key);
     int tx = 0;
     if (it == chosen.end()) {
-      int st = glasma_autotune(h, dt, &tx);
+      int st = glasma_autotune_staple(h, dt, &tx);
       if (st != GLASMA_OK) return st;
       chosen[key] = tx;
     } else {

@@ -919,6 +919,15 @@ int glasma_fft3d_f32(glasma_lattice* h, const float* in, float* out, int inverse
 
 int glasma_autotune(glasma_lattice* h, double dt, int* tile_x) {
   GLASMA_CHECK_HANDLE(h);
+  if (h->step_method == GLASMA_STEP_PLAQUETTE) {  // its kernels are pointwise: no tile to choose
+    if (tile_x) *tile_x = h->tile_x;
+    return GLASMA_OK;
+  }
+  return glasma_autotune_staple(h, dt, tile_x);
+}
+
+int glasma_autotune_staple(glasma_lattice* h, double dt, int* tile_x) {
+  GLASMA_CHECK_HANDLE(h);
   const int candidates[5] = {128, 64, 32, 16, 8};
   cudaEvent_t e0, e1;
   GLASMA_CUDA(cudaEventCreate(&e0), "cudaEventCreate");

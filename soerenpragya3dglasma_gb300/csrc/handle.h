@@ -37,6 +37,10 @@ struct glasma_lattice {
   unsigned pending;          // fields begun and not yet finished (bit per glasma_field)
 };
 
+// The autotuner of the staple kernels whatever the handle's step method (batches step their events
+// with the staple kernels).
+extern "C" int glasma_autotune_staple(glasma_lattice* h, double dt, int* tile_x);
+
 namespace glasma {
 // Default K1 tile width: the widest power of two dividing the block that does not exceed Nx.
 inline int default_tile_x(int nx) {
