@@ -295,6 +295,8 @@ def run_ours(args):
                       stream=stream)
         lat.set_step_method(args.step_method)
         lat.link_reals = link_reals
+        if precision == "fp64":
+            lat.fp64_arithmetic = args.fp64_arith
         for k in INPUT_FIELDS:
             lat.upload_device(k, inputs[k].data_ptr())
         lat.upload_device("UOld", inputs["U"].data_ptr())
@@ -615,6 +617,7 @@ def run_ours(args):
         # per step: the one-pass kernel (or K1 + K2); per step() call: one ghost-slice sync
         "gpu_launches": (1 if "fused_step" in (k_ms or {}) else 2) * args.steps + 1,
         "step_method": args.step_method,
+        "fp64_arithmetic": args.fp64_arith,
         "tiles": tiles,
     }
     print(json.dumps(line), flush=True)
@@ -908,6 +911,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-gauge", action="store_true", help="skip the gauge-fixing / FFT leg")
     ap.add_argument("--step-method", default="plaquette", choices=["one_pass", "two_pass", "plaquette"])
+    ap.add_argument("--fp64-arith", default="native", choices=["native", "double_float"],
+                    help="arithmetic of the FP64 plaquette force kernel")
     ap.add_argument("--gauge-evolve", type=int, default=40, help="leapfrog steps of the MV state before gauge fixing")
     ap.add_argument("--gauge-iters", type=int, default=300)
     ap.add_argument("--local-gauge-iters", type=int, default=20,

@@ -149,6 +149,15 @@ int glasma_get_step_method(glasma_lattice* h, int* method);
  * kernels are bound by the FP64 pipe, which the reconstruction would load further).
  * No reference counterpart (the reference stores full links, S/LATTICE/GaugeLinks.cpp). */
 int glasma_set_link_storage(glasma_lattice* h, int reals_per_link);
+
+/* Arithmetic of the plaquette method's force kernel on FP64 handles: GLASMA_FP64_NATIVE (default) or
+ * GLASMA_FP64_DOUBLE_FLOAT, double-float arithmetic on the FP32 pipe (each value an unevaluated sum of
+ * two floats, ~48-bit significand; the FP64 fields are converted on load and store).  GB300 runs FP64
+ * at 1/64 of its FP32 rate.  Ignored by FP32 handles and the other step methods. */
+#define GLASMA_FP64_NATIVE 0
+#define GLASMA_FP64_DOUBLE_FLOAT 1
+int glasma_set_fp64_arithmetic(glasma_lattice* h, int mode);
+int glasma_get_fp64_arithmetic(glasma_lattice* h, int* mode);
 int glasma_get_link_storage(glasma_lattice* h, int* reals_per_link);
 
 /* glasma_step with CUDA events recorded on the handle's stream around the kernels of every

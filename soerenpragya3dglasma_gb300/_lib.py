@@ -52,6 +52,8 @@ SIGNATURES = [
     ("glasma_set_step_method", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_get_step_method", ctypes.c_int, [_H, _I]),
     ("glasma_set_link_storage", ctypes.c_int, [_H, ctypes.c_int]),
+    ("glasma_set_fp64_arithmetic", ctypes.c_int, [_H, ctypes.c_int]),
+    ("glasma_get_fp64_arithmetic", ctypes.c_int, [_H, _I]),
     ("glasma_get_link_storage", ctypes.c_int, [_H, _I]),
     ("glasma_update_efield", ctypes.c_int, [_H, ctypes.c_double]),
     ("glasma_update_jstat", ctypes.c_int, [_H, ctypes.c_double]),

@@ -1,0 +1,159 @@
+// ddf.cuh -- double-float ("float-float") arithmetic: a value is the unevaluated sum hi + lo of two
+// FP32 numbers (|lo| <= ulp(hi)/2, ~48-bit significand).  GB300's FP64 pipe runs at 1/64 of its FP32
+// rate, so FP64-grade arithmetic built from FP32 instructions (~15 per fused multiply-add) is several
+// times faster for the FP64 step's matrix products (3.97x on chained 3x3 complex products, measured).
+// Algorithms: Dekker's product (TwoProd, here exact by FMA) and Knuth's TwoSum, with a Fast2Sum
+// renormalisation (Dekker, Numer. Math. 18 (1971) 224; Knuth, TAOCP vol. 2, 4.2.2).
+// The operators below let the templated SU(3) arithmetic of su3.cuh run on ddf unchanged.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "su3.cuh"
+
+namespace glasma {
+
+using ::fma;  // the native overloads stay visible beside fma(ddf, ddf, ddf) below
+
+struct ddf {
+  float hi, lo;
+  ddf() = default;
+  // from a double: hi its nearest float, lo the nearest float to the remainder (constants fold)
+  // explicit: a double never becomes a ddf silently (glasma::fma(ddf, ddf, ddf) must not capture
+  // the FP64 code's fma calls)
+  __host__ __device__ __forceinline__ explicit ddf(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  __host__ __device__ __forceinline__ ddf(float h, float l) : hi(h), lo(l) {}
+};
+
+// Bit-level conversions, so that moving FP64 fields in and out of double-float costs no FP64
+// instruction but the one addition of a store (GB300's conversions between FP64 and FP32 run at the
+// FP64 rate).
+__host__ __device__ __forceinline__ unsigned long long ddf_bits64(double d) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(d);
+#else
+  unsigned long long b;
+  __builtin_memcpy(&b, &d, 8);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ double ddf_double_from_bits(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  __builtin_memcpy(&d, &b, 8);
+  return d;
+#endif
+}
+__host__ __device__ __forceinline__ unsigned ddf_bits32(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  unsigned b;
+  __builtin_memcpy(&b, &f, 4);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ float ddf_float_from_bits(unsigned b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float f;
+  __builtin_memcpy(&f, &b, 4);
+  return f;
+#endif
+}
+
+// d = head + tail: head = the leading 24 bits of d's significand (exponent rebiased), tail = the
+// remaining 29 bits as t 2^(e-1075), rounded to a float; then renormalised (Fast2Sum).  Outside
+// 2^-74 <= |d| < 2^128 (zero, tiny, huge, inf, nan) the FP64 conversion is used instead.
+__host__ __device__ __forceinline__ ddf ddf_from_double(double d) {
+  const unsigned long long b = ddf_bits64(d);
+  const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
+  const int e = (int)((hi32 >> 20) & 0x7ffu);  // biased exponent
+  if (e < 949 || e > 1150) return ddf(d);
+  const unsigned sign = hi32 & 0x80000000u;
+  const unsigned top23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+  const float head = ddf_float_from_bits(sign | ((unsigned)(e - 896) << 23) | top23);
+  const float scale = ddf_float_from_bits((unsigned)(e - 948) << 23);  // 2^(e - 1075)
+  float tail = (float)(lo32 & 0x1fffffffu) * scale;
+  tail = sign ? -tail : tail;
+  const float h = head + tail;
+  return ddf(h, tail - (h - head));
+}
+// exact float -> double by bits (normal floats; zero, subnormal, inf and nan by conversion)
+__host__ __device__ __forceinline__ double ddf_widen(float x) {
+  const unsigned u = ddf_bits32(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 255u) return (double)x;
+  return ddf_double_from_bits(((unsigned long long)(u & 0x80000000u) << 32) |
+                              ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29));
+}
+__host__ __device__ __forceinline__ double to_double(ddf a) { return ddf_widen(a.hi) + ddf_widen(a.lo); }
+
+// s = a + b exactly as s.hi + s.lo (TwoSum), then the low parts, then renormalised
+__device__ __forceinline__ ddf operator+(ddf a, ddf b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  const float hi = s + e;
+  return ddf(hi, e - (hi - s));
+}
+__device__ __forceinline__ ddf operator-(ddf a) { return ddf(-a.hi, -a.lo); }
+__device__ __forceinline__ ddf operator-(ddf a, ddf b) { return a + (-b); }
+// a b: the exact product of the high parts by FMA, plus the cross terms (lo*lo is below the precision)
+__device__ __forceinline__ ddf operator*(ddf a, ddf b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float hi = p + e;
+  return ddf(hi, e - (hi - p));
+}
+// c + a b with one renormalisation
+__device__ __forceinline__ ddf fma(ddf a, ddf b, ddf c) {
+  const float p = a.hi * b.hi;
+  float pe = fmaf(a.hi, b.hi, -p);
+  pe = fmaf(a.hi, b.lo, pe);
+  pe = fmaf(a.lo, b.hi, pe);
+  const float s = c.hi + p;
+  const float bb = s - c.hi;
+  float e = (c.hi - (s - bb)) + (p - bb);
+  e += c.lo + pe;
+  const float hi = s + e;
+  return ddf(hi, e - (hi - s));
+}
+__device__ __forceinline__ ddf& operator+=(ddf& a, ddf b) { return a = a + b; }
+__device__ __forceinline__ ddf& operator-=(ddf& a, ddf b) { return a = a - b; }
+__device__ __forceinline__ ddf& operator*=(ddf& a, ddf b) { return a = a * b; }
+
+// storage type <-> compute type
+template <typename TC, typename T>
+__device__ __forceinline__ TC to_compute(T x) {
+  if constexpr (std::is_same<TC, ddf>::value && std::is_same<T, double>::value)
+    return ddf_from_double(x);
+  else
+    return TC(x);
+}
+template <typename T>
+__device__ __forceinline__ T from_compute(T x) {
+  return x;
+}
+template <typename T>
+__device__ __forceinline__ T from_compute(ddf x);
+template <>
+__device__ __forceinline__ double from_compute<double>(ddf x) {
+  return to_double(x);
+}
+
+template <>
+struct Consts<ddf> {
+  static __device__ __forceinline__ ddf inv_sqrt3() { return ddf(0.57735026918962576450914878050195745564760175127013); }
+  static __device__ __forceinline__ ddf inv_sqrt2() { return ddf(0.70710678118654752440084436210484903928483593768847); }
+};
+
+}  // namespace glasma

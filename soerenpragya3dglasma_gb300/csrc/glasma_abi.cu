@@ -277,7 +277,8 @@ int step_impl(glasma_lattice* h, double dt, int nsteps, unsigned flags, cudaEven
       if (ev) cudaEventRecord(ev[3 * n], h->stream);
       const bool save = (flags & GLASMA_STEP_SAVE_UOLD) && (n == nsteps - 1);
       e = glasma::launch_plaquette_step<T>(h->g, p, static_cast<T*>(h->contrib), dt, save, h->stream,
-                                           ev ? ev[3 * n + 1] : nullptr, h->link_rows);
+                                           ev ? ev[3 * n + 1] : nullptr, h->link_rows,
+                                           h->fp64_arith == GLASMA_FP64_DOUBLE_FLOAT);
       if (e != cudaSuccess) return cuda_fail(e, "plaquette step");
       if (ev) cudaEventRecord(ev[3 * n + 2], h->stream);
       h->steps_done++;
@@ -357,6 +358,7 @@ int glasma_create(int nx, int ny, int nz, double ax, double ay, double az, int p
   // at 128x128x512); falls back to two-pass when its buffer cannot be allocated
   h->step_method = GLASMA_STEP_PLAQUETTE;
   h->link_rows = 3;
+  h->fp64_arith = GLASMA_FP64_NATIVE;
   h->last_method = GLASMA_STEP_TWO_PASS;
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
@@ -586,6 +588,21 @@ int glasma_set_step_method(glasma_lattice* h, int method) {
     cudaFree(h->contrib);
     h->contrib = nullptr;
   }
+  return GLASMA_OK;
+}
+
+int glasma_set_fp64_arithmetic(glasma_lattice* h, int mode) {
+  GLASMA_CHECK_HANDLE(h);
+  if (mode != GLASMA_FP64_NATIVE && mode != GLASMA_FP64_DOUBLE_FLOAT)
+    return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown FP64 arithmetic mode");
+  h->fp64_arith = mode;
+  return GLASMA_OK;
+}
+
+int glasma_get_fp64_arithmetic(glasma_lattice* h, int* mode) {
+  GLASMA_CHECK_HANDLE(h);
+  if (!mode) return fail(GLASMA_ERR_INVALID_ARGUMENT, "mode is null");
+  *mode = h->fp64_arith;
   return GLASMA_OK;
 }
 

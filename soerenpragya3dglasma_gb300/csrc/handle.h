@@ -28,6 +28,7 @@ struct glasma_lattice {
   int last_method;    // method the last glasma_step used
   int link_rows;      // rows of each link the step kernels read and write: 3, or 2 (12-real links, FP32)
   void* contrib;      // plaquette method: 6 x 8 weighted force contributions per site (lazily)
+  int fp64_arith;     // GLASMA_FP64_NATIVE or GLASMA_FP64_DOUBLE_FLOAT (the plaquette force kernel)
   unsigned long long swaps;  // buffer swaps so far (batched launches rebuild their tables on change)
   // asynchronous uploads (glasma_upload_begin / glasma_upload_finish)
   cudaStream_t xfer_stream;  // copies host -> staging, overlapping the handle's kernels (first use)

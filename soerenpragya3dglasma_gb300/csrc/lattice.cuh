@@ -15,6 +15,7 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "ddf.cuh"
 #include "su3.cuh"
 
 namespace glasma {
@@ -101,6 +102,45 @@ __device__ __forceinline__ void store_link_r(cx<T>* __restrict__ U, I S, int mu,
     }
   }
 }
+// Loads and stores that convert between the storage type T and a compute type TC (identity when equal;
+// double <-> ddf for the FP64 step computed in double-float arithmetic, ddf.cuh).
+template <int R, typename TC, typename T, typename I>
+__device__ __forceinline__ void load_link_c(const cx<T>* __restrict__ U, I S, int mu, I s, Mat<TC>& m) {
+  if constexpr (std::is_same<T, TC>::value) {
+    load_link_r<R>(U, S, mu, s, m);
+  } else {
+    Mat<T> t;
+    load_link_r<R>(U, S, mu, s, t);
+#pragma unroll
+    for (int k = 0; k < 9; k++) m.e[k] = mk<TC>(to_compute<TC>(t.e[k].re), to_compute<TC>(t.e[k].im));
+  }
+}
+template <typename T, typename I>
+__device__ __forceinline__ void load_alg(const T* __restrict__ F, I S, int base, I s, Alg<T>& v);
+template <typename T, typename I>
+__device__ __forceinline__ void store_alg(T* __restrict__ F, I S, int base, I s, const Alg<T>& v);
+template <typename TC, typename T, typename I>
+__device__ __forceinline__ void load_alg_c(const T* __restrict__ F, I S, int base, I s, Alg<TC>& v) {
+  if constexpr (std::is_same<T, TC>::value) {
+    load_alg(F, S, base, s, v);
+  } else {
+    Alg<T> t;
+    load_alg(F, S, base, s, t);
+#pragma unroll
+    for (int a = 0; a < 8; a++) v.a[a] = to_compute<TC>(t.a[a]);
+  }
+}
+template <typename TC, typename T, typename I>
+__device__ __forceinline__ void store_alg_c(T* __restrict__ F, I S, int base, I s, const Alg<TC>& v) {
+  if constexpr (std::is_same<T, TC>::value) {
+    store_alg(F, S, base, s, v);
+  } else {
+    Alg<T> t;
+#pragma unroll
+    for (int a = 0; a < 8; a++) t.a[a] = from_compute<T>(v.a[a]);
+    store_alg(F, S, base, s, t);
+  }
+}
 template <typename T, typename I>
 __device__ __forceinline__ void load_alg(const T* __restrict__ F, I S, int base, I s, Alg<T>& v) {
   const T* p = F + ((I)base * S + s);
@@ -147,9 +187,11 @@ cudaError_t launch_complete_links(const Geometry& g, cx<T>* U, cudaStream_t stre
 // One step by the plaquette method: the force kernel over the plaquette owners, then the link kernel
 // gathering their contributions into E.  `contrib` holds 48 S reals; `between` (optional) is recorded
 // between the two launches.
+// double_float (FP64 fields only): the force kernel computes in double-float arithmetic (ddf.cuh).
 template <typename T>
 cudaError_t launch_plaquette_step(const Geometry& g, FieldPtrs<T> f, T* contrib, double dt, bool save_uold,
-                                  cudaStream_t stream, cudaEvent_t between, int link_rows = 3);
+                                  cudaStream_t stream, cudaEvent_t between, int link_rows = 3,
+                                  bool double_float = false);
 
 // Sub-step kernels with the reference's exact sub-step boundaries.
 template <typename T>

@@ -60,13 +60,13 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kFusedMinBlocks)
 
 // The plaquette method (leapfrog_sites.cuh): K1' over the plaquette owners of slices -1 .. Nz-1,
 // K2' gathering the contributions into E before the link update.
-template <typename T, typename I, int R>
-__global__ void __launch_bounds__(kThreads, Occupancy<T>::kPlaqMinBlocks)
+template <typename T, typename I, int R, typename TC>
+__global__ void __launch_bounds__(kThreads, PlaqOccupancy<T, TC>::kMinBlocks)
     plaquette_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> f, T* __restrict__ C,
                      const __grid_constant__ EParams<T> p) {
   const I idx = (I)blockIdx.x * (I)blockDim.x + (I)threadIdx.x;
   if (idx >= (I)(g.plane * (g.nz + 1))) return;
-  plaquette_site<T, I, R>(g, f, C, p, idx);
+  plaquette_site<T, I, R, TC>(g, f, C, p, idx);
 }
 
 template <typename T, typename I, int R>
@@ -298,28 +298,36 @@ void launch_links_rows(const Geometry& g, FieldPtrs<T> f, const LParams<T>& p, c
 
 template <typename T, typename I, int R>
 void launch_plaquette_rows(const Geometry& g, FieldPtrs<T> f, T* C, const EParams<T>& pe, const LParams<T>& pl,
-                           cudaStream_t stream, cudaEvent_t between) {
-  plaquette_kernel<T, I, R><<<grid_for(g.plane * (g.nz + 1), kThreads), kThreads, 0, stream>>>(g, f, C, pe);
+                           cudaStream_t stream, cudaEvent_t between, bool double_float) {
+  const unsigned grid = grid_for(g.plane * (g.nz + 1), kThreads);
+  if constexpr (sizeof(T) == 8) {
+    if (double_float)
+      plaquette_kernel<T, I, R, ddf><<<grid, kThreads, 0, stream>>>(g, f, C, pe);
+    else
+      plaquette_kernel<T, I, R, T><<<grid, kThreads, 0, stream>>>(g, f, C, pe);
+  } else {
+    plaquette_kernel<T, I, R, T><<<grid, kThreads, 0, stream>>>(g, f, C, pe);
+  }
   if (between) cudaEventRecord(between, stream);
   links_gather_kernel<T, I, R><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, C, pl);
 }
 
 template <typename T>
 cudaError_t launch_plaquette_step(const Geometry& g, FieldPtrs<T> f, T* contrib, double dt, bool save_uold,
-                                  cudaStream_t stream, cudaEvent_t between, int link_rows) {
+                                  cudaStream_t stream, cudaEvent_t between, int link_rows, bool double_float) {
   const EParams<T> pe = make_eparams<T>(g, dt, 1, 1, 0);
   const LParams<T> pl = make_lparams<T>(g, dt, save_uold, true, true);
   // the contribution buffer has 48 S entries: 32-bit offsets only while that fits
   const bool i32 = g.S * 48 < (1LL << 31) - 1;
   if constexpr (sizeof(T) == 4) {
     if (two_row<T>(link_rows)) {
-      i32 ? launch_plaquette_rows<T, int, 2>(g, f, contrib, pe, pl, stream, between)
-          : launch_plaquette_rows<T, long long, 2>(g, f, contrib, pe, pl, stream, between);
+      i32 ? launch_plaquette_rows<T, int, 2>(g, f, contrib, pe, pl, stream, between, false)
+          : launch_plaquette_rows<T, long long, 2>(g, f, contrib, pe, pl, stream, between, false);
       return cudaGetLastError();
     }
   }
-  i32 ? launch_plaquette_rows<T, int, 3>(g, f, contrib, pe, pl, stream, between)
-      : launch_plaquette_rows<T, long long, 3>(g, f, contrib, pe, pl, stream, between);
+  i32 ? launch_plaquette_rows<T, int, 3>(g, f, contrib, pe, pl, stream, between, double_float)
+      : launch_plaquette_rows<T, long long, 3>(g, f, contrib, pe, pl, stream, between, double_float);
   return cudaGetLastError();
 }
 
@@ -398,7 +406,7 @@ cudaError_t launch_copy_links(const Geometry& g, const cx<T>* src, cx<T>* dst, c
   template cudaError_t launch_reunitarize<T>(const Geometry&, cx<T>*, cudaStream_t, int);                      \
   template cudaError_t launch_complete_links<T>(const Geometry&, cx<T>*, cudaStream_t);                        \
   template cudaError_t launch_plaquette_step<T>(const Geometry&, FieldPtrs<T>, T*, double, bool, cudaStream_t,  \
-                                                cudaEvent_t, int);                                              \
+                                                cudaEvent_t, int, bool);                                        \
   template cudaError_t launch_copy_links<T>(const Geometry&, const cx<T>*, cx<T>*, cudaStream_t);              \
   template cudaError_t launch_sync_ghosts<T>(const Geometry&, T*, int, cudaStream_t);                          \
   template cudaError_t launch_sync_ghosts<cx<T>>(const Geometry&, cx<T>*, int, cudaStream_t);

@@ -27,6 +27,9 @@ constexpr int kThreads = 128;
 #ifndef GLASMA_FP32_PLAQ_MIN_BLOCKS
 #define GLASMA_FP32_PLAQ_MIN_BLOCKS 4
 #endif
+#ifndef GLASMA_DDF_PLAQ_MIN_BLOCKS
+#define GLASMA_DDF_PLAQ_MIN_BLOCKS 2
+#endif
 template <typename T>
 struct Occupancy;
 template <>
@@ -250,8 +253,10 @@ __device__ __forceinline__ void plaquette_alg(const Mat<T>& a, const Mat<T>& b, 
   retr_itg(P, T(1), al);
 }
 
-// K1' per owner site: idx = owner site s (slice -1 starts at s = 0); covers (Nz+1) slices.
-template <typename T, typename I, int R>
+// K1' per owner site: idx = owner site s (slice -1 starts at s = 0); covers (Nz+1) slices.  TC is the
+// arithmetic type: T itself, or ddf for FP64 fields (double-float arithmetic on the FP32 pipe, the
+// fields converted on load and store).
+template <typename T, typename I, int R, typename TC = T>
 __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtrs<T>& f, T* __restrict__ C,
                                                const EParams<T>& p, I idx) {
   const I S = (I)g.S, plane = (I)g.plane;
@@ -263,18 +268,19 @@ __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtr
   const bool interior = z >= 0;
   const bool below_top = z < g.nz - 1;  // y+z is an interior site
   const I sxp = nb<I>(g, x, y, z, 1, 0, 0), syp = nb<I>(g, x, y, z, 0, 1, 0), szp = s + plane;
-  const T w01p = p.gc[0] * p.cnu[1], w01q = p.gc[1] * p.cnu[0];  // wp = gc_p c_q, wq = gc_q c_p
-  const T w02p = p.gc[0] * p.cnu[2], w02q = p.gc[2] * p.cnu[0];
-  const T w12p = p.gc[1] * p.cnu[2], w12q = p.gc[2] * p.cnu[1];
-  Alg<T> F0, F1, F2, al, out;
-  Mat<T> u0, u1, u2, b, c;
-  load_link_r<R>(f.U, S, 0, s, u0);
-  load_link_r<R>(f.U, S, 1, s, u1);
-  load_link_r<R>(f.U, S, 2, s, u2);
+  // wp = gc_p c_q, wq = gc_q c_p (formed in the storage type, then converted)
+  const TC w01p = to_compute<TC>(p.gc[0] * p.cnu[1]), w01q = to_compute<TC>(p.gc[1] * p.cnu[0]);
+  const TC w02p = to_compute<TC>(p.gc[0] * p.cnu[2]), w02q = to_compute<TC>(p.gc[2] * p.cnu[0]);
+  const TC w12p = to_compute<TC>(p.gc[1] * p.cnu[2]), w12q = to_compute<TC>(p.gc[2] * p.cnu[1]);
+  Alg<TC> F0, F1, F2, al, out;
+  Mat<TC> u0, u1, u2, b, c;
+  load_link_c<R>(f.U, S, 0, s, u0);
+  load_link_c<R>(f.U, S, 1, s, u1);
+  load_link_c<R>(f.U, S, 2, s, u2);
   if (interior) {
     // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
-    load_link_r<R>(f.U, S, 1, sxp, b);
-    load_link_r<R>(f.U, S, 0, syp, c);
+    load_link_c<R>(f.U, S, 1, sxp, b);
+    load_link_c<R>(f.U, S, 0, syp, c);
     plaquette_alg(u0, b, c, u1, al);
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -283,19 +289,19 @@ __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtr
     }
     inv_adj_mul(u1, al, out);  // to link 0 at y+y
     scale_alg(-w01p, out);
-    if (!p.dry) store_alg(C, S, kC01q * 8, s, out);
+    if (!p.dry) store_alg_c(C, S, kC01q * 8, s, out);
     inv_adj_mul(u0, al, out);  // to link 1 at y+x
     scale_alg(w01q, out);
-    if (!p.dry) store_alg(C, S, kC01p * 8, s, out);
+    if (!p.dry) store_alg_c(C, S, kC01p * 8, s, out);
   }
   // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
-  load_link_r<R>(f.U, S, 2, sxp, b);
-  load_link_r<R>(f.U, S, 0, szp, c);
+  load_link_c<R>(f.U, S, 2, sxp, b);
+  load_link_c<R>(f.U, S, 0, szp, c);
   plaquette_alg(u0, b, c, u2, al);
   if (below_top) {
     inv_adj_mul(u2, al, out);  // to link 0 at y+z
     scale_alg(-w02p, out);
-    if (!p.dry) store_alg(C, S, kC02q * 8, s, out);
+    if (!p.dry) store_alg_c(C, S, kC02q * 8, s, out);
   }
   if (interior) {
 #pragma unroll
@@ -305,16 +311,16 @@ __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtr
     }
     inv_adj_mul(u0, al, out);  // to link 2 at y+x
     scale_alg(w02q, out);
-    if (!p.dry) store_alg(C, S, kC02p * 8, s, out);
+    if (!p.dry) store_alg_c(C, S, kC02p * 8, s, out);
   }
   // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
-  load_link_r<R>(f.U, S, 2, syp, b);
-  load_link_r<R>(f.U, S, 1, szp, c);
+  load_link_c<R>(f.U, S, 2, syp, b);
+  load_link_c<R>(f.U, S, 1, szp, c);
   plaquette_alg(u1, b, c, u2, al);
   if (below_top) {
     inv_adj_mul(u2, al, out);  // to link 1 at y+z
     scale_alg(-w12p, out);
-    if (!p.dry) store_alg(C, S, kC12q * 8, s, out);
+    if (!p.dry) store_alg_c(C, S, kC12q * 8, s, out);
   }
   if (!interior) return;
 #pragma unroll
@@ -324,52 +330,64 @@ __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtr
   }
   inv_adj_mul(u1, al, out);  // to link 2 at y+y
   scale_alg(w12q, out);
-  if (!p.dry) store_alg(C, S, kC12p * 8, s, out);
+  if (!p.dry) store_alg_c(C, S, kC12p * 8, s, out);
   // E += the forces of the plaquettes owned here (+ the current source on E_z); K2' adds the rest
-  Alg<T> e;
-  load_alg(f.E, S, 0, s, e);
+  Alg<TC> e;
+  load_alg_c(f.E, S, 0, s, e);
 #pragma unroll
   for (int k = 0; k < 8; k++) e.a[k] += F0.a[k];
-  if (!p.dry) store_alg(f.E, S, 0, s, e);
-  load_alg(f.E, S, 8, s, e);
+  if (!p.dry) store_alg_c(f.E, S, 0, s, e);
+  load_alg_c(f.E, S, 8, s, e);
 #pragma unroll
   for (int k = 0; k < 8; k++) e.a[k] += F1.a[k];
-  if (!p.dry) store_alg(f.E, S, 8, s, e);
+  if (!p.dry) store_alg_c(f.E, S, 8, s, e);
   {
-    Alg<T> jp, jm;
-    load_alg(f.E, S, 16, s, e);
-    load_alg(f.Jp, S, 0, s, jp);
-    load_alg(f.Jm, S, 0, s, jm);
+    Alg<TC> jp, jm;
+    const TC jz = to_compute<TC>(p.jz);
+    load_alg_c(f.E, S, 16, s, e);
+    load_alg_c(f.Jp, S, 0, s, jp);
+    load_alg_c(f.Jm, S, 0, s, jm);
 #pragma unroll
-    for (int k = 0; k < 8; k++) e.a[k] += F2.a[k] + p.jz * (jp.a[k] - jm.a[k]);
-    if (!p.dry) store_alg(f.E, S, 16, s, e);
+    for (int k = 0; k < 8; k++) e.a[k] += F2.a[k] + jz * (jp.a[k] - jm.a[k]);
+    if (!p.dry) store_alg_c(f.E, S, 16, s, e);
   }
   // UpdateJStat, as K1
   const bool lo = (z == 0), hi = (z == g.nz - 1);
   const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
   const I szm = s - plane;
-  Mat<T> uzm;
-  load_link_r<R>(f.U, S, 2, szm, uzm);
-  Alg<T> down, jc, st;
-  load_alg(f.Jp, S, 0, szm, jc);
+  const TC cj = to_compute<TC>(p.cj);
+  Mat<TC> uzm;
+  load_link_c<R>(f.U, S, 2, szm, uzm);
+  Alg<TC> down, jc, st;
+  load_alg_c(f.Jp, S, 0, szm, jc);
   inv_adj_mul(uzm, jc, down);
-  load_alg(f.Jp, S, 0, s, jc);
-  load_alg(f.JpStat, S, 0, s, st);
-  axpy_diff(st, -p.cj, jc, down);
+  load_alg_c(f.Jp, S, 0, s, jc);
+  load_alg_c(f.JpStat, S, 0, s, st);
+  axpy_diff(st, -cj, jc, down);
   if (!p.dry) {
-    store_alg(f.JpStat, S, 0, s, st);
-    if (sg >= 0) store_alg(f.JpStat, S, 0, sg, st);
+    store_alg_c(f.JpStat, S, 0, s, st);
+    if (sg >= 0) store_alg_c(f.JpStat, S, 0, sg, st);
   }
-  load_alg(f.Jm, S, 0, szm, jc);
+  load_alg_c(f.Jm, S, 0, szm, jc);
   inv_adj_mul(uzm, jc, down);
-  load_alg(f.Jm, S, 0, s, jc);
-  load_alg(f.JmStat, S, 0, s, st);
-  axpy_diff(st, p.cj, jc, down);
+  load_alg_c(f.Jm, S, 0, s, jc);
+  load_alg_c(f.JmStat, S, 0, s, st);
+  axpy_diff(st, cj, jc, down);
   if (!p.dry) {
-    store_alg(f.JmStat, S, 0, s, st);
-    if (sg >= 0) store_alg(f.JmStat, S, 0, sg, st);
+    store_alg_c(f.JmStat, S, 0, s, st);
+    if (sg >= 0) store_alg_c(f.JmStat, S, 0, sg, st);
   }
 }
+
+// Blocks per SM of the force kernel: by storage type, and for FP64 fields computed in double-float.
+template <typename T, typename TC>
+struct PlaqOccupancy {
+  static constexpr int kMinBlocks = Occupancy<T>::kPlaqMinBlocks;
+};
+template <>
+struct PlaqOccupancy<double, ddf> {
+  static constexpr int kMinBlocks = GLASMA_DDF_PLAQ_MIN_BLOCKS;
+};
 
 // Thread-to-site map of K1: a block of kThreads threads covers a tile of tile_x x (kThreads/tile_x)
 // sites of one z slice, so most y-neighbours a block reads are its own sites (L1 hits).

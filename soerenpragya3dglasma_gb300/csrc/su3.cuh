@@ -93,7 +93,7 @@ __device__ __forceinline__ void mul_nn(const Mat<T>& A, const Mat<T>& B, Mat<T>&
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
 #pragma unroll
       for (int k = 0; k < 3; k++) cfma(acc, A.e[i + 3 * k], B.e[k + 3 * j]);
       C.e[i + 3 * j] = acc;
@@ -106,7 +106,7 @@ __device__ __forceinline__ void mul_nd(const Mat<T>& A, const Mat<T>& B, Mat<T>&
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
 #pragma unroll
       for (int k = 0; k < 3; k++) cfma_nc(acc, A.e[i + 3 * k], B.e[j + 3 * k]);
       C.e[i + 3 * j] = acc;
@@ -119,7 +119,7 @@ __device__ __forceinline__ void mul_dn(const Mat<T>& A, const Mat<T>& B, Mat<T>&
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
 #pragma unroll
       for (int k = 0; k < 3; k++) cfma_cn(acc, A.e[k + 3 * i], B.e[k + 3 * j]);
       C.e[i + 3 * j] = acc;
@@ -132,7 +132,7 @@ __device__ __forceinline__ void mul_dd(const Mat<T>& A, const Mat<T>& B, Mat<T>&
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
 #pragma unroll
       for (int k = 0; k < 3; k++) cfma_cc(acc, A.e[k + 3 * i], B.e[j + 3 * k]);
       C.e[i + 3 * j] = acc;
@@ -164,7 +164,7 @@ __device__ __forceinline__ void add_mul_nn(const Mat<T>& A, const Mat<T>& B, T s
 template <typename T>
 __device__ __forceinline__ void set_zero(Mat<T>& A) {
 #pragma unroll
-  for (int k = 0; k < 9; k++) A.e[k] = mk<T>(0, 0);
+  for (int k = 0; k < 9; k++) A.e[k] = mk<T>(T(0), T(0));
 }
 
 // out_a = c * Re tr(i t^a V)
@@ -185,9 +185,9 @@ __device__ __forceinline__ void retr_itg(const Mat<T>& V, T c, Alg<T>& out) {
 template <typename T>
 __device__ __forceinline__ void herm_from_alg(const Alg<T>& al, Mat<T>& M) {
   const T s8 = al.a[7] * Consts<T>::inv_sqrt3();
-  M.e[0] = mk<T>(T(0.5) * (al.a[2] + s8), 0);
-  M.e[4] = mk<T>(T(-0.5) * (al.a[2] - s8), 0);
-  M.e[8] = mk<T>(-s8, 0);
+  M.e[0] = mk<T>(T(0.5) * (al.a[2] + s8), T(0));
+  M.e[4] = mk<T>(T(-0.5) * (al.a[2] - s8), T(0));
+  M.e[8] = mk<T>(-s8, T(0));
   M.e[1] = mk<T>(T(0.5) * al.a[0], T(0.5) * al.a[1]);   // (1,0)
   M.e[2] = mk<T>(T(0.5) * al.a[3], T(0.5) * al.a[4]);   // (2,0)
   M.e[5] = mk<T>(T(0.5) * al.a[5], T(0.5) * al.a[6]);   // (2,1)
@@ -217,7 +217,7 @@ __device__ __forceinline__ void mul_nd_herm(const Mat<T>& A, const Mat<T>& B, Ma
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
       if (i == j) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -237,7 +237,7 @@ __device__ __forceinline__ void mul_nn_herm(const Mat<T>& A, const Mat<T>& B, Ma
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
       if (i == j) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -279,7 +279,7 @@ __device__ __forceinline__ void mul_nn_traceless(const Mat<T>& A, const Mat<T>& 
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
       if (i == j) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -301,7 +301,7 @@ __device__ __forceinline__ void mul_nd_traceless(const Mat<T>& A, const Mat<T>& 
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
       if (i == j) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -323,7 +323,7 @@ __device__ __forceinline__ void mul_dn_traceless(const Mat<T>& A, const Mat<T>& 
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cx<T> acc = mk<T>(0, 0);
+      cx<T> acc = mk<T>(T(0), T(0));
       if (i == j) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {  // Im conj(A_ki) B_ki
@@ -434,7 +434,7 @@ __device__ __forceinline__ void expi_impl(T c, const Alg<T>& al, Mat<T>& X) {
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) {
-    cx<T> v = mk<T>(0, 0);
+    cx<T> v = mk<T>(T(0), T(0));
     cfma(v, f1, Q.e[k]);
     cfma(v, f2, Q2.e[k]);
     X.e[k] = v;

@@ -238,6 +238,20 @@ class Lattice:
         check(self.lib.glasma_get_step_method(self.h, ctypes.byref(m)))
         return {v: k for k, v in self.STEP_METHODS.items()}[m.value]
 
+    FP64_ARITHMETIC = {"native": 0, "double_float": 1}
+
+    @property
+    def fp64_arithmetic(self):
+        """"native" (default) or "double_float": the arithmetic of the plaquette force kernel on FP64
+        handles (double-float = pairs of FP32 numbers on the FP32 pipe)."""
+        m = ctypes.c_int()
+        check(self.lib.glasma_get_fp64_arithmetic(self.h, ctypes.byref(m)))
+        return {v: k for k, v in self.FP64_ARITHMETIC.items()}[m.value]
+
+    @fp64_arithmetic.setter
+    def fp64_arithmetic(self, mode):
+        check(self.lib.glasma_set_fp64_arithmetic(self.h, self.FP64_ARITHMETIC[mode]))
+
     @property
     def link_reals(self):
         """Reals per link the leapfrog step reads and writes: 18, or 12 (rows 0 and 1 of each link,

@@ -117,6 +117,27 @@ def test_one_pass_equals_two_pass_bit_exact(precision, N):
         assert np.array_equal(outs[0][k], outs[1][k]), k
 
 
+@pytest.mark.parametrize("tag,nsteps", [("s1", 1), ("s10", 10)])
+def test_double_float_force_matches_reference_golden(golden_dir, tag, nsteps):
+    """The FP64 plaquette force computed in double-float arithmetic (pairs of floats, ~48-bit
+    significand; FP64 fields converted by bits on load and store): the reference's golden fields at
+    the FP64 bar, and the native FP64 step to 1e-13."""
+    g = _load(golden_dir, "leapfrog_random.npz")
+    N, a, dt = tuple(g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_dt"])
+    init = {k: g["init_" + k] for k in FIELDS}
+    outs = {}
+    for mode in ("double_float", "native"):
+        with _gpu(init, N, a) as lat:
+            lat.set_step_method("plaquette")
+            lat.fp64_arithmetic = mode
+            assert lat.fp64_arithmetic == mode
+            lat.step(dt, nsteps)
+            outs[mode] = lat.download_fields()
+    for k in FIELDS:
+        assert _rel(outs["double_float"][k], g[tag + "_" + k]) < 1e-12, k
+        assert _rel(outs["double_float"][k], outs["native"][k]) < 1e-13, k
+
+
 @pytest.mark.parametrize("precision,reals", [("fp64", 18), ("fp32", 18), ("fp32", 12)])
 @pytest.mark.parametrize("N", [(6, 5, 8), (3, 7, 2), (16, 8, 4)])
 def test_plaquette_method_equals_two_pass(precision, reals, N):
