@@ -150,6 +150,91 @@ __device__ __forceinline__ double from_compute<double>(ddf x) {
   return to_double(x);
 }
 
+// The double-float 3x3 products run as out-of-line functions: fully unrolled and inlined at every use
+// the force kernel's code overflowed the instruction cache (ncu: "no instruction" the dominant stall,
+// 22 % issue); one copy of each product serves every call.
+static __device__ __noinline__ void ddf_mul_nn(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C);
+static __device__ __noinline__ void ddf_mul_dn(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C);
+static __device__ __noinline__ void ddf_mul_nn_herm(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C);
+static __device__ __noinline__ void ddf_mul_nd_traceless(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C);
+template <>
+__device__ __forceinline__ void mul_nn<ddf>(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+  ddf_mul_nn(A, B, C);
+}
+template <>
+__device__ __forceinline__ void mul_dn<ddf>(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+  ddf_mul_dn(A, B, C);
+}
+template <>
+__device__ __forceinline__ void mul_nn_herm<ddf>(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+  ddf_mul_nn_herm(A, B, C);
+}
+template <>
+__device__ __forceinline__ void mul_nd_traceless<ddf>(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+  ddf_mul_nd_traceless(A, B, C);
+}
+// the bodies: the generic products' own arithmetic, on ddf
+static __device__ __noinline__ void ddf_mul_nn(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<ddf> acc = mk<ddf>(ddf(0.0), ddf(0.0));
+#pragma unroll
+      for (int k = 0; k < 3; k++) cfma(acc, A.e[i + 3 * k], B.e[k + 3 * j]);
+      C.e[i + 3 * j] = acc;
+    }
+}
+static __device__ __noinline__ void ddf_mul_dn(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<ddf> acc = mk<ddf>(ddf(0.0), ddf(0.0));
+#pragma unroll
+      for (int k = 0; k < 3; k++) cfma_cn(acc, A.e[k + 3 * i], B.e[k + 3 * j]);
+      C.e[i + 3 * j] = acc;
+    }
+}
+static __device__ __noinline__ void ddf_mul_nn_herm(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      cx<ddf> acc = mk<ddf>(ddf(0.0), ddf(0.0));
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          acc.re = fma(A.e[i + 3 * k].re, B.e[k + 3 * j].re, acc.re);
+          acc.re = fma(-A.e[i + 3 * k].im, B.e[k + 3 * j].im, acc.re);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma(acc, A.e[i + 3 * k], B.e[k + 3 * j]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+}
+static __device__ __noinline__ void ddf_mul_nd_traceless(const Mat<ddf>& A, const Mat<ddf>& B, Mat<ddf>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cx<ddf> acc = mk<ddf>(ddf(0.0), ddf(0.0));
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          acc.im = fma(-A.e[i + 3 * k].re, B.e[j + 3 * k].im, acc.im);
+          acc.im = fma(A.e[i + 3 * k].im, B.e[j + 3 * k].re, acc.im);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma_nc(acc, A.e[i + 3 * k], B.e[j + 3 * k]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+}
+
 template <>
 struct Consts<ddf> {
   static __device__ __forceinline__ ddf inv_sqrt3() { return ddf(0.57735026918962576450914878050195745564760175127013); }

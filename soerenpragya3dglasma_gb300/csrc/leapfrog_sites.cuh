@@ -28,7 +28,7 @@ constexpr int kThreads = 128;
 #define GLASMA_FP32_PLAQ_MIN_BLOCKS 4
 #endif
 #ifndef GLASMA_DDF_PLAQ_MIN_BLOCKS
-#define GLASMA_DDF_PLAQ_MIN_BLOCKS 2
+#define GLASMA_DDF_PLAQ_MIN_BLOCKS 3
 #endif
 template <typename T>
 struct Occupancy;
