@@ -235,10 +235,37 @@ static __device__ __noinline__ void ddf_mul_nd_traceless(const Mat<ddf>& A, cons
     }
 }
 
+// links of FP64 fields loaded and split out of line: p points at element 0 of the link, the nine
+// complex elements `stride` apart
+static __device__ __noinline__ void ddf_load_link9(const cx<double>* __restrict__ p, long long stride, Mat<ddf>& m) {
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const cx<double> v = p[(long long)k * stride];
+    m.e[k] = mk<ddf>(ddf_from_double(v.re), ddf_from_double(v.im));
+  }
+}
+
 template <>
 struct Consts<ddf> {
   static __device__ __forceinline__ ddf inv_sqrt3() { return ddf(0.57735026918962576450914878050195745564760175127013); }
   static __device__ __forceinline__ ddf inv_sqrt2() { return ddf(0.70710678118654752440084436210484903928483593768847); }
 };
+
+// V^dagger (t.e) V in double-float, out of line (six per site in the force kernel)
+template <typename T>
+__device__ __forceinline__ void herm_from_alg(const Alg<T>& al, Mat<T>& M);
+template <typename T>
+__device__ __forceinline__ void alg_from_herm(const Mat<T>& W, Alg<T>& out);
+static __device__ __noinline__ void ddf_inv_adj_mul(const Mat<ddf>& V, const Alg<ddf>& e, Alg<ddf>& out) {
+  Mat<ddf> M, W, R;
+  herm_from_alg(e, M);
+  ddf_mul_dn(V, M, W);
+  ddf_mul_nn_herm(W, V, R);
+  alg_from_herm(R, out);
+}
+template <>
+__device__ __forceinline__ void inv_adj_mul<ddf>(const Mat<ddf>& V, const Alg<ddf>& e, Alg<ddf>& out) {
+  ddf_inv_adj_mul(V, e, out);
+}
 
 }  // namespace glasma

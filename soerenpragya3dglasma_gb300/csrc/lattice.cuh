@@ -108,6 +108,8 @@ template <int R, typename TC, typename T, typename I>
 __device__ __forceinline__ void load_link_c(const cx<T>* __restrict__ U, I S, int mu, I s, Mat<TC>& m) {
   if constexpr (std::is_same<T, TC>::value) {
     load_link_r<R>(U, S, mu, s, m);
+  } else if constexpr (std::is_same<T, double>::value && std::is_same<TC, ddf>::value && R == 3) {
+    ddf_load_link9(U + ((I)(mu * 9) * S + s), (long long)S, m);
   } else {
     Mat<T> t;
     load_link_r<R>(U, S, mu, s, t);
