@@ -69,7 +69,9 @@ __host__ __device__ __forceinline__ float ddf_float_from_bits(unsigned b) {
 
 // d = head + tail: head = the leading 24 bits of d's significand (exponent rebiased), tail = the
 // remaining 29 bits as t 2^(e-1075), rounded to a float; then renormalised (Fast2Sum).  Outside
-// 2^-74 <= |d| < 2^128 (zero, tiny, huge, inf, nan) the FP64 conversion is used instead.
+// 2^-74 <= |d| < 2^128 the FP64 conversion is used instead: zero stays zero, tiny values keep fewer
+// bits, and |d| >= 2^128 (beyond FP32's exponent range, as in any double-float format) becomes
+// +-inf.  Field values of the evolution are far inside the range.
 __host__ __device__ __forceinline__ ddf ddf_from_double(double d) {
   const unsigned long long b = ddf_bits64(d);
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
