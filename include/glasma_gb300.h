@@ -74,6 +74,13 @@ enum glasma_field {
                                             (the gradient, the update and the links stay FP64): the
                                             iterates differ from the reference's at the 1e-7 level,
                                             the converged gauge is the same */
+#define GLASMA_GF_OPEN_Z 0x4u            /* open-z functional, a documented variant: the top slice's
+                                            forward z link (into the ghost slice) is left out of the
+                                            deviation (the reference counts it at one end only,
+                                            CoulombGaugeDeviation.cpp:37, so its iteration does not
+                                            converge with open z boundaries); Delta is then the
+                                            gradient of sum Re tr UG over the links inside the lattice
+                                            and the iteration converges */
 
 /* Create a lattice (replaces Lattice::Init, S/LATTICE/SUNcVariables.cpp:71-90, and the
  * container constructors, S/LATTICE/GaugeLinks.cpp:110-127): links set to the identity,

@@ -512,8 +512,13 @@ void gauge_transform_efield(const Lat& l, const double* E, double* EG, cplx* G) 
 // ------------------------------------------------------------- Coulomb gauge deviation at one site
 // GET_LOCAL_GAUGE_VIOLATION (S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41):
 // w(x) = sum_mu c_mu (UG_mu(x) + UG_mu^dagger(x - mu)), the z term only if Nz > 1; Delta^a = ReTr(i t^a w).
-void gauge_deviation(const Lat& l, const cplx* UG, int x, int y, int z, const double* cw, cplx* w, double* dev) {
+// open_top != 0 (the open-z functional, a documented variant): the forward z link of the top slice,
+// which points into the ghost slice, is left out, so Delta is the gradient of
+// F = sum over links with both ends in [0, Nz-1] of Re tr UG.
+void gauge_deviation(const Lat& l, const cplx* UG, int x, int y, int z, const double* cw, cplx* w, double* dev,
+                     int open_top = 0) {
   const double zterm = l.N[2] > 1 ? 1.0 : 0.0;
+  const double ztop = (open_top && z == l.N[2] - 1) ? 0.0 : 1.0;
   const cplx* u0 = L(UG, l, x, y, z, 0);
   const cplx* u1 = L(UG, l, x, y, z, 1);
   const cplx* u2 = L(UG, l, x, y, z, 2);
@@ -524,7 +529,7 @@ void gauge_deviation(const Lat& l, const cplx* UG, int x, int y, int z, const do
     for (int j = 0; j < 3; j++) {
       const int k = mi(i, j), kt = mi(j, i);
       w[k] = cw[0] * (u0[k] + std::conj(d0[kt])) + cw[1] * (u1[k] + std::conj(d1[kt])) +
-             zterm * cw[2] * (u2[k] + std::conj(d2[kt]));
+             zterm * cw[2] * (ztop * u2[k] + std::conj(d2[kt]));
     }
   retr_itg(w, dev);
 }
@@ -833,8 +838,12 @@ void oracle_emt_map(const int* N, const double* a, double aScale, double* Uin, d
 // fields; their ghost slices are never written (the reference's GaugeFixedVariables keep the identity /
 // zero ghosts they were created with).  log_out[n*7 + k] = n, maxdev, avgdev, maxstep, avgstep,
 // minfunctional, sumfunctional/V.  Returns 0, or 5 when the unitarity guard fires (the reference exits).
+// flags: 0 for the reference's iteration; 0x1 drops the p = 0 mode of the update (the reference leaves it
+// unnormalised, FourierAcceleration.cpp:69-77); 0x4 the open-z functional (gauge_deviation's open_top).
 int oracle_coulomb_fix(const int* N, const double* a, double aScale, const double* Uin, const double* E, double* Gin,
-                       double* UGin, double* EG, double alpha, int total_steps, double tol, double* log_out, int* n_out) {
+                       double* UGin, double* EG, double alpha, int total_steps, double tol, double* log_out, int* n_out,
+                       unsigned flags) {
+  const int project_zero = (flags & 0x1u) ? 1 : 0, open_top = (flags & 0x4u) ? 1 : 0;
   Lat l = make_lat(N, a, aScale);
   const cplx* U = reinterpret_cast<const cplx*>(Uin);
   cplx* G = reinterpret_cast<cplx*>(Gin);
@@ -860,7 +869,7 @@ int oracle_coulomb_fix(const int* N, const double* a, double aScale, const doubl
         for (int x = 0; x < Nx; x++) {
           cplx w[9];
           double dev[8];
-          gauge_deviation(l, UG, x, y, z, cw, w, dev);
+          gauge_deviation(l, UG, x, y, z, cw, w, dev, open_top);
           const long site = x + (long)Nx * (y + (long)Ny * z);
           for (int aa = 0; aa < 8; aa++) {
             maxdev = std::max(maxdev, std::fabs(dev[aa]));
@@ -880,9 +889,11 @@ int oracle_coulomb_fix(const int* N, const double* a, double aScale, const doubl
           const double p2 = (2.0 - 2.0 * std::cos(2.0 * M_PI * px / (double)Nx)) / (l.a[0] * l.a[0]) +
                             (2.0 - 2.0 * std::cos(2.0 * M_PI * py / (double)Ny)) / (l.a[1] * l.a[1]) +
                             (2.0 - 2.0 * std::cos(2.0 * M_PI * pz / (double)Nz)) / (l.a[2] * l.a[2]);
+          const long site = px + (long)Nx * (py + (long)Ny * pz);
           if (p2 > 0.0) {
-            const long site = px + (long)Nx * (py + (long)Ny * pz);
             for (int aa = 0; aa < 8; aa++) X[aa + 8 * site] = nf * X[aa + 8 * site] / p2;
+          } else if (project_zero) {
+            for (int aa = 0; aa < 8; aa++) X[aa + 8 * site] = 0.0;
           }
         }
     fft3d(X.data(), l.N, 8, +1);

@@ -179,7 +179,7 @@ class Oracle:
         L.oracle_unitarity.argtypes = [_ip, _dp, _dp, _dp]
         L.oracle_emt_map.argtypes = [_ip, _dp, ctypes.c_double, _dp, _dp, _dp, _dp]
         L.oracle_coulomb_fix.argtypes = [_ip, _dp, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, ctypes.c_double,
-                                         ctypes.c_int, ctypes.c_double, _dp, _ip]
+                                         ctypes.c_int, ctypes.c_double, _dp, _ip, ctypes.c_uint]
         L.oracle_coulomb_fix.restype = ctypes.c_int
         L.oracle_coulomb_fix_local.argtypes = [_ip, _dp, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
                                                ctypes.c_double, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_double,
@@ -197,15 +197,6 @@ class Oracle:
 
     def threads(self):
         return self.lib.oracle_get_threads()
-
-    def coulomb_fix_local(self, algorithm, param, total_steps, uniforms=()):
-        """Los Alamos / Jacobi gauge fixing with the reference's own update functions; uniforms are
-        what its rng() returns, in call order (construct with threads=1 for a fixed order)."""
-        u = np.ascontiguousarray(uniforms, dtype=np.float64)
-        log = np.zeros((max(total_steps, 1), 7))
-        n = self.lib.ref_coulomb_local(LOCAL_GAUGE_ALGORITHMS[algorithm], param, _ptr(u), u.size, total_steps,
-                                       _ptr(log), total_steps)
-        return log[:n]
 
     def expi(self, c, alpha):
         out = np.zeros(9, dtype=np.complex128)
@@ -242,14 +233,15 @@ class Oracle:
         self.lib.oracle_emt_map(_ivec(N), _dvec(a), a_scale, _ptr(f["U"]), _ptr(f["UOld"]), _ptr(f["E"]), _ptr(out))
         return out
 
-    def coulomb_fix(self, f, G, N, a, alpha, total_steps, tol=1e-15, a_scale=1.0, UG=None, EG=None):
-        """Returns (status, log[n,7], UG, EG); G is updated in place."""
+    def coulomb_fix(self, f, G, N, a, alpha, total_steps, tol=1e-15, a_scale=1.0, UG=None, EG=None, flags=0):
+        """Returns (status, log[n,7], UG, EG); G is updated in place.  flags: 0 for the reference's
+        iteration, GF_PROJECT_ZERO_MODE | GF_OPEN_Z for the converging open-z variant."""
         UG = identity_links(N) if UG is None else UG
         EG = zero_efield(N) if EG is None else EG
         log = np.zeros((max(total_steps, 1), 7))
         n = ctypes.c_int()
         st = self.lib.oracle_coulomb_fix(_ivec(N), _dvec(a), a_scale, _ptr(f["U"]), _ptr(f["E"]), _ptr(G), _ptr(UG),
-                                         _ptr(EG), alpha, total_steps, tol, _ptr(log), ctypes.byref(n))
+                                         _ptr(EG), alpha, total_steps, tol, _ptr(log), ctypes.byref(n), flags)
         return st, log[: n.value], UG, EG
 
     def coulomb_fix_local(self, f, G, N, a, algorithm, param, total_steps, seed=0, tol=1e-15, a_scale=1.0,
@@ -281,7 +273,10 @@ class Oracle:
         return np.array(out)
 
 
-LOCAL_GAUGE_ALGORITHMS = {"los_alamos": 1, "jacobi": 2}
+LOCAL_GAUGE_ALGORITHMS = {"los_alamos": 1, "jacobi": 2, "fourier": 0}
+# coulomb_fix flags (the values of the library's GLASMA_GF_PROJECT_ZERO_MODE / GLASMA_GF_OPEN_Z)
+GF_PROJECT_ZERO_MODE = 0x1
+GF_OPEN_Z = 0x4
 
 
 # ----------------------------------------------------------------- the reference itself
@@ -314,6 +309,7 @@ class Reference:
         L.ref_coulomb_local.argtypes = [ctypes.c_int, ctypes.c_double, _dp, ctypes.c_long, ctypes.c_int, _dp,
                                         ctypes.c_int]
         L.ref_coulomb_local.restype = ctypes.c_int
+        L.ref_coulomb_profile.argtypes = [_dp, _dp]
         L.ref_expi.argtypes = [ctypes.c_double, _dp, _dp]
         L.ref_matrix_ilog.argtypes = [ctypes.c_double, _dp, _dp]
         L.ref_set_outdir.argtypes = [ctypes.c_char_p]
@@ -394,6 +390,13 @@ class Reference:
         log = np.zeros((max(total_steps, 1), 7))
         n = self.lib.ref_coulomb(alpha, total_steps, _ptr(log), total_steps)
         return log[:n]
+
+    def coulomb_profile(self):
+        """Per-slice (max |Delta|, sum Delta^2) of the reference's current gauge-fixed links, from its
+        own deviation macro."""
+        zmax, zsq = np.zeros(self.N[2]), np.zeros(self.N[2])
+        self.lib.ref_coulomb_profile(_ptr(zmax), _ptr(zsq))
+        return zmax, zsq
 
     def coulomb_fix_local(self, algorithm, param, total_steps, uniforms=()):
         """Los Alamos / Jacobi gauge fixing with the reference's own update functions; uniforms are

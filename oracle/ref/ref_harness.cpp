@@ -321,41 +321,74 @@ int ref_coulomb(double alpha, int total_steps, double* log_out, int max_rows) {
   return n;
 }
 
-// SetCoulombGauge's loop (S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:32-88) with the Los Alamos
-// (algorithm 1, param = OverRelaxationProbability) or the Jacobi (2, param = alphaStepSize) update in
-// place of the Fourier-accelerated one.  The reference selects its algorithm with a #define inside
-// CoulombGaugeFixing.cpp, so the loop is restated here around the reference's own
-// LosAlamosAlgorithm / JacobiAlgorithm::UpdateGaugeTransformation; the log rows come from the
-// Global* monitors at full precision.  uniforms: the values rng() returns, in call order.
+// Per-slice Coulomb gauge deviation of the reference's gauge-fixed links GaugeFixedVariables::U, with
+// its own deviation macro GET_LOCAL_GAUGE_VIOLATION (S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41):
+// zmax[z] = max |Delta^a|, zsq[z] = sum Delta^a^2 over slice z.
+void ref_coulomb_profile(double* zmax, double* zsq) {
+  using namespace CoulombGaugeFixing;
+  GaugeLinks* UGaugeTransformed = GaugeFixedVariables::U;
+  SET_GAUGE_DEVIATION_BUFFERS();
+  for (int z = 0; z < Lattice::N[2]; z++) {
+    double mx = 0.0, sq = 0.0;
+    for (int y = 0; y < Lattice::N[1]; y++)
+      for (int x = 0; x < Lattice::N[0]; x++) {
+        GET_LOCAL_GAUGE_VIOLATION(x, y, z);
+        for (int a = 0; a < SUNcAlgebra::NumberOfGenerators; a++) {
+          mx = std::max(mx, std::abs(DeviationBuffer[a]));
+          sq += DeviationBuffer[a] * DeviationBuffer[a];
+        }
+      }
+    zmax[z] = mx;
+    zsq[z] = sq;
+  }
+}
+
+// SetCoulombGauge's loop (S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:32-88) around one of the
+// reference's own updates: the Fourier-accelerated one (algorithm 0, param = alphaStepSize), Los Alamos
+// (1, param = OverRelaxationProbability) or Jacobi (2, param = alphaStepSize).  The reference selects its
+// algorithm with a #define inside CoulombGaugeFixing.cpp and logs with the stream's default 6 digits, so
+// the loop is restated here; the log rows come from the Global* monitors at full precision, into log_out
+// and, row by row and flushed, into <outdir>/HarnessCoulombRows.txt (which survives the exit(0) of the
+// unitarity guard).  uniforms: the values rng() returns, in call order.
 int ref_coulomb_local(int algorithm, double param, const double* uniforms, long n_uniforms, int total_steps,
                       double* log_out, int max_rows) {
   RandomNumberGenerator::Uniforms.assign(uniforms, uniforms + n_uniforms);
   RandomNumberGenerator::UniformCursor = 0;
-  if (algorithm == 1)
+  if (algorithm == 0)
+    CoulombGaugeFixing::FourierAccelerationAlgorithm::alphaStepSize = param;
+  else if (algorithm == 1)
     CoulombGaugeFixing::LosAlamosAlgorithm::OverRelaxationProbability = param;
   else
     CoulombGaugeFixing::JacobiAlgorithm::alphaStepSize = param;
+  FILE* rows = std::fopen((g_outdir + "/HarnessCoulombRows.txt").c_str(), "w");
   GaugeTransformation::Operations::CopyFields();
   GaugeTransformation::Operations::GaugeTransformLinks();
   CoulombGaugeFixing::GlobalMaxDeviation = 1;
   int n = 0;
   while (n < total_steps && CoulombGaugeFixing::GlobalMaxDeviation > std::pow(10.0, -15)) {
-    if (algorithm == 1)
+    if (algorithm == 0)
+      CoulombGaugeFixing::FourierAccelerationAlgorithm::UpdateGaugeTransformation();
+    else if (algorithm == 1)
       CoulombGaugeFixing::LosAlamosAlgorithm::UpdateGaugeTransformation();
     else
       CoulombGaugeFixing::JacobiAlgorithm::UpdateGaugeTransformation();
-    if (n < max_rows) {
-      double* o = log_out + 7 * n;
-      o[0] = n;
-      o[1] = CoulombGaugeFixing::GlobalMaxDeviation;
-      o[2] = CoulombGaugeFixing::GlobalAvgDeviation;
-      o[3] = CoulombGaugeFixing::GlobalMaxStepSize;
-      o[4] = CoulombGaugeFixing::GlobalAvgStepSize;
-      o[5] = CoulombGaugeFixing::GlobalMinGaugeFunctional;
-      o[6] = CoulombGaugeFixing::GlobalSumGaugeFunctional;
+    const double row[7] = {(double)n,
+                           CoulombGaugeFixing::GlobalMaxDeviation,
+                           CoulombGaugeFixing::GlobalAvgDeviation,
+                           CoulombGaugeFixing::GlobalMaxStepSize,
+                           CoulombGaugeFixing::GlobalAvgStepSize,
+                           CoulombGaugeFixing::GlobalMinGaugeFunctional,
+                           CoulombGaugeFixing::GlobalSumGaugeFunctional};
+    if (n < max_rows)
+      for (int k = 0; k < 7; k++) log_out[7 * n + k] = row[k];
+    if (rows) {
+      for (int k = 0; k < 7; k++) std::fprintf(rows, k ? " %.17g" : "%.17g", row[k]);
+      std::fprintf(rows, "\n");
+      std::fflush(rows);
     }
     n++;
   }
+  if (rows) std::fclose(rows);
   GaugeTransformation::Operations::GaugeTransformLinks();
   GaugeTransformation::Operations::GaugeTransformElectricFields();
   return n;

@@ -19,6 +19,7 @@ FIELDS = {"U": 0, "UOld": 1, "E": 2, "Jp": 3, "Jm": 4, "JpStat": 5, "JmStat": 6,
 STEP_SAVE_UOLD = 0x1
 GF_PROJECT_ZERO_MODE = 0x1
 GF_FFT_FP32 = 0x2
+GF_OPEN_Z = 0x4
 GF_ALGORITHMS = {"fourier": 0, "los_alamos": 1, "jacobi": 2}
 
 

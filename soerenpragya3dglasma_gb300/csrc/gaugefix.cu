@@ -8,6 +8,14 @@
 //   FFT         8 colours, unnormalised, forward sign -1 (FFTW semantics of S/FFT/FFT3D.cpp:126-138)
 //   accelerate  Delta(p) <- Delta(p) / (p^2 V) for p^2 > 0; the p = 0 mode is left as it is
 //               (optionally projected out: GLASMA_GF_PROJECT_ZERO_MODE)
+// With open z boundaries the reference's deviation counts the top slice's forward z link (into the
+// ghost slice) at one end only.  Its contribution cannot be gauged away (the ghost G follows the top
+// slice, so the link is only conjugated), sum_x Delta(x) is then not zero, and the unnormalised
+// p = 0 mode turns it into a global rotation V times too large: the iteration leaves SU(3) (the
+// compiled reference exits on its unitarity guard within a few tens of iterations on an evolved MV
+// collision).  GLASMA_GF_OPEN_Z leaves that link out of the deviation, which makes Delta the gradient
+// of sum Re tr UG over the links inside the lattice; sum_x Delta(x) is then zero up to rounding and
+// the iteration converges (documented variant; the reference's iteration stays the default).
 //   inverse FFT
 //   update      wt = exp(-i alpha t.Re Delta), guard ||wt wt^d - 1|| <= 1e-13, G <- wt^d G
 //   transform   UG_mu(x) = G(x) U_mu(x) G^d(x+mu), reading the ghost G(x,y,Nz) before the ghost
@@ -85,15 +93,20 @@ __device__ __forceinline__ long long nbr(const Geometry& g, int x, int y, int z,
 }
 
 // w(x) = sum_mu c_mu (UG_mu(x) + UG_mu^d(x - mu)) at interior site s = (x, y, z); c2 = 0 when Nz = 1
-// (GET_LOCAL_GAUGE_VIOLATION, S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41)
+// (GET_LOCAL_GAUGE_VIOLATION, S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41).
+// open_top (GLASMA_GF_OPEN_Z): the forward z link of the top slice, which points into the ghost slice,
+// is left out, so that every link in w is counted at both of its ends (the backward z link of slice 0
+// is the identity ghost, which adds nothing to Delta) and Delta is the gradient of one functional.
 template <typename T>
 __device__ __forceinline__ void site_w(const Geometry& g, const cx<T>* UG, int x, int y, int z, long long s, double c0,
-                                       double c1, double c2, Mat<double>& w) {
+                                       double c1, double c2, Mat<double>& w, int open_top = 0) {
   const double c[3] = {c0, c1, c2};
   const long long back[3] = {nbr(g, x, y, z, -1, 0, 0), nbr(g, x, y, z, 0, -1, 0), s - g.plane};
+  const double fwd2 = (open_top && z == g.nz - 1) ? 0.0 : 1.0;
   set_zero(w);
   for (int mu = 0; mu < 3; mu++) {
     if (c[mu] == 0.0) continue;
+    const double cf = mu == 2 ? fwd2 : 1.0;
     Mat<double> u, d;
     ld_d(UG, g.S, mu * 9, s, u);
     ld_d(UG, g.S, mu * 9, back[mu], d);
@@ -102,8 +115,8 @@ __device__ __forceinline__ void site_w(const Geometry& g, const cx<T>* UG, int x
 #pragma unroll
       for (int j = 0; j < 3; j++) {
         const int k = i + 3 * j, kt = j + 3 * i;
-        w.e[k].re += c[mu] * (u.e[k].re + d.e[kt].re);
-        w.e[k].im += c[mu] * (u.e[k].im - d.e[kt].im);
+        w.e[k].re += c[mu] * (cf * u.e[k].re + d.e[kt].re);
+        w.e[k].im += c[mu] * (cf * u.e[k].im - d.e[kt].im);
       }
   }
 }
@@ -114,7 +127,7 @@ __device__ __forceinline__ void site_w(const Geometry& g, const cx<T>* UG, int x
 // min ReTr w, sum ReTr w}
 template <typename T, typename C>
 __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const cx<T>* UG, double c0, double c1,
-                                                               double c2, C* X, double* partials) {
+                                                               double c2, C* X, double* partials, int open_top) {
   double v[4] = {0.0, 0.0, 1.0e300, 0.0};
   const int op[4] = {1, 0, 2, 0};
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
@@ -123,7 +136,7 @@ __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const
     const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
     const long long s = idx + g.plane;
     Mat<double> w;
-    site_w(g, UG, x, y, z, s, c0, c1, c2, w);
+    site_w(g, UG, x, y, z, s, c0, c1, c2, w, open_top);
     Alg<double> dev;
     retr_itg(w, 1.0, dev);
 #pragma unroll
@@ -690,11 +703,12 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
   float2* X32 = static_cast<float2*>(s->X);
   const long long tot = 4 * g.vol;
   const int project = (flags & GLASMA_GF_PROJECT_ZERO_MODE) ? 1 : 0;
+  const int open_top = (flags & GLASMA_GF_OPEN_Z) ? 1 : 0;
   while (n < max_iters && gmax > tol) {
     if (fft32)
-      deviation_kernel<T, float2><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], X32, part_dev);
+      deviation_kernel<T, float2><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], X32, part_dev, open_top);
     else
-      deviation_kernel<T, double2><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], X64, part_dev);
+      deviation_kernel<T, double2><<<nb, kGfThreads, 0, st>>>(g, UG, cw[0], cw[1], cw[2], X64, part_dev, open_top);
     red::finish_kernel<4><<<1, red::kThreads, 0, st>>>(part_dev, (int)nb, 1 | (0 << 2) | (2 << 4) | (0 << 6), res);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "deviation");
     e = fft32 ? fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 0, s->twiddles, st);

@@ -25,6 +25,13 @@ Fixtures (npz, float64/complex128, reference host layout with ghost slices):
                         the subnormal range where the reference's eigen-decomposition exp
                         fails): per-slice sums of squares of every field, and the full
                         fields on ten slices; inputs regenerated from PCG64 seeds
+  coulomb_mv.npz        evolved MV collisions on 8x8x16 and 16x16x32: the reference's
+                        Fourier-accelerated iteration run to its own stop rule (it exits on its
+                        unitarity guard), its full-precision log, where it exited, per-slice
+                        deviation profiles, and the 8x8x16 state (U, E) with the G it reached
+  config1_collision.npz the plain-method collision at full size (32x32x128 MV nuclei, 200 steps
+                        at dt 0.125): bulk observables, Gauss-law and unitarity violation every
+                        10 steps, the Gauss-law z-profile every 100, from injected charges
   coulomb_local.npz     4x3x5 anisotropic lattice, weak field in a random gauge: the
                         reference's Los Alamos update (over-relaxation probability 0, and
                         0.5 with the draws injected into its rng()) and its Jacobi update,
@@ -242,6 +249,107 @@ def tmd_case(q):
     q.put(res)
 
 
+COULOMB_MV = dict(N=(8, 8, 16), N_large=(16, 16, 32), a=(1.0, 1.0, 1.0), dt=0.125, qs=0.5, sigma=2.0, lam=1.65,
+                  meff=0.2, seed=1003, seed_large=1004, steps=20, steps_large=40, alpha=0.96, max_iters=1000)
+
+
+def _coulomb_mv_state(ref, N, seed, steps):
+    """MV collision (centres Nz/2 -+ Nz/4, the parameters of COULOMB_MV) evolved `steps` steps."""
+    c = COULOMB_MV
+    g = mv_gaussians(N, seed)
+    ref.mv_init(g, c["dt"], c["qs"], c["qs"], N[2] // 2 - N[2] // 4, N[2] // 2 + N[2] // 4, c["sigma"], c["lam"],
+                c["meff"])
+    ref.update(steps, c["dt"])
+    return g
+
+
+def _coulomb_mv_child(q, N, seed, steps, iters):
+    """Child process: the MV state, then SetCoulombGauge's loop with the reference's own
+    Fourier-accelerated update for `iters` iterations.  The reference calls exit(0) when its unitarity
+    guard fires, so everything the parent needs before that is sent first, and the log is read back
+    from the rows file the harness flushes after every iteration."""
+    c = COULOMB_MV
+    ref = O.Reference(N, c["a"])
+    _coulomb_mv_state(ref, N, seed, steps)
+    ref.coulomb_fix_local("fourier", c["alpha"], 0)  # no iteration: the gauge-fixed links are U itself
+    q.put({"outdir": ref._tmp, "U": ref.get("U"), "E": ref.get("E"), "profile0": ref.coulomb_profile()})
+    log = ref.coulomb_fix_local("fourier", c["alpha"], iters)
+    q.put({"log": log, "G": ref.get("G"), "profile": ref.coulomb_profile()})
+
+
+def _coulomb_mv_run(N, seed, steps, iters):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    p = ctx.Process(target=_coulomb_mv_child, args=(q, N, seed, steps, iters))
+    p.start()
+    first = q.get(timeout=600)
+    second = None
+    while second is None:
+        try:
+            second = q.get(timeout=1)
+        except Exception:
+            if not p.is_alive():
+                break
+    p.join()
+    if second is None:  # the guard fired: read the rows logged (full precision) before it exited
+        second = {"log": np.loadtxt(os.path.join(first["outdir"], "HarnessCoulombRows.txt"), ndmin=2)}
+    return first, second
+
+
+def coulomb_mv_case(q):
+    """The reference's own Fourier-accelerated iteration (alpha_ref 0.96) on evolved MV collisions, run
+    to its own stop rule (max deviation <= 1e-15, or 1000 iterations).  On open-z lattices it leaves
+    SU(3) and exits on its unitarity guard; the fixture records where, its log up to there, and the
+    per-slice deviation (from the reference's own deviation macro) before the first and after the last
+    completed iteration (a second run stopped there).  The 8x8x16 state itself is stored so that the
+    oracle and the GPU can run on it; the 16x16x32 one is rebuilt from its charges."""
+    c = COULOMB_MV
+    res = {}
+    for tag, N, seed, steps in (("s", c["N"], c["seed"], c["steps"]), ("l", c["N_large"], c["seed_large"],
+                                                                      c["steps_large"])):
+        first, second = _coulomb_mv_run(N, seed, steps, c["max_iters"])
+        log = second["log"]
+        rows = len(log)
+        exited = rows < c["max_iters"] and not (rows and log[-1, 1] <= 1e-15)
+        res[tag + "_log"] = log
+        res[tag + "_exited_on_guard"] = np.array(exited)
+        res[tag + "_profile0_max"], res[tag + "_profile0_sq"] = first["profile0"]
+        _, last = _coulomb_mv_run(N, seed, steps, rows)
+        res[tag + "_profile_max"], res[tag + "_profile_sq"] = last["profile"]
+        res[tag + "_gauss_in"] = mv_gaussians(N, seed)
+        if tag == "s":
+            res["s_U"], res["s_E"] = first["U"], first["E"]
+            res["s_G"] = last["G"]
+    q.put(res)
+
+
+CONFIG1 = dict(N=(32, 32, 128), a=(1.0, 1.0, 1.0), dt=0.125, qs=0.5, sigma=4.0, lam=1.65, meff=0.2, seed=1001,
+               centers=(40, 88), steps=200, every=10)
+
+
+def config1_case(q):
+    """The plain-method collision at its full size: two MV nuclei on 32x32x128 (g^2 mu 0.5, m 0.2,
+    sigma_z 4, centres 40/88, SingleSheet over z in [0,63] and [64,127] as Simulation::Run sets them
+    up), 200 leapfrog steps at dt 0.125, the bulk observables and the Gauss-law violation every 10
+    steps (Simulation::Evolve measures every 20 and 1000; the denser cadence is the benchmark's)."""
+    c = CONFIG1
+    N = c["N"]
+    g = mv_gaussians(N, c["seed"])
+    ref = O.Reference(N, c["a"])
+    ref.mv_init(g, c["dt"], c["qs"], c["qs"], c["centers"][0], c["centers"][1], c["sigma"], c["lam"], c["meff"])
+    bulk, gauss, unit, prof = [], [], [], []
+    for k in range(c["steps"] // c["every"] + 1):
+        if k:
+            ref.update(c["every"], c["dt"])
+        bulk.append(ref.bulk())
+        gauss.append(ref.gauss())
+        unit.append(ref.unitarity())
+        if k % 10 == 0:
+            prof.append(ref.gauss_profile())
+    q.put({"gauss_in": g, "bulk": np.array(bulk), "gauss": np.array(gauss), "unitarity": np.array(unit),
+           "gauss_profile": np.array(prof)})
+
+
 # fixture name -> (case function, configuration stored beside it); the functions run in spawned
 # children, so they are named here rather than passed as closures
 CASES = {
@@ -252,6 +360,8 @@ CASES = {
     "config_text": ("config_case", CONFIG),
     "coulomb_local": ("local_case", LOCAL),
     "tmd_glauber": ("tmd_case", TMD),
+    "coulomb_mv": ("coulomb_mv_case", COULOMB_MV),
+    "config1_collision": ("config1_case", CONFIG1),
 }
 
 

@@ -147,3 +147,80 @@ def test_unitarity_guard_returns_status_instead_of_exiting():
         lat.upload("U", f["U"])
         lat.gauge_reset()
         assert len(lat.coulomb_fix(0.5, 2)) == 2
+
+
+def _coulomb_mv(golden_dir):
+    g = dict(np.load(os.path.join(golden_dir, "coulomb_mv.npz")))
+    return g, tuple(int(v) for v in g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_alpha"])
+
+
+def test_reference_iteration_on_mv_state_exits_like_the_reference(golden_dir):
+    """On an evolved MV collision the reference's own iteration leaves SU(3) and exits on its guard
+    (golden: the compiled reference run to its stop rule).  The GPU follows its full-precision log
+    while the iteration is well conditioned and returns GLASMA_ERR_NUMERICAL where the reference
+    calls exit(0); later iterations amplify rounding (tests/test_oracle_golden.py has the control)."""
+    g, N, a, alpha = _coulomb_mv(golden_dir)
+    with Lattice(N, a) as lat:
+        lat.upload("U", g["s_U"])
+        lat.upload("E", g["s_E"])
+        log = lat.coulomb_fix(alpha, 5)
+        ref = g["s_log"][:5]
+        assert np.max(np.abs(log[:, 1:] - ref[:, 1:]) / np.abs(ref[:, 1:])) < 1e-10
+        lat.gauge_reset()
+        with pytest.raises(GlasmaError) as ei:
+            lat.coulomb_fix(alpha, 1000)
+        assert ei.value.status == 5 and 5 < len(ei.value.log) < 1000
+
+
+@pytest.mark.parametrize("fft_fp32", [False, True])
+def test_open_z_converges_on_reference_state(oracle, golden_dir, fft_fp32):
+    """GLASMA_GF_OPEN_Z on the state the reference fails on: converges to the reference's own stop
+    rule (max |Delta| <= 1e-15), and the gauge-fixed fields equal the oracle's converged ones."""
+    g, N, a, alpha = _coulomb_mv(golden_dir)
+    f = {"U": g["s_U"].copy(), "E": g["s_E"].copy()}
+    G = O.identity_gauge(N)
+    st, olog, UG, EG = oracle.coulomb_fix(f, G, N, a, alpha, 1000, flags=O.GF_OPEN_Z)
+    assert st == 0 and olog[-1, 1] <= 1e-15
+    with Lattice(N, a) as lat:
+        lat.upload("U", f["U"])
+        lat.upload("E", f["E"])
+        log = lat.coulomb_fix(alpha, 1000, open_z=True, fft_fp32=fft_fp32)
+        assert log[-1, 1] <= 1e-15 and len(log) < 1000
+        assert np.max(np.abs(lat.download("UG") - UG)) < 1e-10
+        assert np.max(np.abs(lat.download("EG") - EG)) < 1e-10 * np.max(np.abs(EG))
+        assert np.max(np.abs(lat.download("G") - G)) < 1e-10
+    if not fft_fp32:
+        # theta = <Delta^2> history, while it is above the rounding floor
+        th, oth = log[:, 2] ** 2, olog[:, 2] ** 2
+        m = min(len(th), len(oth))
+        k = oth[:m] > 1e-20
+        assert np.allclose(th[:m][k], oth[:m][k], rtol=1e-6)
+
+
+def test_open_z_converged_fields_match_oracle_16x16x32(oracle, golden_dir):
+    """16x16x32 MV collision built and evolved on the GPU (40 steps from the charges of the golden
+    16x16x32 case), then Coulomb-fixed with GLASMA_GF_OPEN_Z through theta < 1e-10 to the reference's
+    stop rule; the oracle runs the same variant on the downloaded fields.  Converged UG, EG and theta
+    agree to 1e-10 (a converged gauge is an attractive fixed point: rounding does not grow)."""
+    g, _, a, alpha = _coulomb_mv(golden_dir)
+    N = tuple(int(v) for v in g["cfg_N_large"])
+    n = 8 * N[0] * N[1]
+    zl, zr = g["l_gauss_in"][:n], g["l_gauss_in"][n:]
+    dt = float(g["cfg_dt"])
+    with Lattice(N, a) as lat:
+        lat.mv_init(zl, zr, qs=(float(g["cfg_qs"]),) * 2, centers=(N[2] // 2 - N[2] // 4, N[2] // 2 + N[2] // 4),
+                    sigma=float(g["cfg_sigma"]), lam=float(g["cfg_lam"]), meff=float(g["cfg_meff"]), dt=dt)
+        lat.step(dt, int(g["cfg_steps_large"]))
+        f = lat.download_fields()
+        log = lat.coulomb_fix(alpha, 2000, open_z=True)
+        UGg, EGg = lat.download("UG"), lat.download("EG")
+    G = O.identity_gauge(N)
+    st, olog, UG, EG = oracle.coulomb_fix(f, G, N, a, alpha, 2000, flags=O.GF_OPEN_Z)
+    assert st == 0 and olog[-1, 1] <= 1e-15 and log[-1, 1] <= 1e-15
+    th, oth = log[:, 2] ** 2, olog[:, 2] ** 2
+    assert abs(int(np.argmax(th < 1e-10)) - int(np.argmax(oth < 1e-10))) <= 1 and np.argmax(oth < 1e-10) < 300
+    m = min(len(th), len(oth))
+    k = oth[:m] > 1e-20
+    assert np.allclose(th[:m][k], oth[:m][k], rtol=1e-6)
+    assert np.max(np.abs(UGg - UG)) < 1e-10
+    assert np.max(np.abs(EGg - EG)) < 1e-10 * np.max(np.abs(EG))

@@ -93,3 +93,61 @@ def test_local_gauge_fixers_match_reference(oracle, golden_dir, tag, alg, param)
     assert np.allclose(log, g[tag + "_log"], rtol=1e-10, atol=1e-14)
     for k, v in (("G", G), ("UG", UG), ("EG", EG)):
         assert np.max(np.abs(v - g[tag + "_" + k])) < tol, k
+
+
+def _coulomb_mv(golden_dir):
+    g = _load(golden_dir, "coulomb_mv.npz")
+    return g, tuple(int(v) for v in g["cfg_N"]), tuple(g["cfg_a"]), float(g["cfg_alpha"])
+
+
+def test_coulomb_mv_reference_iteration_exits_on_guard(oracle, golden_dir):
+    """The reference's own Fourier-accelerated iteration on an evolved MV collision (open z) leaves
+    SU(3) and exits on its unitarity guard; the oracle follows its full-precision log while the
+    iteration is still well conditioned and exits on the same guard.  After that the iteration
+    amplifies rounding ~30x per step (its unnormalised p = 0 mode carries V sum Delta): the oracle
+    run against itself from links perturbed by 1e-15 diverges the same way (chaos control)."""
+    g, N, a, alpha = _coulomb_mv(golden_dir)
+    assert bool(g["s_exited_on_guard"]) and bool(g["l_exited_on_guard"])
+    f = {"U": g["s_U"].copy(), "E": g["s_E"].copy()}
+    st, log, _, _ = oracle.coulomb_fix(f, O.identity_gauge(N), N, a, alpha, 1000)
+    assert st == 5  # the unitarity guard, where the reference calls exit(0)
+    ref = g["s_log"]
+    rel = np.abs(log[:5, 1:] - ref[:5, 1:]) / np.abs(ref[:5, 1:])
+    assert rel.max() < 1e-10, rel.max(axis=1)
+    rng = np.random.default_rng(0)
+    f2 = {"U": g["s_U"] * (1 + 1e-15 * rng.standard_normal(g["s_U"].shape)), "E": g["s_E"].copy()}
+    st2, log2, _, _ = oracle.coulomb_fix(f2, O.identity_gauge(N), N, a, alpha, 1000)
+    assert st2 == 5
+    m = min(len(log), len(log2), 9)
+    ctrl = (np.abs(log2[:m, 1:] - log[:m, 1:]) / np.abs(log[:m, 1:])).max(axis=1)
+    vs_ref = (np.abs(log[:m, 1:] - ref[:m, 1:]) / np.abs(ref[:m, 1:])).max(axis=1)
+    # both grow from the rounding level to ~1e-6 within 9 iterations
+    assert ctrl[0] < 1e-13 and ctrl[-1] > 1e-8 and vs_ref[-1] > 1e-8
+
+
+def test_coulomb_mv_reference_boundary_profile(golden_dir):
+    """Where the reference stops, its deviation is largest in the two boundary slices."""
+    g, N, _, _ = _coulomb_mv(golden_dir)
+    for t in ("s", "l"):
+        prof = g[t + "_profile_max"]
+        assert min(prof[0], prof[-1]) > 3 * np.max(prof[1:-1]), prof
+
+
+def test_coulomb_mv_open_z_converges(oracle, golden_dir):
+    """The open-z functional (the top slice's z link into the ghost left out of the deviation)
+    converges on the same state to the reference's own stop rule, max |Delta| <= 1e-15, in every
+    slice, and leaves the p = 0 mode of the update at the rounding level."""
+    g, N, a, alpha = _coulomb_mv(golden_dir)
+    f = {"U": g["s_U"].copy(), "E": g["s_E"].copy()}
+    G = O.identity_gauge(N)
+    st, log, UG, EG = oracle.coulomb_fix(f, G, N, a, alpha, 1000, flags=O.GF_OPEN_Z)
+    assert st == 0 and log[-1, 1] <= 1e-15 and len(log) < 1000
+    theta = log[:, 2] ** 2
+    assert np.argmax(theta < 1e-10) < 100
+    # projecting the p = 0 mode out changes nothing: sum_x Delta(x) = 0 for this functional
+    G2 = O.identity_gauge(N)
+    _, log2, UG2, _ = oracle.coulomb_fix(f, G2, N, a, alpha, 1000, flags=O.GF_OPEN_Z | O.GF_PROJECT_ZERO_MODE)
+    assert abs(len(log2) - len(log)) <= 2 and _rel(UG2, UG) < 1e-12
+    # links stay in SU(3)
+    M = O.links_as_matrices(UG)[1:-1]
+    assert np.max(np.abs(M @ np.swapaxes(M.conj(), -1, -2) - np.eye(3))) < 1e-12
