@@ -45,10 +45,11 @@ KERNEL_BYTES = {
     "links_j": {"fp64": 192 + 2 * 432 + 128 + 2 * 128, "fp32": 96 + 2 * 216 + 64 + 2 * 64,
                 "fp32_l12": 96 + 2 * 144 + 64 + 2 * 64},
     "fused_step": {"fp64": 1760, "fp32": 880, "fp32_l12": 736},  # one pass: every per-site array read and written once
-    # plaquette method: K1 as two-pass plus the 48 contribution reals written per site; K2 as two-pass
-    # plus those reals read and E written
-    "plaquette_forces": {"fp64": 1200 + 384, "fp32": 600 + 192, "fp32_l12": 528 + 192},
-    "links_gather": {"fp64": 1440 + 384 + 192, "fp32": 720 + 192 + 96, "fp32_l12": 576 + 192 + 96},
+    # plaquette method: the same compulsory state traffic as K1 / K2 (the 48 contribution reals per site
+    # the force kernel hands to the link kernel are an intermediate of this method, not algorithmic
+    # bytes; ncu's DRAM traffic shows what they cost)
+    "plaquette_forces": {"fp64": 1200, "fp32": 600, "fp32_l12": 528},
+    "links_gather": {"fp64": 1440, "fp32": 720, "fp32_l12": 576},
 }
 STEP_BYTES = {"fp64": 1760, "fp32": 880, "fp32_l12": 736}  # every per-site state array read and written once
 FALLBACK_HBM_GBS = 6800.0
@@ -194,39 +195,79 @@ def numpy_inputs(N, seed):
 
 
 # ----------------------------------------------------------------------------- CPU legs
-def time_oracle(fields, N, threads, min_seconds, max_steps):
-    from oracle import oracle as O
+# Both CPU legs time the same bounded sample of the workload: full leapfrog steps (SaveOldLink included,
+# as Dynamics::SUNc::Update does) of a 128x128x32 slab of the lattice, on all host threads.
+CPU_SLAB_NZ = 32
 
-    orc = O.Oracle(threads=threads)
-    orc.update(fields, N, A_WORK, DT, 1, save_uold=False)  # warm-up
+
+def cpu_impl():
+    """'reference' where the reference's own code compiled here (oracle/_ref, built only where the
+    reference checkout exists), else 'port' (the oracle restatement, built everywhere)."""
+    from oracle import build as ob
+
+    return "reference" if ob.reference_source_dir() and ob.build_reference() else "port"
+
+
+class CpuStepper:
+    """One full leapfrog step of a slab on the host CPU, by the reference's own compiled code or by the
+    oracle restatement; `threads` = the OpenMP threads it runs on."""
+
+    def __init__(self, fields, N, impl):
+        from oracle import oracle as O
+
+        self.impl, self.N = impl, N
+        threads = os.cpu_count() or 1
+        if impl == "reference":
+            self.ref = O.Reference(N, A_WORK, threads=threads)
+            self.ref.set_fields(fields)
+            self.threads = threads
+        else:
+            self.orc = O.Oracle(threads=threads)
+            self.fields = fields
+            self.threads = self.orc.threads()
+
+    def step(self):
+        if self.impl == "reference":
+            self.ref.update(1, DT)
+        else:
+            self.orc.update(self.fields, self.N, A_WORK, DT, 1, save_uold=True)
+
+
+def cpu_sample_desc(n, secs, threads, impl):
+    who = "the reference's own code compiled from its sources" if impl == "reference" else "oracle restatement"
+    return ("%s leapfrog steps (Dynamics::SUNc::Update incl. SaveOldLink) of a %dx%dx%d slab of the workload%s, "
+            "%s, %d threads" % (n, N_WORK[0], N_WORK[1], CPU_SLAB_NZ, "" if secs is None else " in %.1f s" % secs,
+                               who, threads))
+
+
+def time_cpu(fields, min_seconds, max_steps, impl):
+    slab = (N_WORK[0], N_WORK[1], CPU_SLAB_NZ)
+    st = CpuStepper(fields, slab, impl)
+    st.step()  # warm-up
     t0 = time.perf_counter()
     n = 0
     while n < max_steps:
-        orc.update(fields, N, A_WORK, DT, 1, save_uold=False)
+        st.step()
         n += 1
         if time.perf_counter() - t0 > min_seconds:
             break
     dt = time.perf_counter() - t0
-    sites = N[0] * N[1] * N[2]
-    return sites * n / dt, n, dt, orc.threads()
+    return slab[0] * slab[1] * slab[2] * n / dt, n, dt, st.threads
 
 
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    slab = (N_WORK[0], N_WORK[1], 32)
-    fields = numpy_inputs(slab, SEED)
-    threads = os.cpu_count() or 1
-    from oracle import oracle as O
-
-    orc = O.Oracle(threads=threads)
+    slab = (N_WORK[0], N_WORK[1], CPU_SLAB_NZ)
+    impl = cpu_impl() if args.cpu_impl == "auto" else args.cpu_impl
+    st = CpuStepper(numpy_inputs(slab, SEED), slab, impl)
     for _ in range(args.warmup):
-        orc.update(fields, slab, A_WORK, DT, 1, save_uold=True)
+        st.step()
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        orc.update(fields, slab, A_WORK, DT, 1, save_uold=True)
+        st.step()
         times.append(time.perf_counter() - t0)
     sites = slab[0] * slab[1] * slab[2]
     ms = 1e3 * sum(times) / len(times)
@@ -244,16 +285,26 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded SU(3) links / E / currents with the workload's shapes)",
-        "config": {"workload": "glasma leapfrog 128x128x512 FP64 (plain method, production size)",
-                   "lattice": list(N_WORK), "dt": DT},
-        "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": orc.threads(), "kind": "port",
-                         "sample": "each step = one full leapfrog step of a 128x128x32 slab of the workload "
-                                   "(Dynamics::SUNc::Update incl. SaveOldLink), oracle restatement, %d threads"
-                                   % orc.threads()},
+        "data": DATA_DESC,
+        "config": workload_config(world),
+        "sample": {"lattice": list(slab), "note": "each step is one full leapfrog step of this slab of the "
+                                                  "workload's lattice; site-updates/s are per slab site"},
+        "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": st.threads, "kind": impl,
+                         "sample": cpu_sample_desc("each of %d" % args.steps, None, st.threads, impl)},
         "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def workload_config(world):
+    """The config object both arms print (identical, so the two lines describe one workload)."""
+    N = N_WORK
+    return {"workload": "glasma leapfrog %dx%dx%d FP64 (plain method, production size)" % N,
+            "lattice": list(N), "dt": DT, "a": list(A_WORK), "parallelism": "replicas" if world > 1 else "1 GPU",
+            "l2": "inputs larger than L2 (%.1f GB of FP64 state)" % (STEP_BYTES["fp64"] / 2 * N[0] * N[1] * N[2] / 1e9)}
+
+
+DATA_DESC = "synthetic (seeded SU(3) links exp(i 0.3 t.r), E ~ N(0,0.01), J ~ N(0,4e-4); workload shapes)"
 
 
 # ----------------------------------------------------------------------------- GPU leg
@@ -313,16 +364,18 @@ def run_ours(args):
     def roofline(name, prec, ms):
         alg = KERNEL_BYTES[name][prec] * vol
         ach = alg / (ms * 1e-3) / 1e9
-        tr = traffic.get("%s_%s" % (name, prec))
-        out = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
-               "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr,
-               "algorithmic_bytes_per_launch": alg, "launch_ms": ms}
-        # the pipe that actually limits the kernel, from the ncu capture of the same kernel (the FP64
-        # kernels sit at ~95 % of GB300's FP64 pipe, which is why their HBM fraction is small)
         key = "%s_%s" % (name, prec)
+        tr = traffic.get(key)
+        # what limits the kernel, from the ncu capture of the same kernel: the FP64 kernels keep GB300's
+        # FP64 pipe >90 % busy (hence their small HBM fraction), the FP32 ones are bound by HBM traffic
+        # and issue
         pa = traffic.get("pipe_active", {}).get(key)
-        if pa:
-            out["pipe_active"] = dict(pa, source=traffic.get("sources", {}).get(key))
+        bound = "fp64_pipe" if pa and pa.get("pipe") == "fp64" and pa.get("frac", 0) > 0.8 else "hbm"
+        out = {"bound": bound, "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
+               "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr,
+               "algorithmic_bytes_per_launch": alg, "launch_ms": ms,
+               "pipe_active": pa.get("frac") if pa else None, "pipe": pa.get("pipe") if pa else None,
+               "pipe_source": traffic.get("sources", {}).get(key)}
         return out
 
     def max_over_ranks(x):
@@ -578,12 +631,11 @@ def run_ours(args):
     # ---- CPU baseline (rank 0 at N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        nz_slab = min(64, N[2])
-        hs = host_slab(inputs, nz_slab)
-        rate, n, secs, threads = time_oracle(hs, (N[0], N[1], nz_slab), os.cpu_count(), 10.0, 50)
-        cpu = {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
-               "sample": "%d leapfrog steps of a %dx%dx%d slab of the workload in %.1f s, oracle "
-                         "restatement, %d threads" % (n, N[0], N[1], nz_slab, secs, threads)}
+        hs = host_slab(inputs, CPU_SLAB_NZ)
+        impl = cpu_impl() if args.cpu_impl == "auto" else args.cpu_impl
+        rate, n, secs, threads = time_cpu(hs, 10.0, 50, impl)
+        cpu = {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": impl,
+               "sample": cpu_sample_desc(n, secs, threads, impl)}
     del lat
     if world > 1:
         dist.destroy_process_group()
@@ -601,10 +653,8 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded SU(3) links exp(i 0.3 t.r), E ~ N(0,0.01), J ~ N(0,4e-4); workload shapes)",
-        "config": {"workload": "glasma leapfrog %dx%dx%d FP64 (plain method, production size)" % N,
-                   "lattice": list(N), "dt": DT, "a": list(A_WORK), "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (%.1f GB of FP64 state)" % (STEP_BYTES["fp64"] / 2 * vol / 1e9)},
+        "data": DATA_DESC,
+        "config": workload_config(world),
         "step_hbm_frac": (STEP_BYTES["fp64"] * vol / (ms_step * 1e-3) / 1e9 / peak) if ms_step else None,
         "roofline": rl,
         "kernel_ms": k_ms,
@@ -908,6 +958,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-impl", default="auto", choices=["auto", "port", "reference"],
+                    help="CPU legs: the reference's own compiled code where it was built (auto), or the oracle port")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-gauge", action="store_true", help="skip the gauge-fixing / FFT leg")
     ap.add_argument("--step-method", default="plaquette", choices=["one_pass", "two_pass", "plaquette"])

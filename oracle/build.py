@@ -5,14 +5,17 @@
 * ``oracle/_ref/libglasma_ref.so`` -- the reference's own SU(3) code path
   compiled from its unmodified sources plus the shims in ``oracle/ref``.  Built
   only where the reference checkout exists; its location comes from the
-  ``GLASMA_REFERENCE_SRC`` environment variable or the default below.
+  ``GLASMA_REFERENCE_SRC`` environment variable, else the checkout's source
+  directory next to this repository (``../reference/...`` from the repository
+  root).  Where neither exists (the GPU host) nothing is built.
 """
 import os
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF_SRC = "/root/reference/Pragya_workingdirectory_worksonm1/Workingdirectory/SourceCode"
+DEFAULT_REF_SRC = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "Pragya_workingdirectory_worksonm1",
+                               "Workingdirectory", "SourceCode")
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libglasma_ref.so")
 

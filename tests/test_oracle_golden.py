@@ -151,3 +151,14 @@ def test_coulomb_mv_open_z_converges(oracle, golden_dir):
     # links stay in SU(3)
     M = O.links_as_matrices(UG)[1:-1]
     assert np.max(np.abs(M @ np.swapaxes(M.conj(), -1, -2) - np.eye(3))) < 1e-12
+
+
+def test_config1_reference_cannot_run_the_asked_width(golden_dir):
+    """At the plain-method configuration's sigma_z 4 the reference's own MV initial state exits (its
+    eigen-decomposition fails on the ~1e-100 profile slices far from a nucleus); its full-size fixture
+    is therefore taken at sigma_z 5, the nearest width it runs, and the asked width is compared with
+    the oracle instead (tests/test_config1_gpu.py)."""
+    g = _load(golden_dir, "config1_collision.npz")
+    assert not bool(g["reference_runs_sigma_asked"])
+    assert float(g["cfg_sigma_asked"]) == 4.0 and float(g["cfg_sigma"]) == 5.0
+    assert g["bulk"].shape == (21, 16) and np.all(np.isfinite(g["bulk"]))
