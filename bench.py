@@ -836,6 +836,105 @@ def run_tmd(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args):
+    """The precision variant: one left-moving MV nucleus (SingleSheet over all z, as
+    S/LeftNucleusSimulation.cpp:357 sets it up; g^2 mu 0.5, m 0.2, sigma_z 8, centre 0.85 Nz/2 - 1),
+    256x256x1024 by default, dt 0.1, 2000 steps.  Four runs from the same seeded charges: FP64 from the
+    exact initial state, FP64 from its FP32-rounded copy, FP32 (reunitarised every 16 steps, FP64
+    reductions) and FP32 with 12-real links from that rounded copy.  Each observable's error of the FP32
+    runs is taken against the FP64 run from the same rounded start; the two FP64 runs give the floor that
+    the rounding of the start alone sets (the evolution amplifies it).  Observables every
+    --measure-every steps: T00, the electric and magnetic sums, the Gauss-law violation (max, avg), the
+    unitarity violation and P_L/P_T of the central 32 slices (from the energy-momentum map)."""
+    import numpy as np
+    import torch
+
+    from soerenpragya3dglasma_gb300 import Lattice, build
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    N = N_WORK if args.lattice else (256, 256, 1024)
+    dt, steps, every = 0.1, args.prec_steps, args.measure_every
+    centre = int(0.85 * N[2] / 2 - 1)
+    z0, z1 = N[2] // 2 - 16, N[2] // 2 + 16
+    zeta = np.random.default_rng(1003).standard_normal(8 * N[0] * N[1])
+    vol = N[0] * N[1] * N[2]
+
+    def measure(lat):
+        b = lat.bulk()
+        gmax, gavg = lat.gauss()
+        umax, uavg = lat.unitarity()
+        r, _, _ = lat.pressure_anisotropy(z0, z1)
+        return {"T00": b[9], "ELECTRIC": b[13], "MAGNETIC": b[14], "gauss_max": gmax, "gauss_avg": gavg,
+                "unitarity_max": umax, "pl_over_pt": r}
+
+    def evolve(lat):
+        rows = [measure(lat)]
+        ms = 0.0
+        for _ in range(steps // every):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lat.step(dt, every, save_uold=True)  # UOld of the last step feeds the energy-momentum map
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+            rows.append(measure(lat))
+        return rows, ms / steps
+
+    runs, rounded = {}, {}
+    t_start = time.time()
+    with Lattice(N, stream=stream) as lat:
+        lat.mv_init(zeta, None, qs=(0.5, 0.5), centers=(centre, centre), sigma=8.0, lam=1.65, meff=0.2, dt=dt)
+        for k in INPUT_FIELDS:  # the FP32-rounded copy of the start, on the device
+            buf = torch.empty(lat.field_doubles(k), dtype=torch.float64, device=dev)
+            lat.download_device(k, buf.data_ptr())
+            for c0 in range(0, buf.numel(), 1 << 28):
+                v = buf[c0:c0 + (1 << 28)]
+                v.copy_(v.to(torch.float32).to(torch.float64))
+            rounded[k] = buf
+        torch.cuda.synchronize()
+        runs["fp64_exact_start"] = evolve(lat)
+    for tag, prec, reals in (("fp64", "fp64", 18), ("fp32", "fp32", 18), ("fp32_links12", "fp32", 12)):
+        with Lattice(N, precision=prec, reunitarize_every=16 if prec == "fp32" else 0, stream=stream) as lat:
+            lat.link_reals = reals
+            for k in INPUT_FIELDS:
+                lat.upload_device(k, rounded[k].data_ptr())
+            lat.upload_device("UOld", rounded["U"].data_ptr())
+            torch.cuda.synchronize()
+            runs[tag] = evolve(lat)
+    ref = runs["fp64"][0]
+
+    def rel(rows, name, k):
+        a, b = rows[k][name], ref[k][name]
+        return abs(a - b) / abs(b) if b != 0 else abs(a - b)
+
+    names = list(ref[0].keys())
+    errors = {}
+    for tag in ("fp32", "fp32_links12", "fp64_exact_start"):
+        rows = runs[tag][0]
+        errors[tag] = {n: {"final": rel(rows, n, -1), "max_over_run": max(rel(rows, n, k) for k in range(len(rows)))}
+                       for n in names}
+    line = {
+        "workload": "precision variant: single left-moving MV nucleus %dx%dx%d (g^2 mu 0.5, m 0.2, sigma_z 8, "
+                    "centre %d), dt %g, %d steps; FP64 and FP32 (reunitarised every 16 steps) from the same "
+                    "FP32-rounded start" % (N + (centre, dt, steps)),
+        "ms_per_step": {t: runs[t][1] for t in runs},
+        "site_updates_per_s": {t: vol / (runs[t][1] * 1e-3) for t in runs},
+        "hbm_frac": {t: STEP_BYTES[{"fp64": "fp64", "fp64_exact_start": "fp64", "fp32": "fp32",
+                                    "fp32_links12": "fp32_l12"}[t]] * vol / (runs[t][1] * 1e-3) / 1e9 / hbm_peak()[0]
+                     for t in runs},
+        "rel_error_vs_fp64_same_start": {t: errors[t] for t in ("fp32", "fp32_links12")},
+        "floor_fp64_rounded_vs_exact_start": errors["fp64_exact_start"],
+        "final": {t: runs[t][0][-1] for t in runs},
+        "measure_every": every,
+        "wall_s": time.time() - t_start,
+        "note": "ms_per_step includes SaveOldLink on the last step of every %d-step call" % every,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_adjoint(args):
     """The adjoint workload: a 64x64x256 MV collision (g^2 mu = 0.5, m = 0.2, sigma_z = 4, centres
     128 -+ 24, seeded charges), FP64, 400 steps at dt = 0.125, objective P_L/P_T over the central 32
@@ -973,7 +1072,10 @@ def main():
                     help="which precisions to run (profiling runs); the JSON line needs both")
     ap.add_argument("--lattice", default=None, help="Nx,Ny,Nz instead of the workload's (profiling runs)")
     ap.add_argument("--event-shape", default=None, help="NX,NY,NZ for every batched event (profiling runs)")
-    ap.add_argument("--workload", default="production", choices=["production", "batched", "adjoint", "fft", "tmd"],
+    ap.add_argument("--prec-steps", type=int, default=2000, help="steps of the precision workload")
+    ap.add_argument("--measure-every", type=int, default=100, help="measurement cadence of the precision workload")
+    ap.add_argument("--workload", default="production",
+                    choices=["production", "batched", "adjoint", "fft", "tmd", "precision"],
                     help="production: the headline 128x128x512 line; batched: 64 uneven events in one launch; "
                          "adjoint: the gradient of P_L/P_T on a 64x64x256 collision; fft: the 3D FFT alone; "
                          "tmd: the TMD/Glauber initial state at 128x128x2048")
@@ -997,6 +1099,8 @@ def main():
         run_fft(args)
     elif args.workload == "tmd":
         run_tmd(args)
+    elif args.workload == "precision":
+        run_precision(args)
     else:
         run_ours(args)
 

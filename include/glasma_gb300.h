@@ -342,8 +342,10 @@ int glasma_fft3d_f32(glasma_lattice* h, const float* in, float* out, int inverse
  * on `stream` (a cudaStream_t, NULL = default stream); the caller synchronises.
  * Scratch is one fixed 512 KiB __device__ array per device, held until the process exits, which
  * limits nz to 992 (larger nz returns GLASMA_ERR_BAD_SHAPE).  The first call on a device looks up
- * that array's address; make it before any stream capture.  All calls on a device share the
- * array: calls that overlap on the GPU race and must be ordered by the caller. */
+ * that array's address; make it before any stream capture.  The address is cached for the process's
+ * lifetime: after a cudaDeviceReset of that device it is stale, so do not call this again after one.
+ * All calls on a device share the array: calls that overlap on the GPU race and must be ordered by the
+ * caller.  Failures are reported as by every other entry point (status, glasma_last_error()). */
 int glasma_gauss_noalloc(const double* U, const double* E, const double* JpStat, const double* JmStat, int nx, int ny,
                          int nz, double ax, double ay, double az, double a_scale, double* result, double* zprofile,
                          void* stream);

@@ -26,6 +26,15 @@ int fail(int status, const std::string& msg) {
   return status;
 }
 
+}  // namespace
+
+namespace glasma {
+// records msg as glasma_last_error() of the calling thread (for entry points in other files)
+int record_error(int status, const std::string& msg) { return fail(status, msg); }
+}  // namespace glasma
+
+namespace {
+
 int cuda_fail(cudaError_t e, const char* where) {
   return fail(GLASMA_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }

@@ -11,14 +11,15 @@
 // allocated.  Host code cannot use that array's name as a device address; the address is
 // looked up once per device with cudaGetSymbolAddress (the first call on each device does
 // this, so make that first call before any stream capture begins) and then passed to the
-// kernels.  Every call on a device shares the one array: calls whose kernels overlap on the
+// kernels.  The address is cached for the life of the process: a cudaDeviceReset (or anything
+// else that destroys the device's primary context) invalidates it, and later calls on that device
+// would then use a stale address, so do not call this entry point after such a reset.  Every call on a device shares the one array: calls whose kernels overlap on the
 // GPU (different streams without ordering) race on it and must be serialised by the caller.
 // The array keeps the last call's contents; nothing in it has to start at zero, because every
 // partial that a call reads was written earlier in the same call.
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <cstdio>
 #include <mutex>
 #include <string>
 
@@ -51,13 +52,12 @@ __global__ void finish_noalloc_kernel(const double* sums, double inv8v, double* 
 }  // namespace
 }  // namespace glasma
 
-namespace {
-thread_local std::string g_noalloc_error;
-int noalloc_fail(int status, const std::string& m) {
-  g_noalloc_error = "glasma_gauss_noalloc: " + m;
-  std::fprintf(stderr, "%s\n", g_noalloc_error.c_str());
-  return status;
+namespace glasma {
+int record_error(int status, const std::string& msg);  // glasma_abi.cu: sets glasma_last_error()
 }
+
+namespace {
+int noalloc_fail(int status, const std::string& m) { return glasma::record_error(status, "glasma_gauss_noalloc: " + m); }
 }  // namespace
 
 extern "C" int glasma_gauss_noalloc(const double* U, const double* E, const double* JpStat, const double* JmStat,
@@ -65,6 +65,8 @@ extern "C" int glasma_gauss_noalloc(const double* U, const double* E, const doub
                                     double* result, double* zprofile, void* stream) {
   using namespace glasma;
   if (nx < 2 || ny < 2 || nz < 2) return noalloc_fail(GLASMA_ERR_BAD_SHAPE, "each extent must be >= 2");
+  if ((long long)nx * ny * (nz + 2) > (1LL << 40))  // the limit glasma_create applies
+    return noalloc_fail(GLASMA_ERR_BAD_SHAPE, "lattice too large");
   if (nz > kNoAllocMaxNz)
     return noalloc_fail(GLASMA_ERR_BAD_SHAPE, "Nz = " + std::to_string(nz) + " exceeds the maximum " +
                                                   std::to_string(kNoAllocMaxNz) +

@@ -51,3 +51,14 @@ def test_create_rejects_bad_shapes(lib):
     assert lib.glasma_create(4, 4, 4, -1.0, 1.0, 1.0, 0, 0, ctypes.byref(h)) == 2
     assert lib.glasma_create(4, 4, 4, 1.0, 1.0, 1.0, 7, 0, ctypes.byref(h)) == 1
     assert lib.glasma_create(4, 4, 4, 1.0, 1.0, 1.0, 0, 0, None) == 1
+
+
+def test_gauss_noalloc_rejects_shapes_before_touching_a_device(lib):
+    """The allocation-free Gauss entry point checks its sizes first and reports through
+    glasma_last_error() like every other entry point (no device call is made for these)."""
+    p = ctypes.c_void_p(16)
+    assert lib.glasma_gauss_noalloc(p, p, p, p, 4, 4, 993, 1.0, 1.0, 1.0, 1.0, p, None, None) == 2
+    assert b"exceeds the maximum" in lib.glasma_last_error()
+    assert lib.glasma_gauss_noalloc(p, p, p, p, 1 << 20, 1 << 20, 900, 1.0, 1.0, 1.0, 1.0, p, None, None) == 2
+    assert b"too large" in lib.glasma_last_error()
+    assert lib.glasma_gauss_noalloc(p, p, p, p, 1, 4, 4, 1.0, 1.0, 1.0, 1.0, p, None, None) == 2

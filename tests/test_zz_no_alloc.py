@@ -54,3 +54,4 @@ def test_gauss_noalloc_rejects_oversized_lattice():
     p = d.data_ptr()
     st = lib.glasma_gauss_noalloc(p, p, p, p, 4, 4, 993, 1.0, 1.0, 1.0, 1.0, p, None, None)
     assert st == 2
+    assert b"exceeds the maximum" in lib.glasma_last_error()
