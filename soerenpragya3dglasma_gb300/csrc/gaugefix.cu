@@ -37,8 +37,8 @@
 // A 3D transform is three passes of batched 1D transforms along x, y and z over X[q][z][y][x].
 // A block stages a tile of lines in shared memory (consecutive lines for the x pass; for the y
 // and z passes a tile of consecutive x, so every global access is a contiguous run), transforms it
-// there and writes it back in place: radix-2 decimation in time for power-of-two lengths, a direct
-// DFT otherwise.  On GB300 the FP64 transform is bound by the FP64 pipe, not by HBM.
+// there and writes it back in place: radix-2 decimation in time for power-of-two lengths, a
+// mixed-radix Stockham transform (radices 4, 2, 3, 5, other primes directly) otherwise.  On GB300 the FP64 transform is bound by the FP64 pipe, not by HBM.
 #include <map>
 #include <vector>
 
@@ -54,6 +54,7 @@ constexpr int kGfThreads = red::kThreads;
 constexpr int kGfBlocks = 1216;
 constexpr int kFftThreads = 256;
 constexpr int kFftMaxTile = 4096;  // complex doubles staged per block (64 KB)
+constexpr size_t kFftMaxSmem = 227 * 1024;  // shared memory a block may opt into
 
 inline unsigned blocks_for(long long n, int threads, int cap) {
   long long b = (n + threads - 1) / threads;
@@ -458,7 +459,7 @@ __global__ void __launch_bounds__(kFftThreads) fft_pow2_kernel(C* X, int logn, l
   }
 }
 
-// Element (line l, k) of a batch of 1D transforms of length n, stride st (direct DFT path):
+// Element (line l, k) of a batch of 1D transforms of length n, stride st (mixed-radix path):
 //   st == 1 : l*n + k
 //   st  > 1 : o*st*n + i + k*st  with l = (o, i), i in [0, st)
 __device__ __forceinline__ long long fft_addr(long long tile, int t, int k, int n, long long st, int tile_lines) {
@@ -469,33 +470,149 @@ __device__ __forceinline__ long long fft_addr(long long tile, int t, int k, int 
   return o * st * n + i + (long long)k * st;
 }
 
-// Direct DFT for lengths that are not powers of two; tw holds exp(-2 pi i k / n), k < n.
+// The radices of a mixed-radix transform of length n = radix[0] * radix[1] * ...: fours first, then
+// two, three, five, then the remaining prime factors (each done as a direct DFT of its length).
+struct FftPlan {
+  int nstages;
+  int radix[24];
+};
+
 template <typename C>
-__global__ void __launch_bounds__(kFftThreads) dft_kernel(C* X, int n, long long st, int tile_lines,
-                                                          const C* __restrict__ tw, int inverse) {
+__device__ __forceinline__ C cmul_c(const C& a, const C& w) {
+  return cmk(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+}
+// -i z (forward) or +i z (inverse) as sgn * (z.y, -z.x) with sgn = +1 / -1
+template <typename C, typename R>
+__device__ __forceinline__ C rot_i(const C& z, R sgn) {
+  return cmk(sgn * z.y, -sgn * z.x);
+}
+
+// Mixed-radix Stockham transform (self-sorting, no bit reversal) of a tile of lines of length n in
+// shared memory, ping-ponging between two buffers; one stage per radix R of the plan.  Stage with
+// Ns = product of the earlier radices, butterfly j < n/R of a line:
+//   v_r = in[j + r n/R] * w^(r (j mod Ns) n/(Ns R)),  r < R            (w = exp(-+2 pi i / n))
+//   out[(j / Ns) Ns R + (j mod Ns) + q Ns] = sum_r v_r exp(-+2 pi i r q / R),  q < R
+// (the Stockham formulation of, e.g., Govindaraju et al., SC 2008), with hand-written butterflies
+// for R = 2, 3, 4, 5 and the direct sum for other primes.  tw[k] = exp(-2 pi i k / n), k < n.
+template <typename C>
+__global__ void __launch_bounds__(kFftThreads) fft_mixed_kernel(C* X, int n, long long st, int tile_lines,
+                                                                const C* __restrict__ tw,
+                                                                const __grid_constant__ FftPlan plan, int inverse) {
+  using R = decltype(C::x);
   extern __shared__ __align__(16) unsigned char fft_smem[];
-  C* sm = reinterpret_cast<C*>(fft_smem);
+  C* a = reinterpret_cast<C*>(fft_smem);
+  C* b = a + tile_lines * n;
   const long long tile = blockIdx.x;
   const int total = tile_lines * n;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     const int t = st == 1 ? idx / n : idx % tile_lines;
     const int k = st == 1 ? idx - t * n : idx / tile_lines;
-    sm[t * n + k] = X[fft_addr(tile, t, k, n, st, tile_lines)];
+    a[t * n + k] = X[fft_addr(tile, t, k, n, st, tile_lines)];
   }
   __syncthreads();
+  const R sgn = inverse ? R(-1) : R(1);  // the sign of -i in the butterflies
+  int Ns = 1;
+  for (int s = 0; s < plan.nstages; s++) {
+    const int rad = plan.radix[s];
+    const int nb = n / rad;
+    const int tstep = n / (Ns * rad);
+    for (int idx = threadIdx.x; idx < tile_lines * nb; idx += blockDim.x) {
+      const int t = idx / nb, j = idx - t * nb;
+      const int jm = j % Ns;
+      const C* src = a + t * n + j;
+      C* dst = b + t * n + (j - jm) * rad + jm;
+      auto twd = [&](int r) {  // w^(r jm tstep), conjugated for the inverse
+        C w = tw[(int)(((long long)r * jm * tstep) % n)];
+        if (inverse) w.y = -w.y;
+        return w;
+      };
+      if (rad == 2) {
+        const C v0 = src[0], v1 = cmul_c(src[nb], twd(1));
+        dst[0] = cmk(v0.x + v1.x, v0.y + v1.y);
+        dst[Ns] = cmk(v0.x - v1.x, v0.y - v1.y);
+      } else if (rad == 4) {
+        const C v0 = src[0], v1 = cmul_c(src[nb], twd(1)), v2 = cmul_c(src[2 * nb], twd(2)),
+                v3 = cmul_c(src[3 * nb], twd(3));
+        const C s02 = cmk(v0.x + v2.x, v0.y + v2.y), d02 = cmk(v0.x - v2.x, v0.y - v2.y);
+        const C s13 = cmk(v1.x + v3.x, v1.y + v3.y), d13 = rot_i(cmk(v1.x - v3.x, v1.y - v3.y), sgn);
+        dst[0] = cmk(s02.x + s13.x, s02.y + s13.y);
+        dst[Ns] = cmk(d02.x + d13.x, d02.y + d13.y);
+        dst[2 * Ns] = cmk(s02.x - s13.x, s02.y - s13.y);
+        dst[3 * Ns] = cmk(d02.x - d13.x, d02.y - d13.y);
+      } else if (rad == 3) {
+        const R h = R(0.86602540378443864676);  // sin(2 pi / 3)
+        const C v0 = src[0], v1 = cmul_c(src[nb], twd(1)), v2 = cmul_c(src[2 * nb], twd(2));
+        const C s = cmk(v1.x + v2.x, v1.y + v2.y);
+        const C m = cmk(v0.x - R(0.5) * s.x, v0.y - R(0.5) * s.y);
+        const C d = rot_i(cmk(h * (v1.x - v2.x), h * (v1.y - v2.y)), sgn);
+        dst[0] = cmk(v0.x + s.x, v0.y + s.y);
+        dst[Ns] = cmk(m.x + d.x, m.y + d.y);
+        dst[2 * Ns] = cmk(m.x - d.x, m.y - d.y);
+      } else if (rad == 5) {
+        const R c1 = R(0.30901699437494742410), c2 = R(-0.80901699437494742410);  // cos(2 pi/5), cos(4 pi/5)
+        const R s1 = R(0.95105651629515357212), s2 = R(0.58778525229247312917);   // sin(2 pi/5), sin(4 pi/5)
+        const C v0 = src[0], v1 = cmul_c(src[nb], twd(1)), v2 = cmul_c(src[2 * nb], twd(2)),
+                v3 = cmul_c(src[3 * nb], twd(3)), v4 = cmul_c(src[4 * nb], twd(4));
+        const C p1 = cmk(v1.x + v4.x, v1.y + v4.y), m1 = cmk(v1.x - v4.x, v1.y - v4.y);
+        const C p2 = cmk(v2.x + v3.x, v2.y + v3.y), m2 = cmk(v2.x - v3.x, v2.y - v3.y);
+        const C a1 = cmk(v0.x + c1 * p1.x + c2 * p2.x, v0.y + c1 * p1.y + c2 * p2.y);
+        const C a2 = cmk(v0.x + c2 * p1.x + c1 * p2.x, v0.y + c2 * p1.y + c1 * p2.y);
+        const C b1 = rot_i(cmk(s1 * m1.x + s2 * m2.x, s1 * m1.y + s2 * m2.y), sgn);
+        const C b2 = rot_i(cmk(s2 * m1.x - s1 * m2.x, s2 * m1.y - s1 * m2.y), sgn);
+        dst[0] = cmk(v0.x + p1.x + p2.x, v0.y + p1.y + p2.y);
+        dst[Ns] = cmk(a1.x + b1.x, a1.y + b1.y);
+        dst[4 * Ns] = cmk(a1.x - b1.x, a1.y - b1.y);
+        dst[2 * Ns] = cmk(a2.x + b2.x, a2.y + b2.y);
+        dst[3 * Ns] = cmk(a2.x - b2.x, a2.y - b2.y);
+      } else {
+        // any other prime: the direct sum, with the stage twiddle folded into the DFT's:
+        // out_q = sum_r in_r w^(r (jm + q Ns) tstep)
+        for (int q = 0; q < rad; q++) {
+          R re = 0, im = 0;
+          const long long e = (long long)(jm + q * Ns) * tstep;
+          for (int r = 0; r < rad; r++) {
+            C w = tw[(int)((r * e) % n)];
+            if (inverse) w.y = -w.y;
+            const C v = src[r * nb];
+            re += v.x * w.x - v.y * w.y;
+            im += v.x * w.y + v.y * w.x;
+          }
+          dst[q * Ns] = cmk(re, im);
+        }
+      }
+    }
+    __syncthreads();
+    C* tmp = a;
+    a = b;
+    b = tmp;
+    Ns *= rad;
+  }
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     const int t = st == 1 ? idx / n : idx % tile_lines;
     const int k = st == 1 ? idx - t * n : idx / tile_lines;
-    decltype(C::x) re = 0, im = 0;
-    for (int j = 0; j < n; j++) {
-      C w = tw[(int)(((long long)j * k) % n)];
-      if (inverse) w.y = -w.y;
-      const C a = sm[t * n + j];
-      re += a.x * w.x - a.y * w.y;
-      im += a.x * w.y + a.y * w.x;
-    }
-    X[fft_addr(tile, t, k, n, st, tile_lines)] = cmk(re, im);
+    X[fft_addr(tile, t, k, n, st, tile_lines)] = a[t * n + k];
   }
+}
+
+FftPlan make_plan(int n) {
+  FftPlan p{};
+  int m = n;
+  auto push = [&](int r) { p.radix[p.nstages++] = r; m /= r; };
+  while (m % 4 == 0) push(4);
+  while (m % 2 == 0) push(2);
+  while (m % 3 == 0) push(3);
+  while (m % 5 == 0) push(5);
+  for (int f = 7; m > 1;) {
+    if ((long long)f * f > m) {
+      push(m);
+      break;
+    }
+    if (m % f == 0)
+      push(f);
+    else
+      f += 2;
+  }
+  return p;
 }
 
 bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
@@ -532,10 +649,11 @@ cudaError_t fft_lines_t(C* X, int n, long long st, long long total, int inverse,
     fft_pow2_kernel<C><<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, ilog2(n), st, ilog2(tl), st > 1 ? st / tl : 0,
                                                                        tw, inverse);
   } else {
-    const size_t smem = (size_t)tl * n * sizeof(C);
-    cudaFuncSetAttribute(dft_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t smem = 2 * (size_t)tl * n * sizeof(C);
+    if (smem > kFftMaxSmem) return cudaErrorInvalidValue;  // lines longer than the shared-memory tile
+    cudaFuncSetAttribute(fft_mixed_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(smem > 48 * 1024 ? smem : 48 * 1024));
-    dft_kernel<C><<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, n, st, tl, tw, inverse);
+    fft_mixed_kernel<C><<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, n, st, tl, tw, make_plan(n), inverse);
   }
   return cudaGetLastError();
 }

@@ -23,7 +23,11 @@ def mild_config(N, seed, eps=0.02, om=0.2):
     return mild_gauge_config(N, seed, eps, om)
 
 
-@pytest.mark.parametrize("N", [(8, 8, 16), (4, 16, 32), (6, 5, 7), (2, 3, 12)])
+# power-of-two lengths (radix-2 kernel) and mixed radix (Stockham: radices 4, 2, 3, 5, other primes by
+# their direct DFT): the lengths of the batched events' lattices (48, 96, 160, 250), primes 7 and 97,
+# and composites with repeated larger primes (49, 121)
+@pytest.mark.parametrize("N", [(8, 8, 16), (4, 16, 32), (6, 5, 7), (2, 3, 12), (48, 96, 160), (250, 3, 97),
+                               (49, 121, 10), (160, 48, 250)])
 def test_fft3d_matches_numpy(N):
     rng = np.random.default_rng(sum(N))
     X = rng.standard_normal((8, N[2], N[1], N[0])) + 1j * rng.standard_normal((8, N[2], N[1], N[0]))
@@ -36,7 +40,7 @@ def test_fft3d_matches_numpy(N):
     assert np.max(np.abs(B - refb)) / np.max(np.abs(refb)) < 1e-14
 
 
-@pytest.mark.parametrize("N", [(8, 8, 16), (16, 4, 32), (6, 5, 7)])
+@pytest.mark.parametrize("N", [(8, 8, 16), (16, 4, 32), (6, 5, 7), (48, 96, 160), (250, 3, 97)])
 def test_fft3d_f32_matches_numpy(N):
     """The FP32 transform (the gauge fixer's GLASMA_GF_FFT_FP32 path): FP32 rounding, ~1e-7 log2(V)."""
     rng = np.random.default_rng(sum(N) + 1)
