@@ -991,7 +991,7 @@ def run_adjoint(args):
         adj_s = time.perf_counter() - t0
         restore(f0)
         _, grads = lat.adjoint(dt, steps, z0, z1, Lattice.PL_OVER_PT, checkpoint_every=every)
-        checks = []
+        checks, dirs = [], []
         eps = 1e-6
         for k in range(args.fd_dirs):
             drng = np.random.default_rng(3000 + k)
@@ -1008,6 +1008,32 @@ def run_adjoint(args):
             fd = (objective_after(fp) - objective_after(fm)) / (2 * eps)
             ad = sum(float(np.sum(grads[name][1:-1] * d[name][1:-1])) for name in names)
             checks.append({"fd": fd, "adjoint": ad, "rel_diff": abs(fd - ad) / max(abs(fd), 1e-300)})
+            dirs.append(d)
+        # eps sweep along the direction with the largest difference: the central difference's truncation
+        # error falls as eps^2 and its rounding error grows as ~1e-16 |L| / eps, so where the difference
+        # to the adjoint is FD noise it changes with eps, and the fourth-order difference removes the
+        # truncation part
+        sweep = None
+        if checks:
+            k = max(range(len(checks)), key=lambda i: checks[i]["rel_diff"])
+            d = dirs[k]
+
+            def shifted(h):
+                fs = dict(f0)
+                for name in names:
+                    fs[name] = f0[name] + h * d[name]
+                return objective_after(fs)
+
+            rows = []
+            for e in (1e-4, 1e-5, 1e-6, 1e-7):
+                fpe, fme = shifted(e), shifted(-e)
+                c2 = (fpe - fme) / (2 * e)
+                row = {"eps": e, "fd": c2, "rel_diff": abs(c2 - checks[k]["adjoint"]) / abs(checks[k]["adjoint"])}
+                if e >= 1e-5:
+                    c4 = (8 * (fpe - fme) - (shifted(2 * e) - shifted(-2 * e))) / (12 * e)
+                    row.update({"fd4": c4, "rel_diff4": abs(c4 - checks[k]["adjoint"]) / abs(checks[k]["adjoint"])})
+                rows.append(row)
+            sweep = {"direction": k, "adjoint": checks[k]["adjoint"], "rows": rows}
     # ---- the same adjoint on an FP32 lattice (FP32 end to end), against the FP64 gradient
     with Lattice(N, precision="fp32", stream=stream) as l32:
         l32.upload_fields(f0)
@@ -1055,6 +1081,7 @@ def run_adjoint(args):
         "objective_forward": L_fwd,
         "fd_checks": checks,
         "fd_eps": eps,
+        "fd_eps_sweep": sweep,
         "fp32": fp32,
     }
     print(json.dumps(line), flush=True)
