@@ -412,8 +412,16 @@ inline void LoadConfiguration(const std::string& Ufname, const std::string& Efna
 // S/GAUGETRANSFORMATION/CoulombGaugeFixing.cpp:6-96.  The reference compiles one of its three updates,
 // chosen by a #define in CoulombGaugeFixing.cpp:4; here the same macro names, defined before this header
 // is included, choose it (GAUGE_FIXING_ALGORITHM_LOS_ALAMOS, GAUGE_FIXING_ALGORITHM_JACOBI), and the
-// Fourier-accelerated update is the default, as in the reference.
+// Fourier-accelerated update is the default, as in the reference.  Defining GAUGE_FIXING_OPEN_Z as well
+// selects the open-z functional for the Fourier update (GLASMA_GF_OPEN_Z: the top slice's z link into
+// the ghost slice left out of the deviation), with which the iteration converges on open-z lattices
+// where the reference's leaves SU(3); Flags can also be set at run time.
 namespace CoulombGaugeFixing {
+#if defined(GAUGE_FIXING_OPEN_Z)
+inline unsigned Flags = GLASMA_GF_OPEN_Z;
+#else
+inline unsigned Flags = 0;  // glasma_coulomb_fix flags for the Fourier update
+#endif
 inline glasma_dropin::DOUBLE GlobalMaxDeviation = 0.0, GlobalAvgDeviation = 0.0, GlobalMaxStepSize = 0.0,
                              GlobalAvgStepSize = 0.0, GlobalMinGaugeFunctional = 0.0, GlobalSumGaugeFunctional = 0.0;
 namespace FourierAccelerationAlgorithm {
@@ -443,8 +451,8 @@ inline void SetCoulombGauge(const std::string& fname, int TotalSteps) {
   const double param = FourierAccelerationAlgorithm::alphaStepSize;
 #endif
   glasma_dropin::check(glasma_coulomb_fix_algorithm(glasma_dropin::handle(), algorithm, param,
-                                                    LosAlamosAlgorithm::DrawSeed, TotalSteps, 1e-15, 0, log.data(),
-                                                    &n));
+                                                    LosAlamosAlgorithm::DrawSeed, TotalSteps, 1e-15,
+                                                    algorithm == GLASMA_GF_FOURIER ? Flags : 0u, log.data(), &n));
   if (n > 0) {
     const double* last = log.data() + (size_t)(n - 1) * 7;
     GlobalMaxDeviation = last[1];
