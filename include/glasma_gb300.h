@@ -139,13 +139,21 @@ int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags);
  * GLASMA_STEP_PLAQUETTE: the electric force summed plaquette by plaquette (each site's three
  * plaquettes and six adjoint rotations instead of twelve staples; the same terms regrouped, equal to
  * the other methods up to rounding), two kernels per step, 48 reals per site more memory (falls back
- * to two-pass for a call when that cannot be allocated).
+ * to two-pass for a call when that cannot be allocated).  GLASMA_STEP_MARCH: the plaquette method in
+ * one kernel per step, each block marching along z through a tile of (x, y) sites (the rotated force
+ * terms handed over in shared memory and registers instead of HBM); bit-identical to
+ * GLASMA_STEP_PLAQUETTE, with the one-pass method's second buffer set (falls back to two-pass for a
+ * call when that cannot be allocated).
  * glasma_get_step_method reports the method the last glasma_step call used. */
 #define GLASMA_STEP_ONE_PASS 0
 #define GLASMA_STEP_TWO_PASS 1
 #define GLASMA_STEP_PLAQUETTE 2
+#define GLASMA_STEP_MARCH 3
 int glasma_set_step_method(glasma_lattice* h, int method);
 int glasma_get_step_method(glasma_lattice* h, int* method);
+/* z slices each block of GLASMA_STEP_MARCH walks (0, the default: chosen from the lattice so that the
+ * blocks fill the GPU); a tuning knob, the fields do not depend on it.  No reference counterpart. */
+int glasma_set_march_chunk(glasma_lattice* h, int slices);
 
 /* Link storage of the leapfrog step (FP32 handles): 18 reals per link (default) or 12, rows 0 and 1
  * of each link, with row 2 formed in registers as the unitary complement conj(row0 x row1).  With 12

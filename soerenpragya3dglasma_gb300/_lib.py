@@ -52,6 +52,7 @@ SIGNATURES = [
     ("glasma_step_profiled", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_uint, _D]),
     ("glasma_set_step_method", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_get_step_method", ctypes.c_int, [_H, _I]),
+    ("glasma_set_march_chunk", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_set_link_storage", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_set_fp64_arithmetic", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_get_fp64_arithmetic", ctypes.c_int, [_H, _I]),

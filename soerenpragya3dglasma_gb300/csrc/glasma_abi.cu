@@ -280,6 +280,27 @@ int step_impl(glasma_lattice* h, double dt, int nsteps, unsigned flags, cudaEven
     }
     return complete_links<T>(h);
   }
+  if (h->step_method == GLASMA_STEP_MARCH && ensure_alt(h)) {
+    h->last_method = GLASMA_STEP_MARCH;
+    for (int n = 0; n < nsteps; n++) {
+      if (ev) cudaEventRecord(ev[3 * n], h->stream);
+      const bool save = (flags & GLASMA_STEP_SAVE_UOLD) && (n == nsteps - 1);
+      e = glasma::launch_march_step<T>(h->g, ptrs<T>(h), alt_ptrs<T>(h), dt, save, h->march_lz, h->stream,
+                                       h->link_rows);
+      if (e != cudaSuccess) return cuda_fail(e, "march step");
+      if (ev) {
+        cudaEventRecord(ev[3 * n + 1], h->stream);
+        cudaEventRecord(ev[3 * n + 2], h->stream);
+      }
+      swap_buffers(h);
+      h->steps_done++;
+      if (h->reunit_every > 0 && h->steps_done % h->reunit_every == 0) {
+        e = glasma::launch_reunitarize<T>(h->g, static_cast<cx<T>*>(h->f[GLASMA_FIELD_U]), h->stream, h->link_rows);
+        if (e != cudaSuccess) return cuda_fail(e, "reunitarize");
+      }
+    }
+    return complete_links<T>(h);
+  }
   if (h->step_method == GLASMA_STEP_PLAQUETTE && ensure_contrib(h)) {
     h->last_method = GLASMA_STEP_PLAQUETTE;
     for (int n = 0; n < nsteps; n++) {
@@ -366,6 +387,7 @@ int glasma_create(int nx, int ny, int nz, double ax, double ay, double az, int p
   // the plaquette method: ~25 % fewer matrix products in the force (FP64 step 75.5 -> 68.2 ms on GB300
   // at 128x128x512); falls back to two-pass when its buffer cannot be allocated
   h->step_method = GLASMA_STEP_PLAQUETTE;
+  h->march_lz = 0;
   h->link_rows = 3;
   h->fp64_arith = GLASMA_FP64_NATIVE;
   h->last_method = GLASMA_STEP_TWO_PASS;
@@ -582,10 +604,11 @@ int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags) {
 
 int glasma_set_step_method(glasma_lattice* h, int method) {
   GLASMA_CHECK_HANDLE(h);
-  if (method != GLASMA_STEP_ONE_PASS && method != GLASMA_STEP_TWO_PASS && method != GLASMA_STEP_PLAQUETTE)
+  if (method != GLASMA_STEP_ONE_PASS && method != GLASMA_STEP_TWO_PASS && method != GLASMA_STEP_PLAQUETTE &&
+      method != GLASMA_STEP_MARCH)
     return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown step method");
   h->step_method = method;
-  if (method != GLASMA_STEP_ONE_PASS) {  // give the second buffer set back
+  if (method != GLASMA_STEP_ONE_PASS && method != GLASMA_STEP_MARCH) {  // give the second buffer set back
     GLASMA_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
     for (int f : kSwapFields) {
       if (h->alt[f]) cudaFree(h->alt[f]);
@@ -597,6 +620,13 @@ int glasma_set_step_method(glasma_lattice* h, int method) {
     cudaFree(h->contrib);
     h->contrib = nullptr;
   }
+  return GLASMA_OK;
+}
+
+int glasma_set_march_chunk(glasma_lattice* h, int slices) {
+  GLASMA_CHECK_HANDLE(h);
+  if (slices < 0) return fail(GLASMA_ERR_INVALID_ARGUMENT, "slices < 0");
+  h->march_lz = slices;
   return GLASMA_OK;
 }
 

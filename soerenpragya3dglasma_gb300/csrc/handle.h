@@ -24,7 +24,8 @@ struct glasma_lattice {
   glasma::GaugeFixState* gf;
   int tile_x;         // K1 tile width along x (autotuned)
   void* alt[10];      // second buffer set of the one-pass step (U, JP, JM, JPSTAT, JMSTAT; lazily)
-  int step_method;    // GLASMA_STEP_ONE_PASS / GLASMA_STEP_TWO_PASS
+  int step_method;    // GLASMA_STEP_ONE_PASS / _TWO_PASS / _PLAQUETTE / _MARCH
+  int march_lz;       // z slices per block of the marching step (0: chosen from the lattice)
   int last_method;    // method the last glasma_step used
   int link_rows;      // rows of each link the step kernels read and write: 3, or 2 (12-real links, FP32)
   void* contrib;      // plaquette method: 6 x 8 weighted force contributions per site (lazily)

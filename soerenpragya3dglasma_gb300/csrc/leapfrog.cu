@@ -18,6 +18,7 @@
 // ReTr(i t^a W^dagger) = -ReTr(i t^a W).  Ghost slices are written by the threads that own
 // slice 0 and slice Nz-1, which is the reference's SynchronizeGhostCells after each sub-step.
 #include "leapfrog_sites.cuh"
+#include "march.cuh"
 
 namespace glasma {
 
@@ -289,6 +290,49 @@ cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> o
 }
 
 template <typename T, int R>
+void launch_march_rows(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, const MarchParams<T>& mp, unsigned grid,
+                       cudaStream_t stream) {
+  if (use_32bit_index(g))
+    march_step_kernel<T, int, R><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
+  else
+    march_step_kernel<T, long long, R><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
+}
+
+// Slices per block of the z-marching step: enough (tile, chunk) blocks to fill every SM several times
+// over, and chunks long enough that the warm-up slice below each chunk stays a small share.
+int march_chunk(const Geometry& g, long long tiles) {
+  const long long want = 152LL * 8;  // blocks
+  long long chunks = (want + tiles - 1) / tiles;
+  if (chunks > g.nz) chunks = g.nz;
+  if (chunks < 1) chunks = 1;
+  int lz = (int)((g.nz + chunks - 1) / chunks);
+  const int min_lz = g.nz < 8 ? g.nz : 8;
+  return lz < min_lz ? min_lz : lz;
+}
+
+template <typename T>
+cudaError_t launch_march_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, double dt, bool save_uold, int lz,
+                              cudaStream_t stream, int link_rows) {
+  MarchParams<T> mp;
+  mp.pe = make_eparams<T>(g, dt, 1, 1, 0);
+  mp.pl = make_lparams<T>(g, dt, save_uold, true, true);
+  mp.ntx = (g.nx + kMarchTX - 1) / kMarchTX;
+  mp.nty = (g.ny + kMarchTY - 1) / kMarchTY;
+  const long long tiles = (long long)mp.ntx * mp.nty;
+  mp.lz = lz > 0 ? (lz < g.nz ? lz : g.nz) : march_chunk(g, tiles);
+  const long long chunks = (g.nz + mp.lz - 1) / mp.lz;
+  const unsigned grid = (unsigned)(tiles * chunks);
+  if constexpr (sizeof(T) == 4) {
+    if (two_row<T>(link_rows)) {
+      launch_march_rows<T, 2>(g, in, out, mp, grid, stream);
+      return cudaGetLastError();
+    }
+  }
+  launch_march_rows<T, 3>(g, in, out, mp, grid, stream);
+  return cudaGetLastError();
+}
+
+template <typename T, int R>
 void launch_links_rows(const Geometry& g, FieldPtrs<T> f, const LParams<T>& p, cudaStream_t stream) {
   if (use_32bit_index(g))
     links_j_kernel<T, int, R><<<grid_for(g.vol, kThreads), kThreads, 0, stream>>>(g, f, p);
@@ -405,6 +449,8 @@ cudaError_t launch_copy_links(const Geometry& g, const cx<T>* src, cx<T>* dst, c
   template cudaError_t launch_j_only<T>(const Geometry&, FieldPtrs<T>, double, cudaStream_t);                  \
   template cudaError_t launch_reunitarize<T>(const Geometry&, cx<T>*, cudaStream_t, int);                      \
   template cudaError_t launch_complete_links<T>(const Geometry&, cx<T>*, cudaStream_t);                        \
+  template cudaError_t launch_march_step<T>(const Geometry&, FieldPtrs<T>, FieldPtrs<T>, double, bool, int,      \
+                                            cudaStream_t, int);                                                 \
   template cudaError_t launch_plaquette_step<T>(const Geometry&, FieldPtrs<T>, T*, double, bool, cudaStream_t,  \
                                                 cudaEvent_t, int, bool);                                        \
   template cudaError_t launch_copy_links<T>(const Geometry&, const cx<T>*, cx<T>*, cudaStream_t);              \

@@ -222,14 +222,19 @@ class Lattice:
     def step(self, dt, nsteps=1, save_uold=True):
         check(self.lib.glasma_step(self.h, float(dt), int(nsteps), _lib.STEP_SAVE_UOLD if save_uold else 0))
 
-    STEP_METHODS = {"one_pass": 0, "two_pass": 1, "plaquette": 2}
+    STEP_METHODS = {"one_pass": 0, "two_pass": 1, "plaquette": 2, "march": 3}
 
     def set_step_method(self, method):
         """"plaquette" (default: the electric force summed plaquette by plaquette, two kernels and a
         contribution buffer), "two_pass" (two kernels per step, in place, staple form) or "one_pass"
-        (one kernel per step over two buffer sets; bit-identical to two_pass).  The plaquette method
-        equals the other two up to rounding."""
+        (one kernel per step over two buffer sets; bit-identical to two_pass) or "march" (the plaquette
+        method in one kernel per step, blocks marching along z; bit-identical to plaquette).  The
+        plaquette methods equal the staple ones up to rounding."""
         check(self.lib.glasma_set_step_method(self.h, self.STEP_METHODS[method]))
+
+    def set_march_chunk(self, slices):
+        """z slices per block of the marching step (0: chosen from the lattice)."""
+        check(self.lib.glasma_set_march_chunk(self.h, int(slices)))
 
     @property
     def last_step_method(self):
