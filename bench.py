@@ -45,6 +45,7 @@ KERNEL_BYTES = {
     "links_j": {"fp64": 192 + 2 * 432 + 128 + 2 * 128, "fp32": 96 + 2 * 216 + 64 + 2 * 64,
                 "fp32_l12": 96 + 2 * 144 + 64 + 2 * 64},
     "fused_step": {"fp64": 1760, "fp32": 880, "fp32_l12": 736},  # one pass: every per-site array read and written once
+    "march_step": {"fp64": 1760, "fp32": 880, "fp32_l12": 736},  # the marching plaquette step, likewise
     # plaquette method: the same compulsory state traffic as K1 / K2 (the 48 contribution reals per site
     # the force kernel hands to the link kernel are an intermediate of this method, not algorithmic
     # bytes; ncu's DRAM traffic shows what they cost)
@@ -344,7 +345,9 @@ def run_ours(args):
     def make_lattice(precision, link_reals=18):
         lat = Lattice(N, A_WORK, precision=precision, reunitarize_every=16 if precision == "fp32" else 0,
                       stream=stream)
-        lat.set_step_method(args.step_method)
+        lat.set_step_method(args.step_method if precision == "fp64" else (args.fp32_step_method or args.step_method))
+        if args.march_chunk:
+            lat.set_march_chunk(args.march_chunk)
         lat.link_reals = link_reals
         if precision == "fp64":
             lat.fp64_arithmetic = args.fp64_arith
@@ -424,6 +427,8 @@ def run_ours(args):
         ms = max_over_ranks(e0.elapsed_time(e1)) / nsteps
         if lat.last_step_method == "one_pass":
             kern = {"fused_step": kms[0] / nsteps}
+        elif lat.last_step_method == "march":
+            kern = {"march_step": kms[0] / nsteps}
         elif lat.last_step_method == "plaquette":
             kern = {"plaquette_forces": kms[0] / nsteps, "links_gather": kms[1] / nsteps}
         else:
@@ -667,8 +672,9 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         # per step: the one-pass kernel (or K1 + K2); per step() call: one ghost-slice sync
-        "gpu_launches": (1 if "fused_step" in (k_ms or {}) else 2) * args.steps + 1,
+        "gpu_launches": (1 if ("fused_step" in (k_ms or {}) or "march_step" in (k_ms or {})) else 2) * args.steps + 1,
         "step_method": args.step_method,
+        "fp32_step_method": args.fp32_step_method or args.step_method,
         "fp64_arithmetic": args.fp64_arith,
         "tiles": tiles,
     }
@@ -1098,7 +1104,10 @@ def main():
                     help="CPU legs: the reference's own compiled code where it was built (auto), or the oracle port")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-gauge", action="store_true", help="skip the gauge-fixing / FFT leg")
-    ap.add_argument("--step-method", default="plaquette", choices=["one_pass", "two_pass", "plaquette"])
+    ap.add_argument("--step-method", default="plaquette", choices=["one_pass", "two_pass", "plaquette", "march"])
+    ap.add_argument("--fp32-step-method", default=None, choices=["one_pass", "two_pass", "plaquette", "march"],
+                    help="step method of the FP32 legs (default: --step-method)")
+    ap.add_argument("--march-chunk", type=int, default=0, help="z slices per block of the marching step")
     ap.add_argument("--fp64-arith", default="native", choices=["native", "double_float"],
                     help="arithmetic of the FP64 plaquette force kernel")
     ap.add_argument("--gauge-evolve", type=int, default=40, help="leapfrog steps of the MV state before gauge fixing")

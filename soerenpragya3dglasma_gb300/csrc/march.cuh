@@ -90,6 +90,24 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     march_step_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> in,
                       const __grid_constant__ FieldPtrs<T> out, const __grid_constant__ MarchParams<T> mp) {
   __shared__ T csm[4 * 8 * kMarchThreads];
+  // FP32: the z-terms carried to the next slice wait in shared memory (each thread its own entries,
+  // two buffers by slice parity) instead of 16 registers; FP64 keeps them in registers
+  constexpr bool kZsm = sizeof(T) == 4;
+  __shared__ T zsm[kZsm ? 2 * 16 * kMarchThreads : 1];
+  auto zput = [&](int z, const Alg<T>& v0, const Alg<T>& v1) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      zsm[((z & 1) * 16 + a) * kMarchThreads + threadIdx.x] = v0.a[a];
+      zsm[((z & 1) * 16 + 8 + a) * kMarchThreads + threadIdx.x] = v1.a[a];
+    }
+  };
+  auto zget = [&](int z, Alg<T>& v0, Alg<T>& v1) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      v0.a[a] = zsm[((z & 1) * 16 + a) * kMarchThreads + threadIdx.x];
+      v1.a[a] = zsm[((z & 1) * 16 + 8 + a) * kMarchThreads + threadIdx.x];
+    }
+  };
   const I S = (I)g.S, plane = (I)g.plane;
   const int tid = threadIdx.x;
   const int lx = tid % kMarchTX, ly = tid / kMarchTX;
@@ -153,6 +171,7 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     inv_adj_mul(u2, al, zc1);
     scale_alg(-w12p, zc1);
     march_jstat(in, S, plane, s + plane, u2, pe.cj, stp, stm);
+    if constexpr (kZsm) zput(zw, zc0, zc1);
   }
 
 #pragma unroll 1
@@ -224,6 +243,9 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
         scale_alg(w12q, o);
         march_put(csm, kM12p, tid + kMarchTX, o);
       }
+      if constexpr (kZsm) {
+        if (below_top) zput(z, zn0, zn1);
+      }
     }
     // ---- B: the plaquettes owned just outside the tile whose rotated terms reach its first column / row
     if (hrole) {
@@ -271,15 +293,6 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     if (own) {
       const bool lo = (z == 0), hi = (z == g.nz - 1);
       const I sg = lo ? s - plane : (hi ? s + plane : (I)-1);
-      Alg<T> sp1, sm1;  // static currents of t+dt one slice up (its ghost copy at the top slice)
-      if (hi) {
-        sp1 = stp;
-        sm1 = stm;
-      } else {
-        Mat<T> uz;
-        load_link_r<R>(in.U, S, 2, s, uz);
-        march_jstat(in, S, plane, s + plane, uz, pe.cj, sp1, sm1);
-      }
       store_alg(out.JpStat, S, 0, s, stp);
       store_alg(out.JmStat, S, 0, s, stm);
       if (sg >= 0) {
@@ -294,12 +307,22 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
 #pragma unroll
           for (int k = 0; k < 8; k++) e.a[k] += F0.a[k];
           march_get(csm, kM01q, tid, a1);
-          a2 = zc0;
+          if constexpr (kZsm) {
+            Alg<T> unused;
+            zget(z - 1, a2, unused);
+          } else {
+            a2 = zc0;
+          }
         } else if (mu == 1) {
 #pragma unroll
           for (int k = 0; k < 8; k++) e.a[k] += F1.a[k];
           march_get(csm, kM01p, tid, a1);
-          a2 = zc1;
+          if constexpr (kZsm) {
+            Alg<T> unused;
+            zget(z - 1, unused, a2);
+          } else {
+            a2 = zc1;
+          }
         } else {
           Alg<T> jp, jm;
           load_alg(in.Jp, S, 0, s, jp);
@@ -315,6 +338,49 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
         if (sg >= 0) store_alg(in.E, S, mu * 8, sg, e);
         Mat<T> X, u, uh;
         load_link_r<R>(in.U, S, mu, s, u);
+        if (mu == 2) {
+          // static currents of t+dt one slice up, from U_z(z) of t (its ghost copy at the top slice);
+          // carried to the next slice as its own
+          Alg<T> sp1, sm1;
+          if (hi) {
+            sp1 = stp;
+            sm1 = stm;
+          } else {
+            march_jstat(in, S, plane, s + plane, u, pe.cj, sp1, sm1);
+          }
+          if (pl.do_j) {
+            // UpdateJ needs U_z at t+dt/2 (formed below); keep both static currents until then
+            link_exp(pick3(pl.cU, mu), e, X);
+            link_apply(X, u, uh);
+            if (pl.save_uold) {
+              store_link(in.UOld, S, mu, s, uh);
+              if (sg >= 0) store_link(in.UOld, S, mu, sg, uh);
+            }
+            Alg<T> up, j;
+            adj_mul(uh, sp1, up);
+            load_alg(in.Jp, S, 0, s, j);
+            axpy_diff(j, -pl.cj, up, stp);
+            store_alg(out.Jp, S, 0, s, j);
+            if (sg >= 0) store_alg(out.Jp, S, 0, sg, j);
+            adj_mul(uh, sm1, up);
+            load_alg(in.Jm, S, 0, s, j);
+            axpy_diff(j, pl.cj, up, stm);
+            store_alg(out.Jm, S, 0, s, j);
+            if (sg >= 0) store_alg(out.Jm, S, 0, sg, j);
+            stp = sp1;
+            stm = sm1;
+            if (pl.do_second) {
+              link_apply(X, uh, u);
+            } else {
+              u = uh;
+            }
+            store_link_r<R>(out.U, S, mu, s, u);
+            if (sg >= 0) store_link_r<R>(out.U, S, mu, sg, u);
+            continue;
+          }
+          stp = sp1;
+          stm = sm1;
+        }
         if (pl.do_second && !pl.save_uold && !(mu == 2 && pl.do_j)) {
           link_exp(T(2) * pick3(pl.cU, mu), e, X);
           link_apply(X, u, uh);
@@ -328,19 +394,6 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
           store_link(in.UOld, S, mu, s, uh);
           if (sg >= 0) store_link(in.UOld, S, mu, sg, uh);
         }
-        if (mu == 2 && pl.do_j) {
-          Alg<T> up, j;
-          adj_mul(uh, sp1, up);
-          load_alg(in.Jp, S, 0, s, j);
-          axpy_diff(j, -pl.cj, up, stp);
-          store_alg(out.Jp, S, 0, s, j);
-          if (sg >= 0) store_alg(out.Jp, S, 0, sg, j);
-          adj_mul(uh, sm1, up);
-          load_alg(in.Jm, S, 0, s, j);
-          axpy_diff(j, pl.cj, up, stm);
-          store_alg(out.Jm, S, 0, s, j);
-          if (sg >= 0) store_alg(out.Jm, S, 0, sg, j);
-        }
         if (pl.do_second) {
           link_apply(X, uh, u);
         } else {
@@ -349,11 +402,11 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
         store_link_r<R>(out.U, S, mu, s, u);
         if (sg >= 0) store_link_r<R>(out.U, S, mu, sg, u);
       }
-      stp = sp1;
-      stm = sm1;
     }
-    zc0 = zn0;
-    zc1 = zn1;
+    if constexpr (!kZsm) {
+      zc0 = zn0;
+      zc1 = zn1;
+    }
     __syncthreads();
   }
 }
