@@ -289,13 +289,18 @@ cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> o
   return cudaGetLastError();
 }
 
+#ifndef GLASMA_MARCH_TX
+#define GLASMA_MARCH_TX 32
+#endif
+constexpr int kMarchTileX = GLASMA_MARCH_TX;  // tile of kMarchTileX x (128 / kMarchTileX) sites
+
 template <typename T, int R>
 void launch_march_rows(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, const MarchParams<T>& mp, unsigned grid,
                        cudaStream_t stream) {
   if (use_32bit_index(g))
-    march_step_kernel<T, int, R><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
+    march_step_kernel<T, int, R, kMarchTileX><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
   else
-    march_step_kernel<T, long long, R><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
+    march_step_kernel<T, long long, R, kMarchTileX><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
 }
 
 // Slices per block of the z-marching step: enough (tile, chunk) blocks to fill every SM several times
@@ -316,8 +321,9 @@ cudaError_t launch_march_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> o
   MarchParams<T> mp;
   mp.pe = make_eparams<T>(g, dt, 1, 1, 0);
   mp.pl = make_lparams<T>(g, dt, save_uold, true, true);
-  mp.ntx = (g.nx + kMarchTX - 1) / kMarchTX;
-  mp.nty = (g.ny + kMarchTY - 1) / kMarchTY;
+  constexpr int ty = kMarchThreads / kMarchTileX;
+  mp.ntx = (g.nx + kMarchTileX - 1) / kMarchTileX;
+  mp.nty = (g.ny + ty - 1) / ty;
   const long long tiles = (long long)mp.ntx * mp.nty;
   mp.lz = lz > 0 ? (lz < g.nz ? lz : g.nz) : march_chunk(g, tiles);
   const long long chunks = (g.nz + mp.lz - 1) / mp.lz;

@@ -5,7 +5,7 @@
 // plaquette once, at its owner site y, and hands the two rotated force terms that belong to other
 // links (U_p(y+q), U_q(y+p)) to the link kernel through a contribution buffer in HBM: 48 reals per
 // site written and read back, and E, U and the currents read by both kernels.  Here one block owns a
-// kMarchTX x kMarchTY tile of (x, y) sites and walks a chunk of z slices; per slice
+// TX x (128/TX) tile of (x, y) sites and walks a chunk of z slices; per slice
 //   A  every thread forms the three plaquettes it owns (planes (0,1), (0,2), (1,2)) and their direct
 //      force terms; the rotated terms for its in-tile neighbours x+1 and y+1 go to shared memory, the
 //      two for the links one slice up (U_0(y+z), U_1(y+z)) stay in the thread's registers for the
@@ -29,9 +29,7 @@
 
 namespace glasma {
 
-constexpr int kMarchTX = 32;
-constexpr int kMarchTY = 4;
-constexpr int kMarchThreads = kMarchTX * kMarchTY;
+constexpr int kMarchThreads = 128;  // threads per block: a tile of TX x (128 / TX) sites
 
 #ifndef GLASMA_FP32_MARCH_MIN_BLOCKS
 #define GLASMA_FP32_MARCH_MIN_BLOCKS 3
@@ -85,7 +83,7 @@ __device__ __forceinline__ void march_jstat(const FieldPtrs<T>& in, I S, I plane
   axpy_diff(stm, cj, jc, down);
 }
 
-template <typename T, typename I, int R>
+template <typename T, typename I, int R, int kMarchTX>
 __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     march_step_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> in,
                       const __grid_constant__ FieldPtrs<T> out, const __grid_constant__ MarchParams<T> mp) {
@@ -109,6 +107,9 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     }
   };
   const I S = (I)g.S, plane = (I)g.plane;
+  constexpr int kMarchTY = kMarchThreads / kMarchTX;
+  static_assert(kMarchTY * kMarchTX == kMarchThreads && 2 * (kMarchTX + kMarchTY) <= kMarchThreads,
+                "one halo plaquette per thread: the tile must leave enough threads");
   const int tid = threadIdx.x;
   const int lx = tid % kMarchTX, ly = tid / kMarchTX;
   int b = blockIdx.x;
@@ -126,23 +127,38 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
   const T w01p = pe.gc[0] * pe.cnu[1], w01q = pe.gc[1] * pe.cnu[0];
   const T w02p = pe.gc[0] * pe.cnu[2], w02q = pe.gc[2] * pe.cnu[0];
   const T w12p = pe.gc[1] * pe.cnu[2], w12q = pe.gc[2] * pe.cnu[1];
-  // halo owner of this thread in phase B: threads [0, TY) take the column x0-1 (rows y0+tid), threads
-  // [TY, TY+TX) the row y0-1 (columns x0+tid-TY); hc = the tile site their terms go to
-  int hrole = 0, hx = 0, hy = 0, hc = 0;
-  if (tid < kMarchTY) {
-    if (y0 + tid < g.ny) {
-      hrole = 1;
-      hx = x0 == 0 ? g.nx - 1 : x0 - 1;
-      hy = y0 + tid;
-      hc = tid * kMarchTX;
+  // one halo plaquette of this thread in phase B (the owners just outside the tile: the row y0-1 and
+  // the column x0-1), grouped so that a warp mostly runs one kind:
+  //   [0, TX)            row owner (x0+t, y0-1), plane (0,1) -> link 0 at (x0+t, y0)
+  //   [TX, TX+TY)        column owner (x0-1, y0+t), plane (0,1) -> link 1 at (x0, y0+t)
+  //   [TX+TY, 2TX+TY)    row owner, plane (1,2) -> link 2 at (x0+t, y0)
+  //   [2TX+TY, 2TX+2TY)  column owner, plane (0,2) -> link 2 at (x0, y0+t)
+  int htask = -1, hx = 0, hy = 0, hc = 0;
+  {
+    int t = tid, kind = -1;
+    if (t < kMarchTX) {
+      kind = 0;
+    } else if ((t -= kMarchTX) < kMarchTY) {
+      kind = 1;
+    } else if ((t -= kMarchTY) < kMarchTX) {
+      kind = 2;
+    } else if ((t -= kMarchTX) < kMarchTY) {
+      kind = 3;
     }
-  } else if (tid < kMarchTY + kMarchTX) {
-    const int t = tid - kMarchTY;
-    if (x0 + t < g.nx) {
-      hrole = 2;
-      hx = x0 + t;
-      hy = y0 == 0 ? g.ny - 1 : y0 - 1;
-      hc = t;
+    if (kind == 0 || kind == 2) {
+      if (x0 + t < g.nx) {
+        htask = kind;
+        hx = x0 + t;
+        hy = y0 == 0 ? g.ny - 1 : y0 - 1;
+        hc = t;
+      }
+    } else if (kind == 1 || kind == 3) {
+      if (y0 + t < g.ny) {
+        htask = kind;
+        hx = x0 == 0 ? g.nx - 1 : x0 - 1;
+        hy = y0 + t;
+        hc = t * kMarchTX;
+      }
     }
   }
   const bool put_x = lx + 1 < kMarchTX && x + 1 < g.nx;  // the x-neighbour is a site of this tile
@@ -248,44 +264,44 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
       }
     }
     // ---- B: the plaquettes owned just outside the tile whose rotated terms reach its first column / row
-    if (hrole) {
+    if (htask >= 0) {
       const I hs = (I)site_index(g, hx, hy, z);
       const I hxp = nb<I>(g, hx, hy, z, 1, 0, 0), hyp = nb<I>(g, hx, hy, z, 0, 1, 0), hzp = hs + plane;
       Mat<T> a, bb, cc, d;
       Alg<T> al, o;
-      if (hrole == 1) {  // owner x0-1: plane (0,1) -> link 1 at x0, plane (0,2) -> link 2 at x0
+      if (htask <= 1) {  // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
         load_link_r<R>(in.U, S, 0, hs, a);
         load_link_r<R>(in.U, S, 1, hxp, bb);
         load_link_r<R>(in.U, S, 0, hyp, cc);
         load_link_r<R>(in.U, S, 1, hs, d);
         plaquette_alg(a, bb, cc, d, al);
-        inv_adj_mul(a, al, o);
-        scale_alg(w01q, o);
-        march_put(csm, kM01p, hc, o);
+        if (htask == 0) {  // to link 0 at y+y
+          inv_adj_mul(d, al, o);
+          scale_alg(-w01p, o);
+          march_put(csm, kM01q, hc, o);
+        } else {  // to link 1 at y+x
+          inv_adj_mul(a, al, o);
+          scale_alg(w01q, o);
+          march_put(csm, kM01p, hc, o);
+        }
+      } else if (htask == 2) {  // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
+        load_link_r<R>(in.U, S, 1, hs, a);
+        load_link_r<R>(in.U, S, 2, hyp, bb);
+        load_link_r<R>(in.U, S, 1, hzp, cc);
+        load_link_r<R>(in.U, S, 2, hs, d);
+        plaquette_alg(a, bb, cc, d, al);
+        inv_adj_mul(a, al, o);  // to link 2 at y+y
+        scale_alg(w12q, o);
+        march_put(csm, kM12p, hc, o);
+      } else {  // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
+        load_link_r<R>(in.U, S, 0, hs, a);
         load_link_r<R>(in.U, S, 2, hxp, bb);
         load_link_r<R>(in.U, S, 0, hzp, cc);
         load_link_r<R>(in.U, S, 2, hs, d);
         plaquette_alg(a, bb, cc, d, al);
-        inv_adj_mul(a, al, o);
+        inv_adj_mul(a, al, o);  // to link 2 at y+x
         scale_alg(w02q, o);
         march_put(csm, kM02p, hc, o);
-      } else {  // owner y0-1: plane (0,1) -> link 0 at y0, plane (1,2) -> link 2 at y0
-        load_link_r<R>(in.U, S, 0, hs, a);
-        load_link_r<R>(in.U, S, 1, hxp, bb);
-        load_link_r<R>(in.U, S, 0, hyp, cc);
-        load_link_r<R>(in.U, S, 1, hs, d);
-        plaquette_alg(a, bb, cc, d, al);
-        inv_adj_mul(d, al, o);
-        scale_alg(-w01p, o);
-        march_put(csm, kM01q, hc, o);
-        // plane (1,2): a = U_1(y) (held in d), b = U_2(y+y), c = U_1(y+z), d = U_2(y) (loaded into a)
-        load_link_r<R>(in.U, S, 2, hyp, bb);
-        load_link_r<R>(in.U, S, 1, hzp, cc);
-        load_link_r<R>(in.U, S, 2, hs, a);
-        plaquette_alg(d, bb, cc, a, al);
-        inv_adj_mul(d, al, o);
-        scale_alg(w12q, o);
-        march_put(csm, kM12p, hc, o);
       }
     }
     __syncthreads();
