@@ -55,6 +55,11 @@ constexpr int kGfBlocks = 1216;
 constexpr int kFftThreads = 256;
 constexpr int kFftMaxTile = 4096;  // complex doubles staged per block (64 KB)
 constexpr size_t kFftMaxSmem = 227 * 1024;  // shared memory a block may opt into
+// Build knob: power-of-two lengths through the mixed-radix Stockham kernel (radix 4) instead of the
+// radix-2 kernel.
+#ifndef GLASMA_FFT_POW2_STOCKHAM
+#define GLASMA_FFT_POW2_STOCKHAM 0
+#endif
 
 inline unsigned blocks_for(long long n, int threads, int cap) {
   long long b = (n + threads - 1) / threads;
@@ -621,7 +626,8 @@ int ilog2(int n) {
   while ((1 << l) < n) l++;
   return l;
 }
-int twiddle_count(int n) { return is_pow2(n) ? (n / 2 > 0 ? n / 2 : 1) : n; }
+// the radix-2 kernel reads exp(-2 pi i k/n) for k < n/2, the mixed-radix kernel for k < n
+int twiddle_count(int n) { return (is_pow2(n) && !GLASMA_FFT_POW2_STOCKHAM) ? (n / 2 > 0 ? n / 2 : 1) : n; }
 
 int tile_lines_for(int n, long long st, long long nlines_total) {
   int cap = kFftMaxTile / n;
@@ -642,8 +648,8 @@ cudaError_t fft_lines_t(C* X, int n, long long st, long long total, int inverse,
   const long long nlines = total / n;
   const int tl = tile_lines_for(n, st, nlines);
   const long long tiles = nlines / tl;
-  if (is_pow2(n)) {
-    if (n == 1) return cudaSuccess;
+  if (n == 1) return cudaSuccess;
+  if (is_pow2(n) && !GLASMA_FFT_POW2_STOCKHAM) {
     const size_t smem = ((size_t)(n / 2) + (size_t)tl * (n + 1)) * sizeof(C);
     cudaFuncSetAttribute(fft_pow2_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     fft_pow2_kernel<C><<<(unsigned)tiles, kFftThreads, smem, stream>>>(X, ilog2(n), st, ilog2(tl), st > 1 ? st / tl : 0,
@@ -733,7 +739,7 @@ int prepare(GaugeFixState** ps, const GaugeFixArgs& a, std::string* err) {
     const int ns[3] = {a.g.nx, a.g.ny, a.g.nz};
     for (int n : ns) {
       if (s->twiddles.count(n)) continue;
-      const int count = is_pow2(n) ? (n / 2 > 0 ? n / 2 : 1) : n;
+      const int count = twiddle_count(n);
       double2* tw = nullptr;
       e = cudaMalloc(&tw, sizeof(double2) * count);
       if (e != cudaSuccess) {
