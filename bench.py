@@ -883,8 +883,10 @@ def run_precision(args):
         gmax, gavg = lat.gauss()
         umax, uavg = lat.unitarity()
         r, _, _ = lat.pressure_anisotropy(z0, z1)
-        return {"T00": b[9], "ELECTRIC": b[13], "MAGNETIC": b[14], "gauss_max": gmax, "gauss_avg": gavg,
-                "unitarity_max": umax, "pl_over_pt": r}
+        # P_L = TZZ and P_T = (TXX + TYY) / 2 of the whole lattice (the central slices' ratio is
+        # ill-conditioned here: the nucleus moves away from them and leaves P_T ~ 0 there)
+        return {"T00": b[9], "ELECTRIC": b[13], "MAGNETIC": b[14], "P_L": b[12], "P_T": 0.5 * (b[10] + b[11]),
+                "gauss_max": gmax, "gauss_avg": gavg, "unitarity_max": umax, "pl_over_pt_central": r}
 
     def evolve(lat):
         rows = [measure(lat)]
