@@ -141,8 +141,8 @@ int glasma_step(glasma_lattice* h, double dt, int nsteps, unsigned flags);
  * the other methods up to rounding), two kernels per step, 48 reals per site more memory (falls back
  * to two-pass for a call when that cannot be allocated).  GLASMA_STEP_MARCH: the plaquette method in
  * one kernel per step, each block marching along z through a tile of (x, y) sites (the rotated force
- * terms handed over in shared memory and registers instead of HBM); bit-identical to
- * GLASMA_STEP_PLAQUETTE, with the one-pass method's second buffer set (falls back to two-pass for a
+ * terms handed over in shared memory and registers instead of HBM); equal to GLASMA_STEP_PLAQUETTE
+ * up to rounding, with the one-pass method's second buffer set (falls back to two-pass for a
  * call when that cannot be allocated).
  * glasma_get_step_method reports the method the last glasma_step call used. */
 #define GLASMA_STEP_ONE_PASS 0

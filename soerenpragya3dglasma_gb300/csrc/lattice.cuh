@@ -197,7 +197,7 @@ cudaError_t launch_plaquette_step(const Geometry& g, FieldPtrs<T> f, T* contrib,
 
 // One step by the plaquette method in one launch (march.cuh): blocks own (x, y) tiles and march along
 // z; reads U, J, JStat of time t from `in`, writes those of t+dt to `out` (distinct buffers), E in
-// place in in.E, UOld (when save_uold) in in.UOld.  Bit-identical to launch_plaquette_step.  lz: z
+// place in in.E, UOld (when save_uold) in in.UOld.  Equal to launch_plaquette_step up to rounding.  lz: z
 // slices per block (0 = chosen from the lattice).
 template <typename T>
 cudaError_t launch_march_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, double dt, bool save_uold, int lz,

@@ -17,8 +17,9 @@
 //      order the two-kernel method adds them), then runs the link/J tail of links_site: the two half
 //      steps of the links, SaveOldLink, UpdateJ with the static currents of t+dt at z and z+1 (the
 //      latter formed here, carried to the next slice).
-// Every plaquette, rotation and sum is the two-kernel method's own expression with the same inputs,
-// so the fields equal that method's bit for bit.  The links, currents and static currents of t are
+// Every plaquette, rotation and sum is the two-kernel method's own expression with the same inputs
+// in the same order, so the fields equal that method's up to rounding (the compiler contracts a few
+// products into fused multiply-adds differently in the two kernels: 1e-15 in FP64).  The links, currents and static currents of t are
 // read from one buffer set and those of t+dt written to a second (`out`), as in the one-pass step:
 // neighbouring blocks still read the links of t while this one writes; E is updated in place (read
 // and written only by its own site).  Per site and step each per-site array is read and written once

@@ -228,7 +228,7 @@ class Lattice:
         """"plaquette" (default: the electric force summed plaquette by plaquette, two kernels and a
         contribution buffer), "two_pass" (two kernels per step, in place, staple form) or "one_pass"
         (one kernel per step over two buffer sets; bit-identical to two_pass) or "march" (the plaquette
-        method in one kernel per step, blocks marching along z; bit-identical to plaquette).  The
+        method in one kernel per step, blocks marching along z; equal to plaquette up to rounding).  The
         plaquette methods equal the staple ones up to rounding."""
         check(self.lib.glasma_set_step_method(self.h, self.STEP_METHODS[method]))
 
