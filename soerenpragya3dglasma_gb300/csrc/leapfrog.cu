@@ -89,17 +89,17 @@ __global__ void __launch_bounds__(kThreads) j_only_kernel(Geometry g, FieldPtrs<
   const I sg = (z == 0) ? s - plane : (z == g.nz - 1 ? s + plane : (I)-1);
   Mat<T> uz;
   load_link(f.U, S, 2, s, uz);
-  Alg<T> up, st, j;
+  Alg<T> up, um, st, j;
   load_alg(f.JpStat, S, 0, s + plane, st);
-  adj_mul(uz, st, up);
+  load_alg(f.JmStat, S, 0, s + plane, j);
+  rotate_currents<T, true>(uz, st, j, up, um);
   load_alg(f.JpStat, S, 0, s, st);
   load_alg(f.Jp, S, 0, s, j);
 #pragma unroll
   for (int a = 0; a < 8; a++) j.a[a] += -cj * (up.a[a] - st.a[a]);
   store_alg(f.Jp, S, 0, s, j);
   if (sg >= 0) store_alg(f.Jp, S, 0, sg, j);
-  load_alg(f.JmStat, S, 0, s + plane, st);
-  adj_mul(uz, st, up);
+  up = um;
   load_alg(f.JmStat, S, 0, s, st);
   load_alg(f.Jm, S, 0, s, j);
 #pragma unroll

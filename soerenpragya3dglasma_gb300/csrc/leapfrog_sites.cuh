@@ -9,6 +9,35 @@ namespace glasma {
 
 constexpr int kThreads = 128;
 
+// Pairs of adjoint actions by one matrix go through inv_adj_mul2 / adj_mul2 (one product pair instead
+// of two); the double-float force kernel keeps its out-of-line single actions (ddf.cuh).
+template <typename TC>
+constexpr bool kPairRotations = !std::is_same<TC, ddf>::value;
+// The pairs of the current transport (Jp and Jm rotated by one link) only in FP64, where the FP64 pipe
+// bounds the kernels: at the FP32 link kernels' 64-register cap the paired form spills.
+template <typename T>
+constexpr bool kPairCurrents = std::is_same<T, double>::value;
+
+// out_p = V (t.ep) V^d, out_m = V (t.em) V^d (adj = true) or the V^d . V forms, paired where kPairCurrents
+template <typename T, bool adj>
+__device__ __forceinline__ void rotate_currents(const Mat<T>& V, const Alg<T>& ep, const Alg<T>& em, Alg<T>& out_p,
+                                                Alg<T>& out_m) {
+  if constexpr (kPairCurrents<T>) {
+    if constexpr (adj)
+      adj_mul2(V, ep, em, out_p, out_m);
+    else
+      inv_adj_mul2(V, ep, em, out_p, out_m);
+  } else {
+    if constexpr (adj) {
+      adj_mul(V, ep, out_p);
+      adj_mul(V, em, out_m);
+    } else {
+      inv_adj_mul(V, ep, out_p);
+      inv_adj_mul(V, em, out_m);
+    }
+  }
+}
+
 // Blocks per SM the register allocation must leave room for (the register cap is 64K / (128 * n)),
 // chosen by measurement on GB300; overridable at build time for tuning sweeps.
 // (GB300 sweep, 128x128x512: FP32 K1 fastest at 5 blocks/SM, K2 at 8; FP64 is FP64-ALU bound.)
@@ -187,9 +216,10 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
     const I szm = s - plane;
     Mat<T> uzm;
     load_link_r<R>(f.U, S, 2, szm, uzm);
-    Alg<T> down, jc, st;
+    Alg<T> down, downm, jc, st;
     load_alg(f.Jp, S, 0, szm, jc);
-    inv_adj_mul(uzm, jc, down);
+    load_alg(f.Jm, S, 0, szm, st);
+    rotate_currents<T, false>(uzm, jc, st, down, downm);
     load_alg(f.Jp, S, 0, s, jc);
     load_alg(f.JpStat, S, 0, s, st);
     axpy_diff(st, -p.cj, jc, down);
@@ -197,8 +227,7 @@ __device__ __forceinline__ void efield_site(const Geometry& g, const FieldPtrs<T
       store_alg(f.JpStat, S, 0, s, st);
       if (sg >= 0) store_alg(f.JpStat, S, 0, sg, st);
     }
-    load_alg(f.Jm, S, 0, szm, jc);
-    inv_adj_mul(uzm, jc, down);
+    down = downm;
     load_alg(f.Jm, S, 0, s, jc);
     load_alg(f.JmStat, S, 0, s, st);
     axpy_diff(st, p.cj, jc, down);
@@ -277,60 +306,117 @@ __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtr
   load_link_c<R>(f.U, S, 0, s, u0);
   load_link_c<R>(f.U, S, 1, s, u1);
   load_link_c<R>(f.U, S, 2, s, u2);
-  if (interior) {
-    // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
-    load_link_c<R>(f.U, S, 1, sxp, b);
-    load_link_c<R>(f.U, S, 0, syp, c);
-    plaquette_alg(u0, b, c, u1, al);
+  if constexpr (kPairRotations<TC>) {
+    // the three plaquettes first, then the six rotations in pairs by the same link:
+    // u1 (al01 -> link 0 at y+y, al12 -> link 2 at y+y), u0 (al01 -> link 1 at y+x, al02 -> link 2 at
+    // y+x), u2 (al02 -> link 0 at y+z, al12 -> link 1 at y+z)
+    Alg<TC> al01, al12, out2;
+    if (interior) {
+      // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
+      load_link_c<R>(f.U, S, 1, sxp, b);
+      load_link_c<R>(f.U, S, 0, syp, c);
+      plaquette_alg(u0, b, c, u1, al01);
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      F0.a[k] = w01p * al.a[k];
-      F1.a[k] = -w01q * al.a[k];
+      for (int k = 0; k < 8; k++) {
+        F0.a[k] = w01p * al01.a[k];
+        F1.a[k] = -w01q * al01.a[k];
+      }
     }
-    inv_adj_mul(u1, al, out);  // to link 0 at y+y
-    scale_alg(-w01p, out);
-    if (!p.dry) store_alg_c(C, S, kC01q * 8, s, out);
-    inv_adj_mul(u0, al, out);  // to link 1 at y+x
-    scale_alg(w01q, out);
-    if (!p.dry) store_alg_c(C, S, kC01p * 8, s, out);
-  }
-  // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
-  load_link_c<R>(f.U, S, 2, sxp, b);
-  load_link_c<R>(f.U, S, 0, szp, c);
-  plaquette_alg(u0, b, c, u2, al);
-  if (below_top) {
-    inv_adj_mul(u2, al, out);  // to link 0 at y+z
-    scale_alg(-w02p, out);
-    if (!p.dry) store_alg_c(C, S, kC02q * 8, s, out);
-  }
-  if (interior) {
+    // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
+    load_link_c<R>(f.U, S, 2, sxp, b);
+    load_link_c<R>(f.U, S, 0, szp, c);
+    plaquette_alg(u0, b, c, u2, al);
+    // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
+    load_link_c<R>(f.U, S, 2, syp, b);
+    load_link_c<R>(f.U, S, 1, szp, c);
+    plaquette_alg(u1, b, c, u2, al12);
+    if (below_top) {
+      inv_adj_mul2(u2, al, al12, out, out2);
+      scale_alg(-w02p, out);  // to link 0 at y+z
+      scale_alg(-w12p, out2);  // to link 1 at y+z
+      if (!p.dry) {
+        store_alg_c(C, S, kC02q * 8, s, out);
+        store_alg_c(C, S, kC12q * 8, s, out2);
+      }
+    }
+    if (!interior) return;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       F0.a[k] += w02p * al.a[k];
       F2.a[k] = -w02q * al.a[k];
+      F1.a[k] += w12p * al12.a[k];
+      F2.a[k] -= w12q * al12.a[k];
     }
-    inv_adj_mul(u0, al, out);  // to link 2 at y+x
-    scale_alg(w02q, out);
-    if (!p.dry) store_alg_c(C, S, kC02p * 8, s, out);
-  }
-  // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
-  load_link_c<R>(f.U, S, 2, syp, b);
-  load_link_c<R>(f.U, S, 1, szp, c);
-  plaquette_alg(u1, b, c, u2, al);
-  if (below_top) {
-    inv_adj_mul(u2, al, out);  // to link 1 at y+z
-    scale_alg(-w12p, out);
-    if (!p.dry) store_alg_c(C, S, kC12q * 8, s, out);
-  }
-  if (!interior) return;
+    inv_adj_mul2(u1, al01, al12, out, out2);
+    scale_alg(-w01p, out);  // to link 0 at y+y
+    scale_alg(w12q, out2);  // to link 2 at y+y
+    if (!p.dry) {
+      store_alg_c(C, S, kC01q * 8, s, out);
+      store_alg_c(C, S, kC12p * 8, s, out2);
+    }
+    inv_adj_mul2(u0, al01, al, out, out2);
+    scale_alg(w01q, out);  // to link 1 at y+x
+    scale_alg(w02q, out2);  // to link 2 at y+x
+    if (!p.dry) {
+      store_alg_c(C, S, kC01p * 8, s, out);
+      store_alg_c(C, S, kC02p * 8, s, out2);
+    }
+  } else {
+    if (interior) {
+      // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
+      load_link_c<R>(f.U, S, 1, sxp, b);
+      load_link_c<R>(f.U, S, 0, syp, c);
+      plaquette_alg(u0, b, c, u1, al);
 #pragma unroll
-  for (int k = 0; k < 8; k++) {
-    F1.a[k] += w12p * al.a[k];
-    F2.a[k] -= w12q * al.a[k];
+      for (int k = 0; k < 8; k++) {
+        F0.a[k] = w01p * al.a[k];
+        F1.a[k] = -w01q * al.a[k];
+      }
+      inv_adj_mul(u1, al, out);  // to link 0 at y+y
+      scale_alg(-w01p, out);
+      if (!p.dry) store_alg_c(C, S, kC01q * 8, s, out);
+      inv_adj_mul(u0, al, out);  // to link 1 at y+x
+      scale_alg(w01q, out);
+      if (!p.dry) store_alg_c(C, S, kC01p * 8, s, out);
+    }
+    // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
+    load_link_c<R>(f.U, S, 2, sxp, b);
+    load_link_c<R>(f.U, S, 0, szp, c);
+    plaquette_alg(u0, b, c, u2, al);
+    if (below_top) {
+      inv_adj_mul(u2, al, out);  // to link 0 at y+z
+      scale_alg(-w02p, out);
+      if (!p.dry) store_alg_c(C, S, kC02q * 8, s, out);
+    }
+    if (interior) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        F0.a[k] += w02p * al.a[k];
+        F2.a[k] = -w02q * al.a[k];
+      }
+      inv_adj_mul(u0, al, out);  // to link 2 at y+x
+      scale_alg(w02q, out);
+      if (!p.dry) store_alg_c(C, S, kC02p * 8, s, out);
+    }
+    // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
+    load_link_c<R>(f.U, S, 2, syp, b);
+    load_link_c<R>(f.U, S, 1, szp, c);
+    plaquette_alg(u1, b, c, u2, al);
+    if (below_top) {
+      inv_adj_mul(u2, al, out);  // to link 1 at y+z
+      scale_alg(-w12p, out);
+      if (!p.dry) store_alg_c(C, S, kC12q * 8, s, out);
+    }
+    if (!interior) return;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      F1.a[k] += w12p * al.a[k];
+      F2.a[k] -= w12q * al.a[k];
+    }
+    inv_adj_mul(u1, al, out);  // to link 2 at y+y
+    scale_alg(w12q, out);
+    if (!p.dry) store_alg_c(C, S, kC12p * 8, s, out);
   }
-  inv_adj_mul(u1, al, out);  // to link 2 at y+y
-  scale_alg(w12q, out);
-  if (!p.dry) store_alg_c(C, S, kC12p * 8, s, out);
   // E += the forces of the plaquettes owned here (+ the current source on E_z); K2' adds the rest
   Alg<TC> e;
   load_alg_c(f.E, S, 0, s, e);
@@ -358,9 +444,14 @@ __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtr
   const TC cj = to_compute<TC>(p.cj);
   Mat<TC> uzm;
   load_link_c<R>(f.U, S, 2, szm, uzm);
-  Alg<TC> down, jc, st;
+  Alg<TC> down, downm, jc, st;
   load_alg_c(f.Jp, S, 0, szm, jc);
-  inv_adj_mul(uzm, jc, down);
+  if constexpr (kPairRotations<TC>) {
+    load_alg_c(f.Jm, S, 0, szm, st);
+    rotate_currents<TC, false>(uzm, jc, st, down, downm);
+  } else {
+    inv_adj_mul(uzm, jc, down);
+  }
   load_alg_c(f.Jp, S, 0, s, jc);
   load_alg_c(f.JpStat, S, 0, s, st);
   axpy_diff(st, -cj, jc, down);
@@ -368,8 +459,12 @@ __device__ __forceinline__ void plaquette_site(const Geometry& g, const FieldPtr
     store_alg_c(f.JpStat, S, 0, s, st);
     if (sg >= 0) store_alg_c(f.JpStat, S, 0, sg, st);
   }
-  load_alg_c(f.Jm, S, 0, szm, jc);
-  inv_adj_mul(uzm, jc, down);
+  if constexpr (kPairRotations<TC>) {
+    down = downm;
+  } else {
+    load_alg_c(f.Jm, S, 0, szm, jc);
+    inv_adj_mul(uzm, jc, down);
+  }
   load_alg_c(f.Jm, S, 0, s, jc);
   load_alg_c(f.JmStat, S, 0, s, st);
   axpy_diff(st, cj, jc, down);
@@ -476,17 +571,26 @@ __device__ __forceinline__ void links_site(const Geometry& g, const FieldPtrs<T>
       if (sg >= 0) store_link(f.UOld, S, mu, sg, uh);
     }
     if (mu == 2 && p.do_j) {
-      Alg<T> up, st, j;
+      Alg<T> up, um, st, j;
       const I szp = s + plane;
       load_alg(f.JpStat, S, 0, szp, st);
-      adj_mul(uh, st, up);
+      if constexpr (kPairCurrents<T>) {
+        load_alg(f.JmStat, S, 0, szp, j);
+        rotate_currents<T, true>(uh, st, j, up, um);
+      } else {
+        adj_mul(uh, st, up);
+      }
       load_alg(f.JpStat, S, 0, s, st);
       load_alg(f.Jp, S, 0, s, j);
       axpy_diff(j, -p.cj, up, st);
       store_alg(f.Jp, S, 0, s, j);
       if (sg >= 0) store_alg(f.Jp, S, 0, sg, j);
-      load_alg(f.JmStat, S, 0, szp, st);
-      adj_mul(uh, st, up);
+      if constexpr (kPairCurrents<T>) {
+        up = um;
+      } else {
+        load_alg(f.JmStat, S, 0, szp, st);
+        adj_mul(uh, st, up);
+      }
       load_alg(f.JmStat, S, 0, s, st);
       load_alg(f.Jm, S, 0, s, j);
       axpy_diff(j, p.cj, up, st);
@@ -518,20 +622,19 @@ template <typename T, typename I, int R = 3>
 __device__ __forceinline__ void fused_currents(const FieldPtrs<T>& in, const FieldPtrs<T>& out, I S, I plane, I s,
                                                I sg, bool hi, const Mat<T>& uz, const Mat<T>& uhz, T cj, bool dry) {
   const I szm = s - plane, szp = s + plane;
-  Alg<T> jc, down, sp, sm;
+  Alg<T> jc, down, downm, sp, sm;
   {
     Mat<T> w;
     load_link_r<R>(in.U, S, 2, szm, w);
     load_alg(in.Jp, S, 0, szm, jc);
-    inv_adj_mul(w, jc, down);
+    load_alg(in.Jm, S, 0, szm, sm);
+    rotate_currents<T, false>(w, jc, sm, down, downm);
     load_alg(in.Jp, S, 0, s, jc);
     load_alg(in.JpStat, S, 0, s, sp);
     axpy_diff(sp, -cj, jc, down);
-    load_alg(in.Jm, S, 0, szm, jc);
-    inv_adj_mul(w, jc, down);
     load_alg(in.Jm, S, 0, s, jc);
     load_alg(in.JmStat, S, 0, s, sm);
-    axpy_diff(sm, cj, jc, down);
+    axpy_diff(sm, cj, jc, downm);
   }
   if (!dry) {
     store_alg(out.JpStat, S, 0, s, sp);
@@ -548,25 +651,24 @@ __device__ __forceinline__ void fused_currents(const FieldPtrs<T>& in, const Fie
     um = sm;
   } else {
     load_alg(in.Jp, S, 0, s, jc);
-    inv_adj_mul(uz, jc, down);
+    load_alg(in.Jm, S, 0, s, um);
+    rotate_currents<T, false>(uz, jc, um, down, downm);
     load_alg(in.Jp, S, 0, szp, jc);
     load_alg(in.JpStat, S, 0, szp, up);
     axpy_diff(up, -cj, jc, down);
-    load_alg(in.Jm, S, 0, s, jc);
-    inv_adj_mul(uz, jc, down);
     load_alg(in.Jm, S, 0, szp, jc);
     load_alg(in.JmStat, S, 0, szp, um);
-    axpy_diff(um, cj, jc, down);
+    axpy_diff(um, cj, jc, downm);
   }
-  Alg<T> t, j;
-  adj_mul(uhz, up, t);
+  Alg<T> t, tm, j;
+  rotate_currents<T, true>(uhz, up, um, t, tm);
   load_alg(in.Jp, S, 0, s, j);
   axpy_diff(j, -cj, t, sp);
   if (!dry) {
     store_alg(out.Jp, S, 0, s, j);
     if (sg >= 0) store_alg(out.Jp, S, 0, sg, j);
   }
-  adj_mul(uhz, um, t);
+  t = tm;
   load_alg(in.Jm, S, 0, s, j);
   axpy_diff(j, cj, t, sm);
   if (!dry) {

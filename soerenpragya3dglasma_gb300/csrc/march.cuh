@@ -71,17 +71,16 @@ __device__ __forceinline__ void march_get(const T* csm, int slot, int c, Alg<T>&
 template <typename T, typename I>
 __device__ __forceinline__ void march_jstat(const FieldPtrs<T>& in, I S, I plane, I sz, const Mat<T>& uzm, T cj,
                                             Alg<T>& stp, Alg<T>& stm) {
-  Alg<T> down, jc;
+  Alg<T> down, downm, jc;
   load_alg(in.Jp, S, 0, sz - plane, jc);
-  inv_adj_mul(uzm, jc, down);
+  load_alg(in.Jm, S, 0, sz - plane, stm);
+  rotate_currents<T, false>(uzm, jc, stm, down, downm);
   load_alg(in.Jp, S, 0, sz, jc);
   load_alg(in.JpStat, S, 0, sz, stp);
   axpy_diff(stp, -cj, jc, down);
-  load_alg(in.Jm, S, 0, sz - plane, jc);
-  inv_adj_mul(uzm, jc, down);
   load_alg(in.Jm, S, 0, sz, jc);
   load_alg(in.JmStat, S, 0, sz, stm);
-  axpy_diff(stm, cj, jc, down);
+  axpy_diff(stm, cj, jc, downm);
 }
 
 template <typename T, typename I, int R, int kMarchTX>
@@ -177,15 +176,15 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     load_link_r<R>(in.U, S, 0, s, u0);
     load_link_r<R>(in.U, S, 1, s, u1);
     load_link_r<R>(in.U, S, 2, s, u2);
+    Alg<T> al12;
     load_link_r<R>(in.U, S, 2, sxp, bb);
     load_link_r<R>(in.U, S, 0, szp, cc);
     plaquette_alg(u0, bb, cc, u2, al);
-    inv_adj_mul(u2, al, zc0);
-    scale_alg(-w02p, zc0);
     load_link_r<R>(in.U, S, 2, syp, bb);
     load_link_r<R>(in.U, S, 1, szp, cc);
-    plaquette_alg(u1, bb, cc, u2, al);
-    inv_adj_mul(u2, al, zc1);
+    plaquette_alg(u1, bb, cc, u2, al12);
+    inv_adj_mul2(u2, al, al12, zc0, zc1);
+    scale_alg(-w02p, zc0);
     scale_alg(-w12p, zc1);
     march_jstat(in, S, plane, s + plane, u2, pe.cj, stp, stm);
     if constexpr (kZsm) zput(zw, zc0, zc1);
@@ -205,60 +204,50 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
       load_link_r<R>(in.U, S, 0, s, u0);
       load_link_r<R>(in.U, S, 1, s, u1);
       load_link_r<R>(in.U, S, 2, s, u2);
+      // the three plaquettes, then the rotations in pairs by the same link (as plaquette_site)
+      Alg<T> al01, al12, o2;
       // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
       load_link_r<R>(in.U, S, 1, sxp, bb);
       load_link_r<R>(in.U, S, 0, syp, cc);
-      plaquette_alg(u0, bb, cc, u1, al);
+      plaquette_alg(u0, bb, cc, u1, al01);
 #pragma unroll
       for (int k = 0; k < 8; k++) {
-        F0.a[k] = w01p * al.a[k];
-        F1.a[k] = -w01q * al.a[k];
-      }
-      if (put_y) {  // to link 0 at y+y
-        inv_adj_mul(u1, al, o);
-        scale_alg(-w01p, o);
-        march_put(csm, kM01q, tid + kMarchTX, o);
-      }
-      if (put_x) {  // to link 1 at y+x
-        inv_adj_mul(u0, al, o);
-        scale_alg(w01q, o);
-        march_put(csm, kM01p, tid + 1, o);
+        F0.a[k] = w01p * al01.a[k];
+        F1.a[k] = -w01q * al01.a[k];
       }
       // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
       load_link_r<R>(in.U, S, 2, sxp, bb);
       load_link_r<R>(in.U, S, 0, szp, cc);
       plaquette_alg(u0, bb, cc, u2, al);
-      if (below_top) {  // to link 0 at y+z: the next slice of this thread
-        inv_adj_mul(u2, al, zn0);
-        scale_alg(-w02p, zn0);
-      }
+      // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
+      load_link_r<R>(in.U, S, 2, syp, bb);
+      load_link_r<R>(in.U, S, 1, szp, cc);
+      plaquette_alg(u1, bb, cc, u2, al12);
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         F0.a[k] += w02p * al.a[k];
         F2.a[k] = -w02q * al.a[k];
+        F1.a[k] += w12p * al12.a[k];
+        F2.a[k] -= w12q * al12.a[k];
       }
-      if (put_x) {  // to link 2 at y+x
-        inv_adj_mul(u0, al, o);
-        scale_alg(w02q, o);
-        march_put(csm, kM02p, tid + 1, o);
-      }
-      // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
-      load_link_r<R>(in.U, S, 2, syp, bb);
-      load_link_r<R>(in.U, S, 1, szp, cc);
-      plaquette_alg(u1, bb, cc, u2, al);
-      if (below_top) {  // to link 1 at y+z
-        inv_adj_mul(u2, al, zn1);
+      if (below_top) {  // to links 0 and 1 at y+z: the next slice of this thread
+        inv_adj_mul2(u2, al, al12, zn0, zn1);
+        scale_alg(-w02p, zn0);
         scale_alg(-w12p, zn1);
       }
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        F1.a[k] += w12p * al.a[k];
-        F2.a[k] -= w12q * al.a[k];
+      if (put_y) {  // to links 0 and 2 at y+y
+        inv_adj_mul2(u1, al01, al12, o, o2);
+        scale_alg(-w01p, o);
+        scale_alg(w12q, o2);
+        march_put(csm, kM01q, tid + kMarchTX, o);
+        march_put(csm, kM12p, tid + kMarchTX, o2);
       }
-      if (put_y) {  // to link 2 at y+y
-        inv_adj_mul(u1, al, o);
-        scale_alg(w12q, o);
-        march_put(csm, kM12p, tid + kMarchTX, o);
+      if (put_x) {  // to links 1 and 2 at y+x
+        inv_adj_mul2(u0, al01, al, o, o2);
+        scale_alg(w01q, o);
+        scale_alg(w02q, o2);
+        march_put(csm, kM01p, tid + 1, o);
+        march_put(csm, kM02p, tid + 1, o2);
       }
       if constexpr (kZsm) {
         if (below_top) zput(z, zn0, zn1);
@@ -373,13 +362,13 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
               store_link(in.UOld, S, mu, s, uh);
               if (sg >= 0) store_link(in.UOld, S, mu, sg, uh);
             }
-            Alg<T> up, j;
-            adj_mul(uh, sp1, up);
+            Alg<T> up, um, j;
+            rotate_currents<T, true>(uh, sp1, sm1, up, um);
             load_alg(in.Jp, S, 0, s, j);
             axpy_diff(j, -pl.cj, up, stp);
             store_alg(out.Jp, S, 0, s, j);
             if (sg >= 0) store_alg(out.Jp, S, 0, sg, j);
-            adj_mul(uh, sm1, up);
+            up = um;
             load_alg(in.Jm, S, 0, s, j);
             axpy_diff(j, pl.cj, up, stm);
             store_alg(out.Jm, S, 0, s, j);

@@ -271,6 +271,60 @@ __device__ __forceinline__ void inv_adj_mul(const Mat<T>& V, const Alg<T>& e, Al
   alg_from_herm(R, out);
 }
 
+// Two adjoint actions by one matrix from one pair of complex products: with M = t.e1 + i t.e2, the
+// product C = V M V^d (or V^d M V) is A + iB, where A and B are the two (Hermitian) actions, so A and B
+// are C's Hermitian and anti-Hermitian parts: A_ij = (C_ij + C_ji^*)/2, B_ij = (C_ij - C_ji^*)/(2i).
+// Two full products (~216 FMA) instead of two Hermitian-result pairs (~288 FMA); equal to the single
+// forms up to rounding.  out1 / out2 as alg_from_herm of A / B.
+template <typename T>
+__device__ __forceinline__ void split_herm_pair(const Mat<T>& C, Alg<T>& out1, Alg<T>& out2) {
+  // C_ij at e[i + 3j]: 01 -> 3, 10 -> 1, 02 -> 6, 20 -> 2, 12 -> 7, 21 -> 5
+  out1.a[0] = C.e[3].re + C.e[1].re;
+  out1.a[1] = C.e[1].im - C.e[3].im;
+  out1.a[2] = C.e[0].re - C.e[4].re;
+  out1.a[3] = C.e[6].re + C.e[2].re;
+  out1.a[4] = C.e[2].im - C.e[6].im;
+  out1.a[5] = C.e[7].re + C.e[5].re;
+  out1.a[6] = C.e[5].im - C.e[7].im;
+  out1.a[7] = (C.e[0].re + C.e[4].re - T(2) * C.e[8].re) * Consts<T>::inv_sqrt3();
+  out2.a[0] = C.e[3].im + C.e[1].im;
+  out2.a[1] = C.e[3].re - C.e[1].re;
+  out2.a[2] = C.e[0].im - C.e[4].im;
+  out2.a[3] = C.e[6].im + C.e[2].im;
+  out2.a[4] = C.e[6].re - C.e[2].re;
+  out2.a[5] = C.e[7].im + C.e[5].im;
+  out2.a[6] = C.e[7].re - C.e[5].re;
+  out2.a[7] = (C.e[0].im + C.e[4].im - T(2) * C.e[8].im) * Consts<T>::inv_sqrt3();
+}
+template <typename T>
+__device__ __forceinline__ void herm_pair(const Alg<T>& e1, const Alg<T>& e2, Mat<T>& M) {
+  Mat<T> M1, M2;
+  herm_from_alg(e1, M1);
+  herm_from_alg(e2, M2);
+#pragma unroll
+  for (int k = 0; k < 9; k++) M.e[k] = mk<T>(M1.e[k].re - M2.e[k].im, M1.e[k].im + M2.e[k].re);
+}
+// out1 = V (t.e1) V^dagger, out2 = V (t.e2) V^dagger
+template <typename T>
+__device__ __forceinline__ void adj_mul2(const Mat<T>& V, const Alg<T>& e1, const Alg<T>& e2, Alg<T>& out1,
+                                         Alg<T>& out2) {
+  Mat<T> M, W, C;
+  herm_pair(e1, e2, M);
+  mul_nn(V, M, W);
+  mul_nd(W, V, C);
+  split_herm_pair(C, out1, out2);
+}
+// out1 = V^dagger (t.e1) V, out2 = V^dagger (t.e2) V
+template <typename T>
+__device__ __forceinline__ void inv_adj_mul2(const Mat<T>& V, const Alg<T>& e1, const Alg<T>& e2, Alg<T>& out1,
+                                             Alg<T>& out2) {
+  Mat<T> M, W, C;
+  herm_pair(e1, e2, M);
+  mul_dn(V, M, W);
+  mul_nn(W, V, C);
+  split_herm_pair(C, out1, out2);
+}
+
 // The entries of C = A B that retr_itg reads: every off-diagonal entry and the imaginary diagonal.
 // Same arithmetic, per entry, as mul_nn.
 template <typename T>
