@@ -294,13 +294,21 @@ cudaError_t launch_fused_step(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> o
 #endif
 constexpr int kMarchTileX = GLASMA_MARCH_TX;  // tile of kMarchTileX x (128 / kMarchTileX) sites
 
+template <typename T, typename I, int R>
+void launch_march_kernel(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, const MarchParams<T>& mp, unsigned grid,
+                         cudaStream_t stream) {
+  const int smem = (int)(kMarchSmemReals * sizeof(T));
+  cudaFuncSetAttribute(march_step_kernel<T, I, R, kMarchTileX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  march_step_kernel<T, I, R, kMarchTileX><<<grid, kMarchThreads, smem, stream>>>(g, in, out, mp);
+}
+
 template <typename T, int R>
 void launch_march_rows(const Geometry& g, FieldPtrs<T> in, FieldPtrs<T> out, const MarchParams<T>& mp, unsigned grid,
                        cudaStream_t stream) {
   if (use_32bit_index(g))
-    march_step_kernel<T, int, R, kMarchTileX><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
+    launch_march_kernel<T, int, R>(g, in, out, mp, grid, stream);
   else
-    march_step_kernel<T, long long, R, kMarchTileX><<<grid, kMarchThreads, 0, stream>>>(g, in, out, mp);
+    launch_march_kernel<T, long long, R>(g, in, out, mp, grid, stream);
 }
 
 // Slices per block of the z-marching step: enough (tile, chunk) blocks to fill every SM several times

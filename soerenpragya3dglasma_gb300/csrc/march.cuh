@@ -83,29 +83,37 @@ __device__ __forceinline__ void march_jstat(const FieldPtrs<T>& in, I S, I plane
   axpy_diff(stm, cj, jc, downm);
 }
 
+// The plaquette in plane (p, q) owned at site so: a = U_p(so), b = U_q(so+p), c = U_p(so+q), d = U_q(so).
+template <typename T, typename I, int R>
+__device__ __forceinline__ void march_plaquette(const cx<T>* __restrict__ U, I S, int p, int q, I so, I sp, I sq,
+                                                Alg<T>& al) {
+  Mat<T> a, b, c, d;
+  load_link_r<R>(U, S, p, so, a);
+  load_link_r<R>(U, S, q, sp, b);
+  load_link_r<R>(U, S, p, sq, c);
+  load_link_r<R>(U, S, q, so, d);
+  plaquette_alg(a, b, c, d, al);
+}
+
+// Dynamic shared memory of the marching kernel, in reals: the in-plane terms by consumer (4 x 8), this
+// thread's plaquettes (planes (0,1), (0,2), (1,2) and its halo plaquette: 4 x 8) and the z-terms by
+// slice parity (2 x 16), per thread.
+constexpr int kMarchSmemReals = (32 + 32 + 32) * kMarchThreads;
+
+// The body is written for a small instruction footprint: one code path for every plaquette (own and
+// halo, in a loop), one for every rotation (a loop over pairs; the halo's single rotation is a pair
+// with a zero second vector), one for the next slice's static currents (the warm-up slice below the
+// chunk runs the same loop iteration), one exponential and one link application per link.  The first
+// version, with every case written out, stalled on instruction fetch (ncu: "no instruction" the
+// largest stall) at 1.7x the two-kernel method's time.
 template <typename T, typename I, int R, int kMarchTX>
 __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     march_step_kernel(const __grid_constant__ Geometry g, const __grid_constant__ FieldPtrs<T> in,
                       const __grid_constant__ FieldPtrs<T> out, const __grid_constant__ MarchParams<T> mp) {
-  __shared__ T csm[4 * 8 * kMarchThreads];
-  // FP32: the z-terms carried to the next slice wait in shared memory (each thread its own entries,
-  // two buffers by slice parity) instead of 16 registers; FP64 keeps them in registers
-  constexpr bool kZsm = sizeof(T) == 4;
-  __shared__ T zsm[kZsm ? 2 * 16 * kMarchThreads : 1];
-  auto zput = [&](int z, const Alg<T>& v0, const Alg<T>& v1) {
-#pragma unroll
-    for (int a = 0; a < 8; a++) {
-      zsm[((z & 1) * 16 + a) * kMarchThreads + threadIdx.x] = v0.a[a];
-      zsm[((z & 1) * 16 + 8 + a) * kMarchThreads + threadIdx.x] = v1.a[a];
-    }
-  };
-  auto zget = [&](int z, Alg<T>& v0, Alg<T>& v1) {
-#pragma unroll
-    for (int a = 0; a < 8; a++) {
-      v0.a[a] = zsm[((z & 1) * 16 + a) * kMarchThreads + threadIdx.x];
-      v1.a[a] = zsm[((z & 1) * 16 + 8 + a) * kMarchThreads + threadIdx.x];
-    }
-  };
+  extern __shared__ __align__(16) unsigned char march_smem[];
+  T* csm = reinterpret_cast<T*>(march_smem);  // [slot][a][consumer]
+  T* asm_ = csm + 32 * kMarchThreads;          // [plaquette slot][a][thread]
+  T* zsm = asm_ + 32 * kMarchThreads;          // [parity][16][thread]
   const I S = (I)g.S, plane = (I)g.plane;
   constexpr int kMarchTY = kMarchThreads / kMarchTX;
   static_assert(kMarchTY * kMarchTX == kMarchThreads && 2 * (kMarchTX + kMarchTY) <= kMarchThreads,
@@ -127,13 +135,22 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
   const T w01p = pe.gc[0] * pe.cnu[1], w01q = pe.gc[1] * pe.cnu[0];
   const T w02p = pe.gc[0] * pe.cnu[2], w02q = pe.gc[2] * pe.cnu[0];
   const T w12p = pe.gc[1] * pe.cnu[2], w12q = pe.gc[2] * pe.cnu[1];
-  // one halo plaquette of this thread in phase B (the owners just outside the tile: the row y0-1 and
-  // the column x0-1), grouped so that a warp mostly runs one kind:
-  //   [0, TX)            row owner (x0+t, y0-1), plane (0,1) -> link 0 at (x0+t, y0)
-  //   [TX, TX+TY)        column owner (x0-1, y0+t), plane (0,1) -> link 1 at (x0, y0+t)
-  //   [TX+TY, 2TX+TY)    row owner, plane (1,2) -> link 2 at (x0+t, y0)
-  //   [2TX+TY, 2TX+2TY)  column owner, plane (0,2) -> link 2 at (x0, y0+t)
-  int htask = -1, hx = 0, hy = 0, hc = 0;
+  auto put = [&](T* base, int slot, int idx, const Alg<T>& v) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) base[(slot * 8 + a) * kMarchThreads + idx] = v.a[a];
+  };
+  auto get = [&](const T* base, int slot, int idx, Alg<T>& v) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) v.a[a] = base[(slot * 8 + a) * kMarchThreads + idx];
+  };
+  // one halo plaquette of this thread (the owners just outside the tile: the row y0-1 and the column
+  // x0-1), grouped so that a warp mostly runs one kind:
+  //   [0, TX)            row owner (x0+t, y0-1), plane (0,1) -> link 0 at (x0+t, y0), rotated by d = U_1
+  //   [TX, TX+TY)        column owner (x0-1, y0+t), plane (0,1) -> link 1 at (x0, y0+t), by a = U_0
+  //   [TX+TY, 2TX+TY)    row owner, plane (1,2) -> link 2 at (x0+t, y0), by a = U_1
+  //   [2TX+TY, 2TX+2TY)  column owner, plane (0,2) -> link 2 at (x0, y0+t), by a = U_0
+  int hplane = -1, hx = 0, hy = 0, hc = 0, hrot = 0, hslot = 0;
+  T hw = T(0);
   {
     int t = tid, kind = -1;
     if (t < kMarchTX) {
@@ -145,154 +162,115 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
     } else if ((t -= kMarchTX) < kMarchTY) {
       kind = 3;
     }
-    if (kind == 0 || kind == 2) {
-      if (x0 + t < g.nx) {
-        htask = kind;
-        hx = x0 + t;
-        hy = y0 == 0 ? g.ny - 1 : y0 - 1;
-        hc = t;
-      }
-    } else if (kind == 1 || kind == 3) {
-      if (y0 + t < g.ny) {
-        htask = kind;
-        hx = x0 == 0 ? g.nx - 1 : x0 - 1;
-        hy = y0 + t;
-        hc = t * kMarchTX;
-      }
+    const bool row = kind == 0 || kind == 2;
+    if (kind >= 0 && (row ? x0 + t < g.nx : y0 + t < g.ny)) {
+      hx = row ? x0 + t : (x0 == 0 ? g.nx - 1 : x0 - 1);
+      hy = row ? (y0 == 0 ? g.ny - 1 : y0 - 1) : y0 + t;
+      hc = row ? t : t * kMarchTX;
+      hplane = kind <= 1 ? 0 : (kind == 2 ? 2 : 1);
+      hrot = kind == 0 ? 1 : (kind == 2 ? 1 : 0);  // the direction of the rotating link at the owner
+      hslot = kind == 0 ? kM01q : (kind == 1 ? kM01p : (kind == 2 ? kM12p : kM02p));
+      hw = kind == 0 ? -w01p : (kind == 1 ? w01q : (kind == 2 ? w12q : w02q));
     }
   }
   const bool put_x = lx + 1 < kMarchTX && x + 1 < g.nx;  // the x-neighbour is a site of this tile
   const bool put_y = ly + 1 < kMarchTY && y + 1 < g.ny;  // the y-neighbour is a site of this tile
 
-  // warm-up: the z-terms of the plaquettes owned one slice below the chunk (the ghost slice -1 for the
-  // first chunk), and the static currents of t+dt at the chunk's first slice
-  Alg<T> zc0, zc1, stp, stm;
-  if (own) {
-    const int zw = za - 1;
-    const I s = (I)site_index(g, x, y, zw);
-    const I sxp = nb<I>(g, x, y, zw, 1, 0, 0), syp = nb<I>(g, x, y, zw, 0, 1, 0), szp = s + plane;
-    Mat<T> u0, u1, u2, bb, cc;
-    Alg<T> al;
-    load_link_r<R>(in.U, S, 0, s, u0);
-    load_link_r<R>(in.U, S, 1, s, u1);
-    load_link_r<R>(in.U, S, 2, s, u2);
-    Alg<T> al12;
-    load_link_r<R>(in.U, S, 2, sxp, bb);
-    load_link_r<R>(in.U, S, 0, szp, cc);
-    plaquette_alg(u0, bb, cc, u2, al);
-    load_link_r<R>(in.U, S, 2, syp, bb);
-    load_link_r<R>(in.U, S, 1, szp, cc);
-    plaquette_alg(u1, bb, cc, u2, al12);
-    inv_adj_mul2(u2, al, al12, zc0, zc1);
-    scale_alg(-w02p, zc0);
-    scale_alg(-w12p, zc1);
-    march_jstat(in, S, plane, s + plane, u2, pe.cj, stp, stm);
-    if constexpr (kZsm) zput(zw, zc0, zc1);
-  }
-
+  Alg<T> stp = {}, stm = {};  // the static currents of t+dt at this slice
 #pragma unroll 1
-  for (int z = za; z < zb; z++) {
+  for (int z = za - 1; z < zb; z++) {
+    // z = za - 1: the slice below the chunk (the ghost slice for the first chunk): only its z-terms for
+    // the chunk's first slice and the static currents of t+dt there
+    const bool warm = z < za;
     const bool below_top = z < g.nz - 1;
-    Alg<T> F0, F1, F2, zn0 = {}, zn1 = {};
-    I s = 0;
-    // ---- A: the plaquettes owned at this site
-    if (own) {
-      s = (I)site_index(g, x, y, z);
-      const I sxp = nb<I>(g, x, y, z, 1, 0, 0), syp = nb<I>(g, x, y, z, 0, 1, 0), szp = s + plane;
-      Mat<T> u0, u1, u2, bb, cc;
-      Alg<T> al, o;
-      load_link_r<R>(in.U, S, 0, s, u0);
-      load_link_r<R>(in.U, S, 1, s, u1);
-      load_link_r<R>(in.U, S, 2, s, u2);
-      // the three plaquettes, then the rotations in pairs by the same link (as plaquette_site)
-      Alg<T> al01, al12, o2;
-      // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
-      load_link_r<R>(in.U, S, 1, sxp, bb);
-      load_link_r<R>(in.U, S, 0, syp, cc);
-      plaquette_alg(u0, bb, cc, u1, al01);
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        F0.a[k] = w01p * al01.a[k];
-        F1.a[k] = -w01q * al01.a[k];
-      }
-      // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
-      load_link_r<R>(in.U, S, 2, sxp, bb);
-      load_link_r<R>(in.U, S, 0, szp, cc);
-      plaquette_alg(u0, bb, cc, u2, al);
-      // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
-      load_link_r<R>(in.U, S, 2, syp, bb);
-      load_link_r<R>(in.U, S, 1, szp, cc);
-      plaquette_alg(u1, bb, cc, u2, al12);
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        F0.a[k] += w02p * al.a[k];
-        F2.a[k] = -w02q * al.a[k];
-        F1.a[k] += w12p * al12.a[k];
-        F2.a[k] -= w12q * al12.a[k];
-      }
-      if (below_top) {  // to links 0 and 1 at y+z: the next slice of this thread
-        inv_adj_mul2(u2, al, al12, zn0, zn1);
-        scale_alg(-w02p, zn0);
-        scale_alg(-w12p, zn1);
-      }
-      if (put_y) {  // to links 0 and 2 at y+y
-        inv_adj_mul2(u1, al01, al12, o, o2);
-        scale_alg(-w01p, o);
-        scale_alg(w12q, o2);
-        march_put(csm, kM01q, tid + kMarchTX, o);
-        march_put(csm, kM12p, tid + kMarchTX, o2);
-      }
-      if (put_x) {  // to links 1 and 2 at y+x
-        inv_adj_mul2(u0, al01, al, o, o2);
-        scale_alg(w01q, o);
-        scale_alg(w02q, o2);
-        march_put(csm, kM01p, tid + 1, o);
-        march_put(csm, kM02p, tid + 1, o2);
-      }
-      if constexpr (kZsm) {
-        if (below_top) zput(z, zn0, zn1);
+    const I s = own ? (I)site_index(g, x, y, z) : (I)0;
+    // ---- A: the plaquettes: this site's (planes (0,1), (0,2), (1,2); (0,2), (1,2) below the chunk)
+    // and this thread's halo plaquette, into the thread's slots
+    {
+      const int p0 = warm ? 1 : 0;
+      const int nown = own ? 3 - p0 : 0;
+      const int ntask = nown + ((!warm && hplane >= 0) ? 1 : 0);
+#pragma unroll 1
+      for (int t = 0; t < ntask; t++) {
+        const bool mine = t < nown;
+        const int xx = mine ? x : hx, yy = mine ? y : hy, pln = mine ? p0 + t : hplane;
+        const int p = pln == 2 ? 1 : 0, q = pln == 0 ? 1 : 2;
+        const I so = (I)site_index(g, xx, yy, z);
+        const I sp = nb<I>(g, xx, yy, z, p == 0 ? 1 : 0, p == 1 ? 1 : 0, 0);
+        const I sq = q == 2 ? so + plane : nb<I>(g, xx, yy, z, 0, 1, 0);
+        Alg<T> al;
+        march_plaquette<T, I, R>(in.U, S, p, q, so, sp, sq, al);
+        put(asm_, mine ? pln : 3, tid, al);
       }
     }
-    // ---- B: the plaquettes owned just outside the tile whose rotated terms reach its first column / row
-    if (htask >= 0) {
-      const I hs = (I)site_index(g, hx, hy, z);
-      const I hxp = nb<I>(g, hx, hy, z, 1, 0, 0), hyp = nb<I>(g, hx, hy, z, 0, 1, 0), hzp = hs + plane;
-      Mat<T> a, bb, cc, d;
-      Alg<T> al, o;
-      if (htask <= 1) {  // plane (0,1): a = U_0(y), b = U_1(y+x), c = U_0(y+y), d = U_1(y)
-        load_link_r<R>(in.U, S, 0, hs, a);
-        load_link_r<R>(in.U, S, 1, hxp, bb);
-        load_link_r<R>(in.U, S, 0, hyp, cc);
-        load_link_r<R>(in.U, S, 1, hs, d);
-        plaquette_alg(a, bb, cc, d, al);
-        if (htask == 0) {  // to link 0 at y+y
-          inv_adj_mul(d, al, o);
-          scale_alg(-w01p, o);
-          march_put(csm, kM01q, hc, o);
-        } else {  // to link 1 at y+x
-          inv_adj_mul(a, al, o);
-          scale_alg(w01q, o);
-          march_put(csm, kM01p, hc, o);
+    // ---- the rotated terms, in pairs by one link: U_2 (planes (0,2), (1,2): to links 0 and 1 one slice
+    // up), U_1 ((0,1), (1,2): to links 0 and 2 at y+y), U_0 ((0,1), (0,2): to links 1 and 2 at y+x), and
+    // the halo plaquette's single term
+    {
+      const unsigned mask = (own && below_top ? 1u : 0u) | (own && !warm && put_y ? 2u : 0u) |
+                            (own && !warm && put_x ? 4u : 0u) | (!warm && hplane >= 0 ? 8u : 0u);
+#pragma unroll 1
+      for (int r = 0; r < 4; r++) {
+        if (!(mask & (1u << r))) continue;
+        int dir, s1, s2 = -1;
+        I vs = s;
+        T c1, c2 = T(0);
+        if (r == 0) {
+          dir = 2, s1 = 1, s2 = 2, c1 = -w02p, c2 = -w12p;
+        } else if (r == 1) {
+          dir = 1, s1 = 0, s2 = 2, c1 = -w01p, c2 = w12q;
+        } else if (r == 2) {
+          dir = 0, s1 = 0, s2 = 1, c1 = w01q, c2 = w02q;
+        } else {
+          dir = hrot, s1 = 3, c1 = hw;
+          vs = (I)site_index(g, hx, hy, z);
         }
-      } else if (htask == 2) {  // plane (1,2): a = U_1(y), b = U_2(y+y), c = U_1(y+z), d = U_2(y)
-        load_link_r<R>(in.U, S, 1, hs, a);
-        load_link_r<R>(in.U, S, 2, hyp, bb);
-        load_link_r<R>(in.U, S, 1, hzp, cc);
-        load_link_r<R>(in.U, S, 2, hs, d);
-        plaquette_alg(a, bb, cc, d, al);
-        inv_adj_mul(a, al, o);  // to link 2 at y+y
-        scale_alg(w12q, o);
-        march_put(csm, kM12p, hc, o);
-      } else {  // plane (0,2): a = U_0(y), b = U_2(y+x), c = U_0(y+z), d = U_2(y)
-        load_link_r<R>(in.U, S, 0, hs, a);
-        load_link_r<R>(in.U, S, 2, hxp, bb);
-        load_link_r<R>(in.U, S, 0, hzp, cc);
-        load_link_r<R>(in.U, S, 2, hs, d);
-        plaquette_alg(a, bb, cc, d, al);
-        inv_adj_mul(a, al, o);  // to link 2 at y+x
-        scale_alg(w02q, o);
-        march_put(csm, kM02p, hc, o);
+        Mat<T> V;
+        Alg<T> e1, e2, o1, o2;
+        load_link_r<R>(in.U, S, dir, vs, V);
+        get(asm_, s1, tid, e1);
+        if (s2 >= 0) {
+          get(asm_, s2, tid, e2);
+        } else {
+#pragma unroll
+          for (int a = 0; a < 8; a++) e2.a[a] = T(0);
+        }
+        inv_adj_mul2(V, e1, e2, o1, o2);
+        scale_alg(c1, o1);
+        scale_alg(c2, o2);
+        if (r == 0) {
+#pragma unroll
+          for (int a = 0; a < 8; a++) {
+            zsm[((z & 1) * 16 + a) * kMarchThreads + tid] = o1.a[a];
+            zsm[((z & 1) * 16 + 8 + a) * kMarchThreads + tid] = o2.a[a];
+          }
+        } else if (r == 1) {
+          put(csm, kM01q, tid + kMarchTX, o1);
+          put(csm, kM12p, tid + kMarchTX, o2);
+        } else if (r == 2) {
+          put(csm, kM01p, tid + 1, o1);
+          put(csm, kM02p, tid + 1, o2);
+        } else {
+          put(csm, hslot, hc, o1);
+        }
       }
+    }
+    // the static currents of t+dt one slice up (its ghost copy at the top slice), from U_z(z) of t
+    Alg<T> sp1, sm1;
+    if (own) {
+      if (below_top) {
+        Mat<T> uz;
+        load_link_r<R>(in.U, S, 2, s, uz);
+        march_jstat(in, S, plane, s + plane, uz, pe.cj, sp1, sm1);
+      } else {
+        sp1 = stp;
+        sm1 = stm;
+      }
+    }
+    if (warm) {
+      stp = sp1;
+      stm = sm1;
+      continue;
     }
     __syncthreads();
     // ---- C: E, the links and the currents of this site
@@ -307,111 +285,80 @@ __global__ void __launch_bounds__(kMarchThreads, MarchOccupancy<T>::kMinBlocks)
       }
 #pragma unroll 1
       for (int mu = 0; mu < 3; mu++) {
-        Alg<T> e, a1, a2;
+        // E_mu + the direct terms (as plaquette_site sums them) + the two rotated terms (as links_site
+        // adds them)
+        Alg<T> e, a1, a2, alA, alB;
         load_alg(in.E, S, mu * 8, s, e);
-        if (mu == 0) {
-#pragma unroll
-          for (int k = 0; k < 8; k++) e.a[k] += F0.a[k];
-          march_get(csm, kM01q, tid, a1);
-          if constexpr (kZsm) {
-            Alg<T> unused;
-            zget(z - 1, a2, unused);
-          } else {
-            a2 = zc0;
-          }
-        } else if (mu == 1) {
-#pragma unroll
-          for (int k = 0; k < 8; k++) e.a[k] += F1.a[k];
-          march_get(csm, kM01p, tid, a1);
-          if constexpr (kZsm) {
-            Alg<T> unused;
-            zget(z - 1, unused, a2);
-          } else {
-            a2 = zc1;
-          }
-        } else {
+        const int sa = mu == 2 ? 1 : 0, sb = mu == 0 ? 1 : 2;  // the two plaquettes that contain link mu here
+        const T wa = mu == 0 ? w01p : (mu == 1 ? -w01q : -w02q);
+        const T wb = mu == 0 ? w02p : (mu == 1 ? w12p : -w12q);
+        get(asm_, sa, tid, alA);
+        get(asm_, sb, tid, alB);
+        if (mu == 2) {
           Alg<T> jp, jm;
           load_alg(in.Jp, S, 0, s, jp);
           load_alg(in.Jm, S, 0, s, jm);
 #pragma unroll
-          for (int k = 0; k < 8; k++) e.a[k] += F2.a[k] + pe.jz * (jp.a[k] - jm.a[k]);
-          march_get(csm, kM02p, tid, a1);
-          march_get(csm, kM12p, tid, a2);
+          for (int k = 0; k < 8; k++) {
+            T f = wa * alA.a[k];
+            f -= w12q * alB.a[k];
+            e.a[k] += f + pe.jz * (jp.a[k] - jm.a[k]);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            T f = wa * alA.a[k];
+            f += wb * alB.a[k];
+            e.a[k] += f;
+          }
+        }
+        if (mu == 2) {
+          get(csm, kM02p, tid, a1);
+          get(csm, kM12p, tid, a2);
+        } else {
+          get(csm, mu == 0 ? kM01q : kM01p, tid, a1);
+#pragma unroll
+          for (int a = 0; a < 8; a++) a2.a[a] = zsm[(((z - 1) & 1) * 16 + (mu == 0 ? 0 : 8) + a) * kMarchThreads + tid];
         }
 #pragma unroll
         for (int k = 0; k < 8; k++) e.a[k] += a1.a[k] + a2.a[k];
         store_alg(in.E, S, mu * 8, s, e);
         if (sg >= 0) store_alg(in.E, S, mu * 8, sg, e);
-        Mat<T> X, u, uh;
+        // the links: one exponential at twice the angle where U(t+dt/2) has no use, else two half steps
+        // with SaveOldLink and UpdateJ between them
+        const bool doubled = pl.do_second && !pl.save_uold && !(mu == 2 && pl.do_j);
+        Mat<T> X, u, w;
         load_link_r<R>(in.U, S, mu, s, u);
-        if (mu == 2) {
-          // static currents of t+dt one slice up, from U_z(z) of t (its ghost copy at the top slice);
-          // carried to the next slice as its own
-          Alg<T> sp1, sm1;
-          if (hi) {
-            sp1 = stp;
-            sm1 = stm;
-          } else {
-            march_jstat(in, S, plane, s + plane, u, pe.cj, sp1, sm1);
-          }
-          if (pl.do_j) {
-            // UpdateJ needs U_z at t+dt/2 (formed below); keep both static currents until then
-            link_exp(pick3(pl.cU, mu), e, X);
-            link_apply(X, u, uh);
+        link_exp(doubled ? T(2) * pick3(pl.cU, mu) : pick3(pl.cU, mu), e, X);
+        const int napply = (doubled || !pl.do_second) ? 1 : 2;
+#pragma unroll 1
+        for (int ap = 0; ap < napply; ap++) {
+          link_apply(X, u, w);
+          u = w;
+          if (ap == 0 && !doubled) {
             if (pl.save_uold) {
-              store_link(in.UOld, S, mu, s, uh);
-              if (sg >= 0) store_link(in.UOld, S, mu, sg, uh);
+              store_link(in.UOld, S, mu, s, u);
+              if (sg >= 0) store_link(in.UOld, S, mu, sg, u);
             }
-            Alg<T> up, um, j;
-            rotate_currents<T, true>(uh, sp1, sm1, up, um);
-            load_alg(in.Jp, S, 0, s, j);
-            axpy_diff(j, -pl.cj, up, stp);
-            store_alg(out.Jp, S, 0, s, j);
-            if (sg >= 0) store_alg(out.Jp, S, 0, sg, j);
-            up = um;
-            load_alg(in.Jm, S, 0, s, j);
-            axpy_diff(j, pl.cj, up, stm);
-            store_alg(out.Jm, S, 0, s, j);
-            if (sg >= 0) store_alg(out.Jm, S, 0, sg, j);
-            stp = sp1;
-            stm = sm1;
-            if (pl.do_second) {
-              link_apply(X, uh, u);
-            } else {
-              u = uh;
+            if (mu == 2 && pl.do_j) {
+              Alg<T> up, um, j;
+              rotate_currents<T, true>(u, sp1, sm1, up, um);
+              load_alg(in.Jp, S, 0, s, j);
+              axpy_diff(j, -pl.cj, up, stp);
+              store_alg(out.Jp, S, 0, s, j);
+              if (sg >= 0) store_alg(out.Jp, S, 0, sg, j);
+              load_alg(in.Jm, S, 0, s, j);
+              axpy_diff(j, pl.cj, um, stm);
+              store_alg(out.Jm, S, 0, s, j);
+              if (sg >= 0) store_alg(out.Jm, S, 0, sg, j);
             }
-            store_link_r<R>(out.U, S, mu, s, u);
-            if (sg >= 0) store_link_r<R>(out.U, S, mu, sg, u);
-            continue;
           }
-          stp = sp1;
-          stm = sm1;
-        }
-        if (pl.do_second && !pl.save_uold && !(mu == 2 && pl.do_j)) {
-          link_exp(T(2) * pick3(pl.cU, mu), e, X);
-          link_apply(X, u, uh);
-          store_link_r<R>(out.U, S, mu, s, uh);
-          if (sg >= 0) store_link_r<R>(out.U, S, mu, sg, uh);
-          continue;
-        }
-        link_exp(pick3(pl.cU, mu), e, X);
-        link_apply(X, u, uh);
-        if (pl.save_uold) {
-          store_link(in.UOld, S, mu, s, uh);
-          if (sg >= 0) store_link(in.UOld, S, mu, sg, uh);
-        }
-        if (pl.do_second) {
-          link_apply(X, uh, u);
-        } else {
-          u = uh;
         }
         store_link_r<R>(out.U, S, mu, s, u);
         if (sg >= 0) store_link_r<R>(out.U, S, mu, sg, u);
       }
-    }
-    if constexpr (!kZsm) {
-      zc0 = zn0;
-      zc1 = zn1;
+      stp = sp1;
+      stm = sm1;
     }
     __syncthreads();
   }
