@@ -629,8 +629,11 @@ int ilog2(int n) {
 // the radix-2 kernel reads exp(-2 pi i k/n) for k < n/2, the mixed-radix kernel for k < n
 int twiddle_count(int n) { return (is_pow2(n) && !GLASMA_FFT_POW2_STOCKHAM) ? (n / 2 > 0 ? n / 2 : 1) : n; }
 
-int tile_lines_for(int n, long long st, long long nlines_total) {
-  int cap = kFftMaxTile / n;
+// Lines per block: up to kFftMaxTile complex values staged (half that for the mixed-radix kernel, which
+// keeps two buffers: at 2 x 64 KB a block of the z pass left one block per SM and the FP64 pipe 55 %
+// busy, ncu), at most 16, a power of two dividing the batch.
+int tile_lines_for(int n, long long st, long long nlines_total, int max_tile = kFftMaxTile) {
+  int cap = max_tile / n;
   if (cap < 1) cap = 1;
   if (cap > 16) cap = 16;
   if (st == 1) {
@@ -646,7 +649,8 @@ int tile_lines_for(int n, long long st, long long nlines_total) {
 template <typename C>
 cudaError_t fft_lines_t(C* X, int n, long long st, long long total, int inverse, const C* tw, cudaStream_t stream) {
   const long long nlines = total / n;
-  const int tl = tile_lines_for(n, st, nlines);
+  const bool mixed = !(is_pow2(n) && !GLASMA_FFT_POW2_STOCKHAM);
+  const int tl = tile_lines_for(n, st, nlines, mixed ? kFftMaxTile / 2 : kFftMaxTile);
   const long long tiles = nlines / tl;
   if (n == 1) return cudaSuccess;
   if (is_pow2(n) && !GLASMA_FFT_POW2_STOCKHAM) {
