@@ -434,7 +434,46 @@ __device__ __forceinline__ void expi_impl(T c, const Alg<T>& al, Mat<T>& X) {
   c0 += T(2) * (Q2.e[7].re * Q.e[5].re - Q2.e[7].im * Q.e[5].im);  // (1,2)*(2,1) + (2,1)*(1,2)
   c0 *= T(1) / T(3);
   cx<T> f0, f1, f2;
-  if (c1 < Trig<T>::taylor_c1()) {
+  if (sizeof(T) == 8 && !kMinusOne && c1 >= Trig<T>::taylor_c1() && c1 < T(0.5)) {
+    // FP64 without transcendental functions (they cost ~60 % of this exponential on GB300's FP64 pipe):
+    // exp(iQ) = sum_n i^n Q^n / n!, and by Cayley-Hamilton (Q^3 = c1 Q + c0) Q^n / n! = a_n + b_n Q + d_n
+    // Q^2 with a_{n+1} = c0 d_n / (n+1), b_{n+1} = (a_n + c1 d_n) / (n+1), d_{n+1} = b_n / (n+1).  The
+    // eigenvalues of Q are at most sqrt(4 c1 / 3) in size, so the first omitted term is below
+    // 0.82^18 / 18! ~ 4e-18 with 17 terms for c1 < 0.5, and below 0.17^13 / 13! ~ 1e-19 with 12 for
+    // c1 < 0.02; beyond c1 = 0.5 the closed form below.
+    const int nterms = c1 < T(0.02) ? 12 : 17;
+    T a = T(1), b = T(0), d = T(0);
+    T f0r = T(1), f0i = T(0), f1r = T(0), f1i = T(0), f2r = T(0), f2i = T(0);
+#pragma unroll
+    for (int n = 1; n <= 17; n++) {
+      if (n > nterms) break;
+      const T inv = T(1) / T(n);
+      const T an = c0 * d * inv, bn = fma(c1, d, a) * inv, dn = b * inv;
+      a = an;
+      b = bn;
+      d = dn;
+      if ((n & 3) == 1) {  // i^n = i
+        f0i += a;
+        f1i += b;
+        f2i += d;
+      } else if ((n & 3) == 2) {  // -1
+        f0r -= a;
+        f1r -= b;
+        f2r -= d;
+      } else if ((n & 3) == 3) {  // -i
+        f0i -= a;
+        f1i -= b;
+        f2i -= d;
+      } else {  // +1
+        f0r += a;
+        f1r += b;
+        f2r += d;
+      }
+    }
+    f0 = mk<T>(f0r, f0i);
+    f1 = mk<T>(f1r, f1i);
+    f2 = mk<T>(f2r, f2i);
+  } else if (c1 < Trig<T>::taylor_c1()) {
     f0 = mk<T>(kMinusOne ? -(c0 * c0 / T(720)) : T(1) - c0 * c0 / T(720), -c0 / T(6) + c1 * c0 / T(120));
     f1 = mk<T>(c0 / T(24) - c0 * c1 / T(360), T(1) - c1 / T(6) + c1 * c1 / T(120));
     f2 = mk<T>(T(-0.5) + c1 / T(24) - c1 * c1 / T(720), c0 / T(120));

@@ -384,3 +384,20 @@ def test_upload_begin_finish(precision):
             pipe.setdefault("bulk", []).append(b.bulk()[9])
             b.upload_finish()
     assert seq["bulk"] == pipe["bulk"]
+
+
+@pytest.mark.parametrize("scale", [1e-4, 0.05, 0.4, 1.5, 6.0])
+def test_link_exponential_across_its_tiers(oracle, scale):
+    """UpdateGaugeLinks alone with E scaled so that the FP64 exponential runs each of its forms (the
+    Taylor polynomial for tiny arguments, the 12- and 17-term Cayley-Hamilton series below c1 = 0.5, the
+    closed form above): links against the oracle's exponential at 1e-14."""
+    N, a, dt = (6, 4, 8), (1.0, 1.0, 1.0), 1.0
+    f = O.random_fields(N, 41)
+    f["E"] = f["E"] * scale
+    ref = O.copy_fields(f)
+    oracle.lib.oracle_update_links(O._ivec(N), O._dvec(a), dt, O._ptr(ref["U"]), O._ptr(ref["E"]))
+    with _gpu(f, N, a) as lat:
+        lat.update_links(dt)
+        U = lat.download("U")
+    sl = slice(1, -1)  # interior slices (the sub-step leaves ghost syncs to the caller)
+    assert np.max(np.abs(U[sl] - ref["U"][sl])) < 1e-14 * max(1.0, scale)
