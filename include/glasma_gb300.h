@@ -242,6 +242,12 @@ int glasma_coulomb_fix_algorithm(glasma_lattice* h, int algorithm, double param,
                                  double tol, unsigned flags, double* log, int* iterations);
 /* GaugeTransformation::SetIdentity (S/GAUGETRANSFORMATION/GaugeTransformation.cpp:41-60). */
 int glasma_gauge_reset(glasma_lattice* h);
+/* The handle's gauge transformation G applied to one colour-charge field, PERFORM_COLOR_CHARGE_TRANSFORMATION
+ * (S/CALC/GaugeTransformation.cpp:28-31; the colour-current form :20-25 is the same action per component):
+ * jG(x) = AdjointMultiplication(G(x), j(x)) = 2 tr(t^a G (t.j) G^dagger) for field GLASMA_FIELD_JP ..
+ * GLASMA_FIELD_JMSTAT, written to out (host or device memory, S x 8 doubles in the field's host layout;
+ * the ghost slices take the edge slices' values).  The handle's fields are not changed. */
+int glasma_transform_charge(glasma_lattice* h, int field, double* out);
 
 /* McLerran-Venugopalan initial state, as Simulation::Run builds it (S/Simulation.cpp:337-374:
  * CollidingObjects::SetWilsonLines for each nucleus, then SingleSheet over z in [0,(Nz-2)/2] for
@@ -400,6 +406,12 @@ int glasma_batch_step(glasma_batch* b, double dt, int nsteps, int use_graph);
 #define GLASMA_BATCH_PERSISTENT 0
 #define GLASMA_BATCH_TILE_GRID 1
 int glasma_batch_set_launch(glasma_batch* b, int mode);
+/* Step method of every event of the batch: GLASMA_STEP_TWO_PASS (the staple kernels, the default) or
+ * GLASMA_STEP_PLAQUETTE (each event's force summed plaquette by plaquette into its contribution
+ * buffer, 48 reals per site, allocated on first use); other methods give GLASMA_ERR_UNSUPPORTED.
+ * Either is bit-identical to stepping each event alone with the same method. */
+int glasma_batch_set_step_method(glasma_batch* b, int method);
+int glasma_batch_get_step_method(glasma_batch* b, int* method);
 /* 12-real links for every event of an FP32 batch (see glasma_set_link_storage): the batched step
  * kernels read and write rows 0 and 1 of each link; row 2 is written back at the end of every
  * glasma_batch_step call. */

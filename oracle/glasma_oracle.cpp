@@ -509,6 +509,23 @@ void gauge_transform_efield(const Lat& l, const double* E, double* EG, cplx* G) 
   sync_G(G, l);
 }
 
+// PERFORM_COLOR_CHARGE_TRANSFORMATION (S/CALC/GaugeTransformation.cpp:28-31; the current form :20-25
+// applies the same action to each spatial component): jG(x) = AdjointMultiplication(G(x), j(x)) on
+// the interior slices, the ghost slices copied from the edge slices as SynchronizeGhostCells does.
+void gauge_transform_charge(const Lat& l, const cplx* G, const double* J, double* JG) {
+  const int Nx = l.N[0], Ny = l.N[1], Nz = l.N[2];
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < Nz; z++)
+    for (int y = 0; y < Ny; y++)
+      for (int x = 0; x < Nx; x++) adj_mul(G + 9 * l.s(x, y, z), JF(J, l, x, y, z), JF(JG, l, x, y, z));
+  for (int y = 0; y < Ny; y++)
+    for (int x = 0; x < Nx; x++)
+      for (int a = 0; a < 8; a++) {
+        JF(JG, l, x, y, -1)[a] = JF(JG, l, x, y, 0)[a];
+        JF(JG, l, x, y, Nz)[a] = JF(JG, l, x, y, Nz - 1)[a];
+      }
+}
+
 // ------------------------------------------------------------- Coulomb gauge deviation at one site
 // GET_LOCAL_GAUGE_VIOLATION (S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41):
 // w(x) = sum_mu c_mu (UG_mu(x) + UG_mu^dagger(x - mu)), the z term only if Nz > 1; Delta^a = ReTr(i t^a w).
@@ -607,6 +624,11 @@ int oracle_get_threads() { return omp_get_max_threads(); }
 void oracle_expi(double c, const double* alpha, double* out18) { expi(c, alpha, reinterpret_cast<cplx*>(out18)); }
 void oracle_adj_mul(const double* V18, const double* e, double* out) { adj_mul(reinterpret_cast<const cplx*>(V18), e, out); }
 void oracle_inv_adj_mul(const double* V18, const double* e, double* out) { inv_adj_mul(reinterpret_cast<const cplx*>(V18), e, out); }
+
+void oracle_transform_charge(const int* N, const double* Gin, const double* J, double* JG) {
+  Lat l = make_lat(N, kUnitSpacing, 1);
+  gauge_transform_charge(l, reinterpret_cast<const cplx*>(Gin), J, JG);
+}
 
 void oracle_sync_links(const int* N, double* U) {
   Lat l = make_lat(N, kUnitSpacing, 1);

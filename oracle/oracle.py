@@ -190,6 +190,7 @@ class Oracle:
         L.oracle_expi.argtypes = [ctypes.c_double, _dp, _dp]
         L.oracle_adj_mul.argtypes = [_dp, _dp, _dp]
         L.oracle_inv_adj_mul.argtypes = [_dp, _dp, _dp]
+        L.oracle_transform_charge.argtypes = [_ip, _dp, _dp, _dp]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_get_threads.restype = ctypes.c_int
         if threads:
@@ -208,6 +209,13 @@ class Oracle:
         uold = _ptr(f["UOld"]) if save_uold else None
         self.lib.oracle_update(_ivec(N), _dvec(a), dt, nsteps, _ptr(f["U"]), uold, _ptr(f["E"]), _ptr(f["Jp"]),
                                _ptr(f["Jm"]), _ptr(f["JpStat"]), _ptr(f["JmStat"]))
+
+    def transform_charge(self, G, J, N):
+        """jG(x) = G(x) j(x) G(x)^dagger on the interior, ghost slices copied from the edges."""
+        out = np.zeros_like(J)
+        self.lib.oracle_transform_charge(_ivec(N), _ptr(np.ascontiguousarray(G)), _ptr(np.ascontiguousarray(J)),
+                                         _ptr(out))
+        return out
 
     def bulk(self, f, N, a, a_scale=1.0):
         out = np.zeros(16)

@@ -74,6 +74,7 @@ SIGNATURES = [
     ("glasma_coulomb_fix_algorithm", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong,
                                                     ctypes.c_int, ctypes.c_double, ctypes.c_uint, _D, _I]),
     ("glasma_gauge_reset", ctypes.c_int, [_H]),
+    ("glasma_transform_charge", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p]),
     ("glasma_mv_init", ctypes.c_int, [_H, ctypes.c_int, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("glasma_mv_last_error", ctypes.c_char_p, []),
@@ -107,6 +108,8 @@ SIGNATURES = [
     ("glasma_batch_autotune", ctypes.c_int, [_H, ctypes.c_double, _I]),
     ("glasma_batch_step", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int]),
     ("glasma_batch_set_launch", ctypes.c_int, [_H, ctypes.c_int]),
+    ("glasma_batch_set_step_method", ctypes.c_int, [_H, ctypes.c_int]),
+    ("glasma_batch_get_step_method", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_int)]),
     ("glasma_batch_set_link_storage", ctypes.c_int, [_H, ctypes.c_int]),
     ("glasma_batch_energy", ctypes.c_int, [_H, _D]),
     ("glasma_batch_synchronize", ctypes.c_int, [_H]),

@@ -57,6 +57,18 @@ class Batch:
         tile list); both cover all events in one launch per kernel and give the same fields."""
         _bcheck(self.lib, self.lib.glasma_batch_set_launch(self.b, {"persistent": 0, "tile_grid": 1}[mode]))
 
+    def set_step_method(self, method):
+        """"plaquette" (default: each event's force summed plaquette by plaquette into a
+        48-real-per-site contribution buffer; two-pass when those cannot be allocated) or "two_pass"
+        (the staple kernels); either gives each event the fields it would reach stepped alone with that
+        method."""
+        _bcheck(self.lib, self.lib.glasma_batch_set_step_method(self.b, Lattice.STEP_METHODS[method]))
+
+    def step_method(self):
+        m = ctypes.c_int()
+        _bcheck(self.lib, self.lib.glasma_batch_get_step_method(self.b, ctypes.byref(m)))
+        return {v: k for k, v in Lattice.STEP_METHODS.items()}[m.value]
+
     def set_link_reals(self, reals):
         """18 (default) or 12 reals per link in the batched step (FP32 batches; rows 0 and 1 of each
         link stored, row 2 formed as conj(row0 x row1)); every event follows the setting."""

@@ -2,9 +2,12 @@
 //
 // Each event is an ordinary lattice handle (its own fields, ghost slices, tile shape).  A step of
 // the whole batch is two launches per group of up to kTableEvents events (one group for the
-// 64-event workload): the electric-field/JStat kernel walks the list of the group's K1 tiles, the
-// link/J kernel the list of its 128-site chunks (one block per tile, or a persistent grid that
-// strides through the list); a block finds its event in a tile -> event table.  The group's event
+// 64-event workload).  With the staple kernels (two-pass method) the electric-field/JStat kernel
+// walks the list of the group's K1 tiles, the link/J kernel the list of its 128-site chunks; with
+// the plaquette method the force kernel walks 128-site chunks of every event's plaquette owners
+// (slices -1 .. Nz-1) and writes the event's contribution buffer, and the gathering link kernel
+// walks the 128-site chunks of the sites.  One block takes one tile or chunk, or a persistent grid
+// strides through the list; a block finds its event in a tile -> event table.  The group's event
 // descriptors are a __grid_constant__ kernel parameter, read in place from the constant bank.  The
 // per-site arithmetic is the
 // single-lattice kernels' (leapfrog_sites.cuh), so a batched step is bit-identical to stepping
@@ -34,7 +37,8 @@ struct EventDesc {
   EParams<T> ep;
   LParams<T> lp;
   TileMap tm;
-  long long k1_begin;  // first K1 tile of this event in the batch's tile list
+  T* C;                // plaquette method: the event's contribution buffer (48 S reals)
+  long long k1_begin;  // first K1 tile (plaquette method: owner chunk) of this event in the batch's list
   long long k2_begin;  // first 128-site chunk of this event
 };
 
@@ -50,6 +54,7 @@ struct EventTable {
   long long t0;    // the group's tiles (K1) or chunks (K2) are [t0, t1) of the batch's list
   long long t1;
 };
+static_assert(sizeof(EventTable<double>) <= 32764, "event table exceeds the kernel-parameter limit");
 
 // R: rows of each link read and written (3 full, 2 for 12-real links).  kStride: the persistent grid
 // strides through the tile list; without it each block takes one tile (the tile grid), and the
@@ -79,6 +84,30 @@ __global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
   }
 }
 
+// The plaquette method over the batch: the single-lattice kernels' site functions on every event's
+// owner chunks (force) and site chunks (gather + link update).
+template <typename T, typename I, int R, bool kStride>
+__global__ void __launch_bounds__(kThreads, PlaqOccupancy<T, T>::kMinBlocks)
+    plaquette_batch_kernel(const __grid_constant__ EventTable<T> tab, const unsigned short* __restrict__ tile_ev) {
+  for (long long t = tab.t0 + blockIdx.x; t < tab.t1; t += gridDim.x) {
+    const EventDesc<T>& d = tab.ev[tile_ev[t] - tab.ev0];
+    const long long idx = (t - d.k1_begin) * kThreads + threadIdx.x;
+    if (idx < d.g.plane * (d.g.nz + 1)) plaquette_site<T, I, R, T>(d.g, d.f, d.C, d.ep, (I)idx);
+    if (!kStride) break;
+  }
+}
+
+template <typename T, typename I, int R, bool kStride>
+__global__ void __launch_bounds__(kThreads, Occupancy<T>::kLinksMinBlocks)
+    links_gather_batch_kernel(const __grid_constant__ EventTable<T> tab, const unsigned short* __restrict__ tile_ev) {
+  for (long long t = tab.t0 + blockIdx.x; t < tab.t1; t += gridDim.x) {
+    const EventDesc<T>& d = tab.ev[tile_ev[t] - tab.ev0];
+    const long long idx = (t - d.k2_begin) * kThreads + threadIdx.x;
+    if (idx < d.g.vol) links_site<T, I, R, true>(d.g, d.f, d.lp, (I)idx, d.C);
+    if (!kStride) break;
+  }
+}
+
 }  // namespace
 }  // namespace glasma
 
@@ -100,6 +129,8 @@ struct glasma_batch {
   bool strided = false;  // some group's grid is smaller than its tile list (strided kernels needed)
   int launch_mode = GLASMA_BATCH_TILE_GRID;
   int link_rows = 3;  // 2: 12-real links (FP32), as glasma_set_link_storage
+  int method = GLASMA_STEP_PLAQUETTE;  // or GLASMA_STEP_TWO_PASS (glasma_batch_set_step_method)
+  int method_used = GLASMA_STEP_PLAQUETTE;  // two-pass when the contribution buffers could not be allocated
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   double graph_dt = NAN;
@@ -144,6 +175,17 @@ std::vector<glasma::EventTable<double>>& tables2<double>(glasma_batch* b) { retu
 template <typename T, int R>
 void batch_occupancy(const glasma_batch* b, int& per1, int& per2) {
   using namespace glasma;
+  if (b->method_used == GLASMA_STEP_PLAQUETTE) {
+    if (b->idx32) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, plaquette_batch_kernel<T, int, R, true>, kThreads, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_gather_batch_kernel<T, int, R, true>, kThreads, 0);
+    } else {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, plaquette_batch_kernel<T, long long, R, true>, kThreads, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_gather_batch_kernel<T, long long, R, true>, kThreads,
+                                                    0);
+    }
+    return;
+  }
   if (b->idx32) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, efield_batch_kernel<T, int, R, true>, kThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, links_batch_kernel<T, int, R, true>, kThreads, 0);
@@ -160,11 +202,17 @@ int build_descriptors(glasma_batch* b, double dt) {
   std::vector<EventDesc<T>> d(b->ev.size());
   long long k1 = 0, k2 = 0;
   b->idx32 = true;
+  // the plaquette method needs every event's contribution buffer; without them the batch steps with
+  // the staple kernels (as a single lattice does)
+  bool plaq = b->method == GLASMA_STEP_PLAQUETTE;
+  for (size_t i = 0; plaq && i < b->ev.size(); i++) plaq = ensure_contrib(b->ev[i]);
+  b->method_used = plaq ? GLASMA_STEP_PLAQUETTE : GLASMA_STEP_TWO_PASS;
   for (size_t i = 0; i < b->ev.size(); i++) {
     glasma_lattice* h = b->ev[i];
     EventDesc<T>& e = d[i];
     e.g = h->g;
     e.f = handle_ptrs<T>(h);
+    e.C = plaq ? static_cast<T*>(h->contrib) : nullptr;
     // same constants as the single-lattice launches (leapfrog.cu)
     const double a3 = h->g.a[0] * h->g.a[1] * h->g.a[2];
     const double gamma = -2.0 * dt * a3;
@@ -186,9 +234,11 @@ int build_descriptors(glasma_batch* b, double dt) {
     e.tm = TileMap::make(h->g.nx, h->g.ny, h->tile_x, kThreads);
     e.k1_begin = k1;
     e.k2_begin = k2;
-    k1 += e.tm.tiles(h->g.nz);
+    k1 += plaq ? (h->g.plane * (h->g.nz + 1) + kThreads - 1) / kThreads : e.tm.tiles(h->g.nz);
     k2 += (h->g.vol + kThreads - 1) / kThreads;
     if (!use_32bit_index(h->g)) b->idx32 = false;
+    // the contribution buffer has 48 S entries: 32-bit offsets only while that fits
+    if (plaq && h->g.S * 48 >= (1LL << 31) - 1) b->idx32 = false;
   }
   b->k1_total = k1;
   b->k2_total = k2;
@@ -269,6 +319,13 @@ int build_descriptors(glasma_batch* b, double dt) {
 template <typename T, typename I, int R, bool kStride>
 void launch_batch_group(glasma_batch* b, size_t grp) {
   using namespace glasma;
+  if (b->method_used == GLASMA_STEP_PLAQUETTE) {
+    plaquette_batch_kernel<T, I, R, kStride><<<b->grid1[grp], kThreads, 0, b->stream>>>(tables1<T>(b)[grp],
+                                                                                        b->d_tile_ev);
+    links_gather_batch_kernel<T, I, R, kStride><<<b->grid2[grp], kThreads, 0, b->stream>>>(
+        tables2<T>(b)[grp], b->d_tile_ev + b->k1_total);
+    return;
+  }
   efield_batch_kernel<T, I, R, kStride><<<b->grid1[grp], kThreads, 0, b->stream>>>(tables1<T>(b)[grp], b->d_tile_ev);
   links_batch_kernel<T, I, R, kStride><<<b->grid2[grp], kThreads, 0, b->stream>>>(tables2<T>(b)[grp],
                                                                                   b->d_tile_ev + b->k1_total);
@@ -493,6 +550,28 @@ int glasma_batch_set_link_storage(glasma_batch* b, int reals_per_link) {
     }
   }
   for (glasma_lattice* h : b->ev) glasma_set_link_storage(h, reals_per_link);  // events stepped alone
+  return GLASMA_OK;
+}
+
+int glasma_batch_set_step_method(glasma_batch* b, int method) {
+  if (!b) return bfail(GLASMA_ERR_INVALID_ARGUMENT, "null batch");
+  if (method != GLASMA_STEP_TWO_PASS && method != GLASMA_STEP_PLAQUETTE)
+    return bfail(GLASMA_ERR_UNSUPPORTED, "batches step with the two-pass or the plaquette method");
+  if (method != b->method) {
+    b->method = method;
+    b->desc_dt = NAN;  // the force kernel's list and the persistent grids depend on the method
+    if (b->graph) {
+      cudaStreamSynchronize(b->stream);
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
+  return GLASMA_OK;
+}
+
+int glasma_batch_get_step_method(glasma_batch* b, int* method) {
+  if (!b || !method) return bfail(GLASMA_ERR_INVALID_ARGUMENT, "bad arguments");
+  *method = std::isnan(b->desc_dt) ? b->method : b->method_used;
   return GLASMA_OK;
 }
 

@@ -369,6 +369,25 @@ __global__ void __launch_bounds__(128) transform_efield_kernel(Geometry g, const
   }
 }
 
+// ---- jG(x) = G(x) j(x) G^d(x): PERFORM_COLOR_CHARGE_TRANSFORMATION (S/CALC/GaugeTransformation.cpp:28-31),
+// the per-component action of PERFORM_COLOR_CURRENT_TRANSFORMATION (:20-25).  One thread per site of
+// the host layout; a ghost site takes the transformed value of the edge slice it mirrors.
+template <typename T>
+__global__ void __launch_bounds__(128) transform_charge_kernel(Geometry g, const T* J, const cx<T>* G, double* out) {
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.S) return;
+  const long long top = g.plane * (g.nz + 1);
+  const long long si = s < g.plane ? s + g.plane : (s >= top ? s - g.plane : s);
+  Mat<double> gx;
+  ld_d(G, g.S, 0, si, gx);
+  Alg<double> j, o;
+#pragma unroll
+  for (int a = 0; a < 8; a++) j.a[a] = (double)J[(long long)a * g.S + si];
+  adj_mul(gx, j, o);
+#pragma unroll
+  for (int a = 0; a < 8; a++) out[s * 8 + a] = o.a[a];
+}
+
 // ---- FFT
 __global__ void twiddle_kernel(double2* tw, int n, int count) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -982,6 +1001,17 @@ int gaugefix_run_local(const GaugeFixArgs& a, int algorithm, double param, unsig
 }
 
 size_t gaugefix_scratch_doubles() { return (size_t)kGfBlocks * 14 + 16; }
+
+cudaError_t launch_transform_charge(const GaugeFixArgs& a, const void* J, double* out) {
+  const unsigned blocks = (unsigned)((a.g.S + 127) / 128);
+  if (a.precision == GLASMA_FP64)
+    transform_charge_kernel<double><<<blocks, 128, 0, a.stream>>>(a.g, static_cast<const double*>(J),
+                                                                  static_cast<const cx<double>*>(a.G), out);
+  else
+    transform_charge_kernel<float><<<blocks, 128, 0, a.stream>>>(a.g, static_cast<const float*>(J),
+                                                                 static_cast<const cx<float>*>(a.G), out);
+  return cudaGetLastError();
+}
 
 void gaugefix_destroy(GaugeFixState* s) {
   if (!s) return;

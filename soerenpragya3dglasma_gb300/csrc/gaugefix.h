@@ -35,6 +35,10 @@ int gaugefix_run_local(const GaugeFixArgs& a, int algorithm, double param, unsig
 size_t gaugefix_scratch_doubles();
 void gaugefix_destroy(GaugeFixState* state);
 
+// jG(x) = G(x) j(x) G^dagger(x) of one colour-charge field (device SoA j[a][S], precision of the handle)
+// into `out`, FP64 in the host layout [S][8]; the ghost slices take the edge slices' values.
+cudaError_t launch_transform_charge(const GaugeFixArgs& a, const void* J, double* out);
+
 // Batched 1D transforms of length n in place over `total` complex values: element k of line l is
 // at l*n + k (st == 1) or at o*st*n + i + k*st (st > 1, l = (o, i)); unnormalised, sign -1 forward,
 // +1 inverse.  tw = make_twiddles(n) (cudaFree it when done).

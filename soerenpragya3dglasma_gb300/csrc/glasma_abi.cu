@@ -31,6 +31,17 @@ int fail(int status, const std::string& msg) {
 namespace glasma {
 // records msg as glasma_last_error() of the calling thread (for entry points in other files)
 int record_error(int status, const std::string& msg) { return fail(status, msg); }
+
+// The plaquette method's contribution buffer (every slot a step reads is written earlier in it).
+bool ensure_contrib(glasma_lattice* h) {
+  if (h->contrib) return true;
+  if (cudaMalloc(&h->contrib, (size_t)h->g.S * 48 * h->real_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    h->contrib = nullptr;
+    return false;
+  }
+  return true;
+}
 }  // namespace glasma
 
 namespace {
@@ -121,16 +132,7 @@ bool ensure_alt(glasma_lattice* h) {
   return true;
 }
 
-// The plaquette method's contribution buffer (every slot a step reads is written earlier in it).
-bool ensure_contrib(glasma_lattice* h) {
-  if (h->contrib) return true;
-  if (cudaMalloc(&h->contrib, (size_t)h->g.S * 48 * h->real_bytes) != cudaSuccess) {
-    cudaGetLastError();
-    h->contrib = nullptr;
-    return false;
-  }
-  return true;
-}
+using glasma::ensure_contrib;
 
 void swap_buffers(glasma_lattice* h) {
   for (int f : kSwapFields) std::swap(h->f[f], h->alt[f]);
@@ -934,6 +936,27 @@ int glasma_coulomb_fix_algorithm(glasma_lattice* h, int algorithm, double param,
   st = glasma::gaugefix_run_local(a, algorithm, param, seed, max_iters, tol, log, &n, &err);
   if (iterations) *iterations = n;
   if (st != GLASMA_OK) return fail(st, err);
+  return GLASMA_OK;
+}
+
+int glasma_transform_charge(glasma_lattice* h, int field, double* out) {
+  GLASMA_CHECK_HANDLE(h);
+  if (field < GLASMA_FIELD_JP || field > GLASMA_FIELD_JMSTAT)
+    return fail(GLASMA_ERR_INVALID_ARGUMENT, "field must be one of GLASMA_FIELD_JP .. GLASMA_FIELD_JMSTAT");
+  if (!out) return fail(GLASMA_ERR_INVALID_ARGUMENT, "null destination");
+  int st;
+  if ((st = ensure_field(h, GLASMA_FIELD_G))) return st;
+  const size_t bytes = (size_t)h->g.S * 8 * sizeof(double);
+  if ((st = ensure_staging(h, bytes))) return st;
+  glasma::GaugeFixArgs a = {};
+  a.g = h->g;
+  a.precision = h->precision;
+  a.stream = h->stream;
+  a.G = h->f[GLASMA_FIELD_G];
+  cudaError_t e = glasma::launch_transform_charge(a, h->f[field], h->staging);
+  if (e != cudaSuccess) return cuda_fail(e, "transform charge");
+  GLASMA_CUDA(cudaMemcpyAsync(out, h->staging, bytes, cudaMemcpyDefault, h->stream), "transform charge copy");
+  GLASMA_CUDA(cudaStreamSynchronize(h->stream), "transform charge sync");
   return GLASMA_OK;
 }
 

@@ -39,12 +39,15 @@ struct glasma_lattice {
   unsigned pending;          // fields begun and not yet finished (bit per glasma_field)
 };
 
-// The autotuner of the staple kernels whatever the handle's step method (batches step their events
-// with the staple kernels).
+// The autotuner of the staple kernels whatever the handle's step method (batches stepping with the
+// two-pass method use the staple kernels).
 extern "C" int glasma_autotune_staple(glasma_lattice* h, double dt, int* tile_x);
 
 namespace glasma {
 // Default K1 tile width: the widest power of two dividing the block that does not exceed Nx.
+// allocates the plaquette method's contribution buffer of h (false when that fails)
+bool ensure_contrib(glasma_lattice* h);
+
 inline int default_tile_x(int nx) {
   int t = 128;
   while (t > 1 && t > nx) t >>= 1;

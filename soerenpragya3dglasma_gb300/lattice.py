@@ -423,3 +423,13 @@ class Lattice:
 
     def gauge_reset(self):
         check(self.lib.glasma_gauge_reset(self.h))
+
+    def transform_charge(self, name, out=None):
+        """G(x) j(x) G(x)^dagger of the colour-charge field `name` (Jp, Jm, JpStat, JmStat) with the
+        handle's gauge transformation (glasma_transform_charge); the field itself is not changed."""
+        if name not in ("Jp", "Jm", "JpStat", "JmStat"):
+            raise ValueError("transform_charge takes Jp, Jm, JpStat or JmStat")
+        if out is None:
+            out = empty_field(name, self.N)
+        check(self.lib.glasma_transform_charge(self.h, _lib.FIELDS[name], _address(out, self.field_doubles(name))))
+        return out

@@ -1,5 +1,6 @@
-"""Batched multi-event stepping (one launch per kernel over all events, CUDA-graph replay):
-bit-identical to stepping each event alone, and the FP64 batch matches the oracle."""
+"""Batched multi-event stepping (one launch per kernel over all events, CUDA-graph replay), with the
+plaquette and the two-pass method: bit-identical to stepping each event alone with the same method,
+and the FP64 batch matches the oracle."""
 import numpy as np
 import pytest
 
@@ -21,6 +22,7 @@ def test_batch_equals_individual_events(precision):
     fields = [O.random_fields(N, 300 + i) for i, N in enumerate(SHAPES)]
     dt, steps = 0.1, 37  # crosses two 16-step graph blocks plus single steps
     with Batch(SHAPES, precision=precision, reunitarize_every=16) as b:
+        b.set_step_method("two_pass")
         tiles = b.autotune(dt)
         assert len(tiles) == len(SHAPES)
         for ev, f in zip(b.events, fields):
@@ -30,7 +32,7 @@ def test_batch_equals_individual_events(precision):
         energies = b.energy()
     for i, (N, f) in enumerate(zip(SHAPES, fields)):
         with Lattice(N, precision=precision, reunitarize_every=16) as lat:
-            lat.set_step_method("two_pass")  # the batched kernels are the two-pass (staple) kernels
+            lat.set_step_method("two_pass")  # the batch's two-pass method: the staple kernels
             lat.set_tile(tiles[i])
             lat.upload_fields(f)
             lat.step(dt, steps, save_uold=False)
@@ -47,6 +49,7 @@ def test_batch_links12_equals_individual_events(mode):
     fields = [O.random_fields(N, 340 + i) for i, N in enumerate(SHAPES)]
     dt, steps = 0.1, 37
     with Batch(SHAPES, precision="fp32", reunitarize_every=16) as b:
+        b.set_step_method("two_pass")
         b.set_launch(mode)
         b.set_link_reals(12)
         tiles = b.autotune(dt)
@@ -71,6 +74,55 @@ def test_batch_links12_equals_individual_events(mode):
             b.set_link_reals(12)
 
 
+@pytest.mark.parametrize("precision,reals,mode", [("fp64", 18, "tile_grid"), ("fp64", 18, "persistent"),
+                                                   ("fp32", 18, "tile_grid"), ("fp32", 12, "persistent")])
+def test_batch_plaquette_equals_individual_events(precision, reals, mode):
+    """The plaquette method over the batch: each event's fields bit-identical to the event stepped
+    alone with the plaquette method (graph blocks, reunitarisation and single steps crossed)."""
+    fields = [O.random_fields(N, 360 + i) for i, N in enumerate(SHAPES)]
+    dt, steps = 0.1, 37
+    with Batch(SHAPES, precision=precision, reunitarize_every=16) as b:
+        assert b.step_method() == "plaquette"  # the default
+        b.set_step_method("two_pass")
+        assert b.step_method() == "two_pass"
+        b.set_step_method("plaquette")
+        b.set_launch(mode)
+        if reals == 12:
+            b.set_link_reals(12)
+        for ev, f in zip(b.events, fields):
+            ev.upload_fields(f)
+        b.step(dt, steps, use_graph=True)
+        assert b.step_method() == "plaquette"
+        got = [ev.download_fields(("U", "E", "Jp", "Jm", "JpStat", "JmStat")) for ev in b.events]
+        with pytest.raises(Exception):
+            b.set_step_method("one_pass")
+    for i, (N, f) in enumerate(zip(SHAPES, fields)):
+        with Lattice(N, precision=precision, reunitarize_every=16) as lat:
+            lat.set_step_method("plaquette")
+            if reals == 12:
+                lat.link_reals = 12
+            lat.upload_fields(f)
+            lat.step(dt, steps, save_uold=False)
+            ref = lat.download_fields(("U", "E", "Jp", "Jm", "JpStat", "JmStat"))
+        for k in ref:
+            assert np.array_equal(got[i][k], ref[k]), (i, k)
+
+
+def test_batch_plaquette_fp64_matches_oracle(oracle):
+    fields = [O.random_fields(N, 410 + i) for i, N in enumerate(SHAPES)]
+    dt, steps = 0.125, 5
+    with Batch(SHAPES, precision="fp64") as b:
+        for ev, f in zip(b.events, fields):
+            ev.upload_fields(f)
+        b.step(dt, steps, use_graph=False)
+        got = [ev.download_fields() for ev in b.events]
+    for N, f, g in zip(SHAPES, fields, got):
+        ref = O.copy_fields(f)
+        oracle.update(ref, N, (1.0, 1.0, 1.0), dt, steps, save_uold=False)
+        for k in ("U", "E", "Jp", "Jm", "JpStat", "JmStat"):
+            assert np.max(np.abs(g[k] - ref[k])) / np.max(np.abs(ref[k])) < 1e-12, k
+
+
 def test_batch_launch_modes_agree():
     """One block per tile and the persistent grid run the same per-site arithmetic."""
     fields = [O.random_fields(N, 330 + i) for i, N in enumerate(SHAPES)]
@@ -93,6 +145,7 @@ def test_batch_after_events_stepped_alone():
     fields = [O.random_fields(N, 350 + i) for i, N in enumerate(SHAPES)]
     dt = 0.1
     with Batch(SHAPES, precision="fp64") as b:
+        b.set_step_method("two_pass")
         for ev, f in zip(b.events, fields):
             ev.upload_fields(f)
         b.step(dt, 2, use_graph=False)
@@ -118,6 +171,7 @@ def test_batch_fp64_matches_oracle(oracle):
     fields = [O.random_fields(N, 400 + i) for i, N in enumerate(SHAPES)]
     dt, steps = 0.125, 5
     with Batch(SHAPES, precision="fp64") as b:
+        b.set_step_method("two_pass")
         for ev, f in zip(b.events, fields):
             ev.upload_fields(f)
         b.step(dt, steps, use_graph=False)

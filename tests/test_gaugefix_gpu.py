@@ -236,3 +236,37 @@ def test_open_z_converged_fields_match_oracle_16x16x32(oracle, golden_dir):
     assert np.allclose(th[:m][k], oth[:m][k], rtol=1e-6)
     assert np.max(np.abs(UGg - UG)) < 1e-10
     assert np.max(np.abs(EGg - EG)) < 1e-10 * np.max(np.abs(EG))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_charge_transformation_matches_oracle(oracle, precision):
+    """glasma_transform_charge (PERFORM_COLOR_CHARGE_TRANSFORMATION, S/CALC/GaugeTransformation.cpp:28-31)
+    with an uploaded G and with the G a gauge-fixing run leaves, against the oracle; the handle's own
+    currents are left as they were."""
+    from tests.test_oracle_golden import random_gauge
+
+    N = (8, 6, 10)
+    f = O.random_fields(N, 77)
+    G = random_gauge(N, 78)
+    tol = 1e-14 if precision == "fp64" else 2e-7
+    with Lattice(N, precision=precision) as lat:
+        lat.upload_fields(f)
+        lat.upload("G", G)
+        Gd = lat.download("G")
+        for k in ("Jp", "Jm", "JpStat", "JmStat"):
+            J = lat.download(k)
+            got = lat.transform_charge(k)
+            want = oracle.transform_charge(Gd, J, N)
+            assert np.max(np.abs(got - want)) < tol * max(1.0, np.max(np.abs(want))), k
+            assert np.array_equal(lat.download(k), J), k
+        with pytest.raises(ValueError):
+            lat.transform_charge("E")
+        if precision != "fp64":
+            return
+        # after gauge fixing: the fixer's G
+        lat.gauge_reset()
+        lat.coulomb_fix(0.5, 5, open_z=True)
+        Gd = lat.download("G")
+        got = lat.transform_charge("JpStat")
+        want = oracle.transform_charge(Gd, lat.download("JpStat"), N)
+        assert np.max(np.abs(got - want)) < tol * max(1.0, np.max(np.abs(want)))

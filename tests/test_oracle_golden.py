@@ -162,3 +162,29 @@ def test_config1_reference_cannot_run_the_asked_width(golden_dir):
     assert not bool(g["reference_runs_sigma_asked"])
     assert float(g["cfg_sigma_asked"]) == 4.0 and float(g["cfg_sigma"]) == 5.0
     assert g["bulk"].shape == (21, 16) and np.all(np.isfinite(g["bulk"]))
+
+
+def random_gauge(N, seed):
+    """Seeded SU(3) gauge transformation in the G storage ([.., j, i] per site, ghosts included)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    Nx, Ny, Nz = N
+    M = O.expi_batched(0.9, rng.standard_normal((Nz + 2, Ny, Nx, 8)))
+    return np.ascontiguousarray(np.swapaxes(M, -1, -2))
+
+
+def test_charge_transformation_is_the_adjoint_action(oracle):
+    """PERFORM_COLOR_CHARGE_TRANSFORMATION (S/CALC/GaugeTransformation.cpp:28-31) restated: the
+    oracle's jG = 2 tr(t^a G (t.j) G^dagger) against the same action formed with numpy matrices,
+    the ghost slices copied from the edge slices; the identity leaves j unchanged."""
+    N = (5, 4, 6)
+    G = random_gauge(N, 71)
+    J = 0.3 * np.random.Generator(np.random.PCG64(72)).standard_normal((N[2] + 2, N[1], N[0], 8))
+    got = oracle.transform_charge(G, J, N)
+    Gm = np.swapaxes(G, -1, -2)
+    want = O.algebra_from_herm(Gm @ O.herm_from_algebra(J) @ np.conj(np.swapaxes(Gm, -1, -2)))
+    O.sync_ghosts(want)
+    assert np.max(np.abs(got - want)) < 1e-14
+    same = oracle.transform_charge(O.identity_gauge(N), J, N)
+    ref = J.copy()
+    O.sync_ghosts(ref)
+    assert np.max(np.abs(same - ref)) < 1e-15
