@@ -304,6 +304,27 @@ __device__ __forceinline__ void herm_pair(const Alg<T>& e1, const Alg<T>& e2, Ma
 #pragma unroll
   for (int k = 0; k < 9; k++) M.e[k] = mk<T>(M1.e[k].re - M2.e[k].im, M1.e[k].im + M2.e[k].re);
 }
+// C = A B (kDag: A B^dagger) for a product known to be traceless (a similarity transform of a
+// traceless matrix): entry (2,2) as -(C00 + C11) instead of its own three products.
+template <typename T, bool kDag>
+__device__ __forceinline__ void mul_traceless_result(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      if (i == 2 && j == 2) continue;
+      cx<T> acc = mk<T>(T(0), T(0));
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        if constexpr (kDag)
+          cfma_nc(acc, A.e[i + 3 * k], B.e[j + 3 * k]);
+        else
+          cfma(acc, A.e[i + 3 * k], B.e[k + 3 * j]);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+  C.e[8] = mk<T>(-(C.e[0].re + C.e[4].re), -(C.e[0].im + C.e[4].im));
+}
 // out1 = V (t.e1) V^dagger, out2 = V (t.e2) V^dagger
 template <typename T>
 __device__ __forceinline__ void adj_mul2(const Mat<T>& V, const Alg<T>& e1, const Alg<T>& e2, Alg<T>& out1,
@@ -311,7 +332,7 @@ __device__ __forceinline__ void adj_mul2(const Mat<T>& V, const Alg<T>& e1, cons
   Mat<T> M, W, C;
   herm_pair(e1, e2, M);
   mul_nn(V, M, W);
-  mul_nd(W, V, C);
+  mul_traceless_result<T, true>(W, V, C);
   split_herm_pair(C, out1, out2);
 }
 // out1 = V^dagger (t.e1) V, out2 = V^dagger (t.e2) V
@@ -321,7 +342,7 @@ __device__ __forceinline__ void inv_adj_mul2(const Mat<T>& V, const Alg<T>& e1, 
   Mat<T> M, W, C;
   herm_pair(e1, e2, M);
   mul_dn(V, M, W);
-  mul_nn(W, V, C);
+  mul_traceless_result<T, false>(W, V, C);
   split_herm_pair(C, out1, out2);
 }
 
@@ -392,6 +413,30 @@ __device__ __forceinline__ void mul_dn_traceless(const Mat<T>& A, const Mat<T>& 
     }
 }
 
+// C = A^dagger B when the product is anti-Hermitian (A^dagger D A with D anti-Hermitian and B = D A):
+// the upper triangle and the imaginary diagonal are formed, the lower triangle as -conj of the upper.
+template <typename T>
+__device__ __forceinline__ void mul_dn_antiherm(const Mat<T>& A, const Mat<T>& B, Mat<T>& C) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      cx<T> acc = mk<T>(T(0), T(0));
+      if (i == j) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {  // Im conj(A_ki) B_ki
+          acc.im = fma(A.e[k + 3 * i].re, B.e[k + 3 * j].im, acc.im);
+          acc.im = fma(-A.e[k + 3 * i].im, B.e[k + 3 * j].re, acc.im);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) cfma_cn(acc, A.e[k + 3 * i], B.e[k + 3 * j]);
+        C.e[j + 3 * i] = mk<T>(-acc.re, acc.im);
+      }
+      C.e[i + 3 * j] = acc;
+    }
+}
+
 template <typename T>
 struct Trig;
 template <>
@@ -438,10 +483,12 @@ __device__ __forceinline__ void expi_impl(T c, const Alg<T>& al, Mat<T>& X) {
     // FP64 without transcendental functions (they cost ~60 % of this exponential on GB300's FP64 pipe):
     // exp(iQ) = sum_n i^n Q^n / n!, and by Cayley-Hamilton (Q^3 = c1 Q + c0) Q^n / n! = a_n + b_n Q + d_n
     // Q^2 with a_{n+1} = c0 d_n / (n+1), b_{n+1} = (a_n + c1 d_n) / (n+1), d_{n+1} = b_n / (n+1).  The
-    // eigenvalues of Q are at most sqrt(4 c1 / 3) in size, so the first omitted term is below
-    // 0.82^18 / 18! ~ 4e-18 with 17 terms for c1 < 0.5, and below 0.17^13 / 13! ~ 1e-19 with 12 for
-    // c1 < 0.02; beyond c1 = 0.5 the closed form below.
-    const int nterms = c1 < T(0.02) ? 12 : 17;
+    // eigenvalues of Q are at most l = sqrt(4 c1 / 3) in size, so after N terms the first omitted one is
+    // below l^(N+1) / (N+1)!: with 17 terms for c1 < 0.5 below 0.82^18 / 18! ~ 4e-18, with 11 for
+    // c1 < 0.02 below 0.17^12 / 12! ~ 8e-19, with 8 for c1 < 1e-3 below 0.037^9 / 9! ~ 3e-19, with 7 for
+    // c1 < 1e-4 below 0.012^8 / 8! ~ 8e-21 (the leapfrog's links mostly fall in the last two tiers);
+    // beyond c1 = 0.5 the closed form below.
+    const int nterms = c1 < T(1e-4) ? 7 : (c1 < T(1e-3) ? 8 : (c1 < T(0.02) ? 11 : 17));
     T a = T(1), b = T(0), d = T(0);
     T f0r = T(1), f0i = T(0), f1r = T(0), f1i = T(0), f2r = T(0), f2i = T(0);
 #pragma unroll

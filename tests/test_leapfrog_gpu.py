@@ -386,11 +386,12 @@ def test_upload_begin_finish(precision):
     assert seq["bulk"] == pipe["bulk"]
 
 
-@pytest.mark.parametrize("scale", [1e-4, 0.05, 0.4, 1.5, 6.0])
+@pytest.mark.parametrize("scale", [1e-4, 0.01, 0.05, 0.1, 0.2, 0.4, 1.5, 6.0])
 def test_link_exponential_across_its_tiers(oracle, scale):
     """UpdateGaugeLinks alone with E scaled so that the FP64 exponential runs each of its forms (the
-    Taylor polynomial for tiny arguments, the 12- and 17-term Cayley-Hamilton series below c1 = 0.5, the
-    closed form above): links against the oracle's exponential at 1e-14."""
+    Taylor polynomial for tiny arguments, the 7-, 8-, 11- and 17-term Cayley-Hamilton series below
+    c1 = 0.5, the closed form above; scale 0.01 gives c1 in 1e-6..1e-5, 0.1 in 7e-5..9e-4, 0.2 in
+    3e-4..4e-3): links against the oracle's exponential at 1e-14."""
     N, a, dt = (6, 4, 8), (1.0, 1.0, 1.0), 1.0
     f = O.random_fields(N, 41)
     f["E"] = f["E"] * scale
