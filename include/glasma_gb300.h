@@ -115,8 +115,9 @@ int glasma_upload_device(glasma_lattice* h, int field, const double* device_aos)
  *   begin(inputs 0); finish(); for k: { begin(inputs k+1); step(); read result; finish(); }
  * The host buffers must stay unchanged until the handle's stream has passed finish's conversion (after
  * any synchronising call: an observable, a download, glasma_synchronize); page-locked buffers let the
- * copy run without the CPU.  A begin waits on the device for the previous finish's conversion to have
- * read the staging.
+ * copy run without the CPU.  The staging is double buffered (two sets of the begun fields' size, allocated
+ * on first use): a begin waits on the device only for the conversion two finishes back, which has
+ * normally long completed, so the copies start at once.
  * No reference counterpart (the reference's fields live on the host). */
 int glasma_upload_begin(glasma_lattice* h, int field, const double* host);
 int glasma_upload_finish(glasma_lattice* h);

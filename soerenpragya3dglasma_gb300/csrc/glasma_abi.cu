@@ -236,9 +236,35 @@ int sync_field_ghosts(glasma_lattice* h, int field) {
   return GLASMA_OK;
 }
 
+// Results come back through a small page-locked, mapped buffer that a kernel writes: a device-to-host
+// cudaMemcpy (into the caller's pageable memory) queued behind the copy engines' uploads of
+// glasma_upload_begin and waited for all of them, so a step's result read serialised the next step's
+// input copies with the step.
+constexpr size_t kResultDoubles = 8192;
+__global__ void result_copy_kernel(const double* __restrict__ src, double* __restrict__ dst, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
 int copy_results_to_host(glasma_lattice* h, const double* dev, double* host, size_t n) {
-  GLASMA_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "result copy");
-  GLASMA_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  if (!h->result_host) {
+    void* p = nullptr;
+    GLASMA_CUDA(cudaHostAlloc(&p, kResultDoubles * sizeof(double), cudaHostAllocMapped), "result buffer");
+    void* d = nullptr;
+    cudaError_t e = cudaHostGetDevicePointer(&d, p, 0);
+    if (e != cudaSuccess) {
+      cudaFreeHost(p);
+      return cuda_fail(e, "result buffer address");
+    }
+    h->result_host = static_cast<double*>(p);
+    h->result_dev = static_cast<double*>(d);
+  }
+  for (size_t done = 0; done < n; done += kResultDoubles) {
+    const size_t m = n - done < kResultDoubles ? n - done : kResultDoubles;
+    result_copy_kernel<<<1, 256, 0, h->stream>>>(dev + done, h->result_dev, (int)m);
+    GLASMA_CUDA(cudaGetLastError(), "result copy");
+    GLASMA_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+    std::memcpy(host + done, h->result_host, m * sizeof(double));
+  }
   return GLASMA_OK;
 }
 
@@ -427,11 +453,14 @@ int glasma_destroy(glasma_lattice* h) {
   if (h->contrib) cudaFree(h->contrib);
   if (h->staging) cudaFree(h->staging);
   if (h->scratch) cudaFree(h->scratch);
+  if (h->result_host) cudaFreeHost(h->result_host);
   if (h->xfer_stream) cudaStreamSynchronize(h->xfer_stream);
-  for (int i = 0; i < 10; i++)
-    if (h->stage_f[i]) cudaFree(h->stage_f[i]);
+  for (int b = 0; b < 2; b++) {
+    for (int i = 0; i < 10; i++)
+      if (h->stage_f[b][i]) cudaFree(h->stage_f[b][i]);
+    if (h->stage_free[b]) cudaEventDestroy(h->stage_free[b]);
+  }
   if (h->xfer_done) cudaEventDestroy(h->xfer_done);
-  if (h->stage_free) cudaEventDestroy(h->stage_free);
   if (h->xfer_stream) cudaStreamDestroy(h->xfer_stream);
   glasma::gaugefix_destroy(h->gf);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -544,22 +573,27 @@ int glasma_upload_begin(glasma_lattice* h, int field, const double* host) {
   if (!h->xfer_stream) {
     GLASMA_CUDA(cudaStreamCreateWithFlags(&h->xfer_stream, cudaStreamNonBlocking), "transfer stream");
     GLASMA_CUDA(cudaEventCreateWithFlags(&h->xfer_done, cudaEventDisableTiming), "transfer event");
-    GLASMA_CUDA(cudaEventCreateWithFlags(&h->stage_free, cudaEventDisableTiming), "staging event");
+    for (int b = 0; b < 2; b++)
+      GLASMA_CUDA(cudaEventCreateWithFlags(&h->stage_free[b], cudaEventDisableTiming), "staging event");
   }
+  const int b = h->stage_slot;
   const size_t bytes = (size_t)h->g.S * host_doubles_per_site(field) * sizeof(double);
-  if (!h->stage_f[field]) {
+  if (!h->stage_f[b][field]) {
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(GLASMA_ERR_OUT_OF_MEMORY, std::string("cudaMalloc upload staging: ") + cudaGetErrorString(e));
     }
-    h->stage_f[field] = static_cast<double*>(p);
+    h->stage_f[b][field] = static_cast<double*>(p);
   }
-  // the previous finish's conversion must have read this staging area before it is overwritten (an
-  // event never recorded is complete)
-  GLASMA_CUDA(cudaStreamWaitEvent(h->xfer_stream, h->stage_free, 0), "wait for staging");
-  GLASMA_CUDA(cudaMemcpyAsync(h->stage_f[field], host, bytes, cudaMemcpyHostToDevice, h->xfer_stream),
+  // The conversion that last read this set (two finishes ago) must be done before it is overwritten
+  // (an event never recorded is complete).  With one set the wait would be on the finish just before,
+  // whose conversion is usually still queued: measured on GB300, copies that wait on such an event
+  // did not start until the next call on the transfer stream, so a begin/step/sync/finish loop ran
+  // the copies after the step instead of under it (116.6 ms against 66.0 per 128x128x512 FP64 step).
+  GLASMA_CUDA(cudaStreamWaitEvent(h->xfer_stream, h->stage_free[b], 0), "wait for staging");
+  GLASMA_CUDA(cudaMemcpyAsync(h->stage_f[b][field], host, bytes, cudaMemcpyHostToDevice, h->xfer_stream),
               "upload copy");
   h->pending |= 1u << field;
   return GLASMA_OK;
@@ -570,15 +604,18 @@ int glasma_upload_finish(glasma_lattice* h) {
   if (!h->pending) return GLASMA_OK;
   GLASMA_CUDA(cudaEventRecord(h->xfer_done, h->xfer_stream), "record transfers");
   GLASMA_CUDA(cudaStreamWaitEvent(h->stream, h->xfer_done, 0), "wait for transfers");
+  const int b = h->stage_slot;
   for (int f = 0; f < 10; f++) {
     if (!(h->pending & (1u << f))) continue;
     const int P = host_doubles_per_site(f);
+    double* src = h->stage_f[b][f];
     cudaError_t e = h->precision == GLASMA_FP64
-                        ? glasma::launch_aos_to_soa<double>(h->stage_f[f], static_cast<double*>(h->f[f]), h->g.S, P, h->stream)
-                        : glasma::launch_aos_to_soa<float>(h->stage_f[f], static_cast<float*>(h->f[f]), h->g.S, P, h->stream);
+                        ? glasma::launch_aos_to_soa<double>(src, static_cast<double*>(h->f[f]), h->g.S, P, h->stream)
+                        : glasma::launch_aos_to_soa<float>(src, static_cast<float*>(h->f[f]), h->g.S, P, h->stream);
     if (e != cudaSuccess) return cuda_fail(e, "aos_to_soa of staged upload");
   }
-  GLASMA_CUDA(cudaEventRecord(h->stage_free, h->stream), "record staging read");
+  GLASMA_CUDA(cudaEventRecord(h->stage_free[b], h->stream), "record staging read");
+  h->stage_slot = b ^ 1;
   h->pending = 0;
   return GLASMA_OK;
 }

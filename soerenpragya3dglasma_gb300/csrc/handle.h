@@ -20,6 +20,8 @@ struct glasma_lattice {
   double* staging;    // device AoS staging buffer for host copies
   size_t staging_bytes;
   double* scratch;    // reduction partials and results
+  double* result_host;  // page-locked, mapped: observables' results written here by a kernel (first use)
+  double* result_dev;   // its device address
   size_t scratch_doubles;
   glasma::GaugeFixState* gf;
   int tile_x;         // K1 tile width along x (autotuned)
@@ -34,8 +36,9 @@ struct glasma_lattice {
   // asynchronous uploads (glasma_upload_begin / glasma_upload_finish)
   cudaStream_t xfer_stream;  // copies host -> staging, overlapping the handle's kernels (first use)
   cudaEvent_t xfer_done;     // recorded on xfer_stream at finish: every begun copy has landed
-  cudaEvent_t stage_free;    // recorded on the handle's stream at finish: the staging has been read
-  double* stage_f[10];       // per-field staging areas in the reference's host layout
+  cudaEvent_t stage_free[2];  // recorded on the handle's stream at finish: that set's staging has been read
+  double* stage_f[2][10];     // two sets of per-field staging areas (reference host layout), alternating
+  int stage_slot;             // the set the next begin copies into (flips at each finish)
   unsigned pending;          // fields begun and not yet finished (bit per glasma_field)
 };
 
