@@ -586,16 +586,21 @@ def run_ours(args):
         fr = {k: (v.astype(np.complex64).astype(np.complex128) if np.iscomplexobj(v)
                   else v.astype(np.float32).astype(np.float64)) for k, v in fp.items()}
         vals = {}
-        for prec, reals in (("fp64", 18), ("fp32", 18), ("fp32_l12", 12)):
-            with Lattice(Np, precision=prec[:4], reunitarize_every=16 if prec != "fp64" else 0, stream=stream) as lp:
+        # fp64_exact: FP64 from the unrounded state, the chaos control -- how far two FP64 runs whose
+        # starts differ only by FP32 rounding drift apart, the floor any FP32 run is measured against
+        for prec, reals in (("fp64", 18), ("fp64_exact", 18), ("fp32", 18), ("fp32_l12", 12)):
+            with Lattice(Np, precision=prec[:4], reunitarize_every=16 if prec.startswith("fp32") else 0,
+                         stream=stream) as lp:
                 lp.link_reals = reals
-                lp.upload_fields(fr)
+                lp.upload_fields(fp if prec == "fp64_exact" else fr)
                 lp.step(DT, stepsp, save_uold=False)
                 vals[prec] = (lp.bulk()[9], lp.objective(112, 144, Lattice.PL_OVER_PT), lp.unitarity()[0])
         fp32["physical_check"] = {
             "state": "MV collision 64x64x256 (g^2 mu 0.5, m 0.2, sigma_z 4, centres 104/152), %d steps, FP32 "
                      "reunitarised every 16 steps, both from the same FP32-rounded fields" % stepsp,
             "energy_rel_err_vs_fp64": abs(vals["fp32"][0] - vals["fp64"][0]) / abs(vals["fp64"][0]),
+            "chaos_floor_energy_rel": abs(vals["fp64_exact"][0] - vals["fp64"][0]) / abs(vals["fp64"][0]),
+            "chaos_floor_note": "FP64 from the unrounded state against FP64 from the FP32-rounded state",
             "pl_over_pt_central_fp64": vals["fp64"][1], "pl_over_pt_central_fp32": vals["fp32"][1],
             "fp32_unitarity_max": vals["fp32"][2],
             "links12_energy_rel_err_vs_fp64": abs(vals["fp32_l12"][0] - vals["fp64"][0]) / abs(vals["fp64"][0]),
@@ -684,6 +689,7 @@ def run_ours(args):
             "fp32_value": fp32["value"], "fp32_ms_per_step": fp32["ms_per_step"],
             "fp32_hbm_frac": fp32["step_hbm_frac"], "fp32_energy_rel_err": fp32["energy_rel_err_vs_fp64"],
             "fp32_energy_rel_err_mv_collision": phys.get("energy_rel_err_vs_fp64"),
+            "mv_collision_chaos_floor": phys.get("chaos_floor_energy_rel"),
             "links12_value": fp32["links12"]["value"], "links12_hbm_frac": fp32["links12"]["step_hbm_frac"],
             "fp32_over_fp64": (fp32["value"] / value) if value else None}
     print(json.dumps(line), flush=True)
