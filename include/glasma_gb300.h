@@ -81,6 +81,13 @@ enum glasma_field {
                                             converge with open z boundaries); Delta is then the
                                             gradient of sum Re tr UG over the links inside the lattice
                                             and the iteration converges */
+#define GLASMA_GF_MIXED 0x8u             /* FP64 handles: the sweeps first run on FP32 copies of U and
+                                            G in FP32 arithmetic (FP32 transforms, FP64 monitor sums)
+                                            until the maximum deviation is <= 1e-5 or stops falling, then
+                                            G is widened, projected onto SU(3) in FP64, and the FP64
+                                            sweeps finish to the stopping rule; log rows and the count
+                                            cover both phases.  The FP32 update's unitarity guard is
+                                            1e-5.  GLASMA_ERR_UNSUPPORTED on FP32 handles */
 
 /* Create a lattice (replaces Lattice::Init, S/LATTICE/SUNcVariables.cpp:71-90, and the
  * container constructors, S/LATTICE/GaugeLinks.cpp:110-127): links set to the identity,

@@ -415,7 +415,8 @@ inline void LoadConfiguration(const std::string& Ufname, const std::string& Efna
 // Fourier-accelerated update is the default, as in the reference.  Defining GAUGE_FIXING_OPEN_Z as well
 // selects the open-z functional for the Fourier update (GLASMA_GF_OPEN_Z: the top slice's z link into
 // the ghost slice left out of the deviation), with which the iteration converges on open-z lattices
-// where the reference's leaves SU(3); Flags can also be set at run time.
+// where the reference's leaves SU(3); Flags can also be set at run time (GLASMA_GF_MIXED adds FP32
+// sweeps before the final FP64 ones).
 namespace CoulombGaugeFixing {
 #if defined(GAUGE_FIXING_OPEN_Z)
 inline unsigned Flags = GLASMA_GF_OPEN_Z;

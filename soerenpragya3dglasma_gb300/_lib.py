@@ -20,6 +20,7 @@ STEP_SAVE_UOLD = 0x1
 GF_PROJECT_ZERO_MODE = 0x1
 GF_FFT_FP32 = 0x2
 GF_OPEN_Z = 0x4
+GF_MIXED = 0x8
 GF_ALGORITHMS = {"fourier": 0, "los_alamos": 1, "jacobi": 2}
 
 

@@ -214,6 +214,142 @@ __global__ void __launch_bounds__(kGfThreads) update_kernel(Geometry g, const C*
   red::block_reduce_store<3>(v, op, partials + (long long)blockIdx.x * 3);
 }
 
+// ---- mixed-precision sweeps (GLASMA_GF_MIXED, FP64 handles): the Fourier-accelerated iteration on
+// FP32 copies of U and G with FP32 arithmetic (GB300 runs FP32 at 64x its FP64 rate) until the FP32
+// deviation reaches its rounding floor; the monitors' sums and extrema stay FP64.  Then G is widened,
+// projected back onto SU(3) in FP64, and the FP64 iteration makes the final sweeps.
+__device__ __forceinline__ void ld_f(const cx<float>* __restrict__ U, long long S, long long comp0, long long s,
+                                     Mat<float>& m) {
+  const cx<float>* p = U + comp0 * S + s;
+#pragma unroll
+  for (int k = 0; k < 9; k++) m.e[k] = p[(long long)k * S];
+}
+__device__ __forceinline__ void st_f(cx<float>* __restrict__ U, long long S, long long comp0, long long s,
+                                     const Mat<float>& m) {
+  cx<float>* p = U + comp0 * S + s;
+#pragma unroll
+  for (int k = 0; k < 9; k++) p[(long long)k * S] = m.e[k];
+}
+
+__global__ void narrow_kernel(const cx<double>* __restrict__ src, cx<float>* __restrict__ dst, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cx<double> v = src[i];
+  dst[i] = mk<float>((float)v.re, (float)v.im);
+}
+
+// UG_mu(x) = G(x) U_mu(x) G^d(x+mu) in FP32, interior sites
+__global__ void __launch_bounds__(128) transform_links32_kernel(Geometry g, const cx<float>* U, const cx<float>* G,
+                                                                cx<float>* UG) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.vol) return;
+  const long long r = idx / g.nx;
+  const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+  const long long s = idx + g.plane;
+  const long long fwd[3] = {nbr(g, x, y, z, 1, 0, 0), nbr(g, x, y, z, 0, 1, 0), s + g.plane};
+  Mat<float> gx, u, gy, t, o;
+  ld_f(G, g.S, 0, s, gx);
+  for (int mu = 0; mu < 3; mu++) {
+    ld_f(U, g.S, mu * 9, s, u);
+    ld_f(G, g.S, 0, fwd[mu], gy);
+    mul_nn(gx, u, t);
+    mul_nd(t, gy, o);
+    st_f(UG, g.S, mu * 9, s, o);
+  }
+}
+
+// deviation_kernel in FP32 (site_w's sum, the projection and X); partials in FP64
+__global__ void __launch_bounds__(kGfThreads) deviation32_kernel(Geometry g, const cx<float>* UG, float c0, float c1,
+                                                                 float c2, float2* X, double* partials, int open_top) {
+  double v[4] = {0.0, 0.0, 1.0e300, 0.0};
+  const int op[4] = {1, 0, 2, 0};
+  const float c[3] = {c0, c1, c2};
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long r = idx / g.nx;
+    const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+    const long long s = idx + g.plane;
+    const long long back[3] = {nbr(g, x, y, z, -1, 0, 0), nbr(g, x, y, z, 0, -1, 0), s - g.plane};
+    const float fwd2 = (open_top && z == g.nz - 1) ? 0.f : 1.f;
+    Mat<float> w;
+    set_zero(w);
+    for (int mu = 0; mu < 3; mu++) {
+      if (c[mu] == 0.f) continue;
+      const float cf = mu == 2 ? fwd2 : 1.f;
+      Mat<float> u, d;
+      ld_f(UG, g.S, mu * 9, s, u);
+      ld_f(UG, g.S, mu * 9, back[mu], d);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          const int k = i + 3 * j, kt = j + 3 * i;
+          w.e[k].re += c[mu] * (cf * u.e[k].re + d.e[kt].re);
+          w.e[k].im += c[mu] * (cf * u.e[k].im - d.e[kt].im);
+        }
+    }
+    Alg<float> dev;
+    retr_itg(w, 1.f, dev);
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      v[0] = fmax(v[0], (double)fabsf(dev.a[a]));
+      v[1] += (double)dev.a[a] * (double)dev.a[a];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) X[(long long)q * g.vol + idx] = make_float2(dev.a[2 * q], dev.a[2 * q + 1]);
+    const double lf = (double)w.e[0].re + (double)w.e[4].re + (double)w.e[8].re;
+    v[2] = fmin(v[2], lf);
+    v[3] += lf;
+  }
+  red::block_reduce_store<4>(v, op, partials + (long long)blockIdx.x * 4);
+}
+
+// update_kernel in FP32.  The unitarity guard cannot hold FP64's 1e-13 here (an FP32 exponential is
+// unitary to ~1e-7): it trips at `guard`, which still catches the runaway the reference's guard exists for.
+__global__ void __launch_bounds__(kGfThreads) update32_kernel(Geometry g, const float2* X, cx<float>* G, float alpha,
+                                                              double* partials, float guard) {
+  double v[3] = {0.0, 0.0, 0.0};
+  const int op[3] = {1, 0, 0};
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
+       idx += (long long)gridDim.x * blockDim.x) {
+    Alg<float> upd;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float2 x = X[(long long)q * g.vol + idx];
+      upd.a[2 * q] = x.x;
+      upd.a[2 * q + 1] = x.y;
+    }
+    Mat<float> wt, gm, gn;
+    expi(-alpha, upd, wt);
+    if (!(unitarity_norm(wt) <= guard)) v[2] += 1.0;
+    const double sr = 3.0 - (double)wt.e[0].re - (double)wt.e[4].re - (double)wt.e[8].re;
+    const double si = -((double)wt.e[0].im + (double)wt.e[4].im + (double)wt.e[8].im);
+    const double step = sqrt(sr * sr + si * si);
+    v[0] = fmax(v[0], step);
+    v[1] += step * step;
+    const long long s = idx + g.plane;
+    ld_f(G, g.S, 0, s, gm);
+    mul_dn(wt, gm, gn);
+    st_f(G, g.S, 0, s, gn);
+  }
+  red::block_reduce_store<3>(v, op, partials + (long long)blockIdx.x * 3);
+}
+
+// G = the SU(3) projection (FP64 Newton, reunitarize_newton) of the widened FP32 G, every site
+__global__ void widen_gauge_kernel(const cx<float>* __restrict__ G32, cx<double>* __restrict__ G, long long S) {
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  Mat<double> m;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const cx<float> v = G32[(long long)k * S + s];
+    m.e[k] = mk<double>((double)v.re, (double)v.im);
+  }
+  reunitarize_newton(m);
+#pragma unroll
+  for (int k = 0; k < 9; k++) G[(long long)k * S + s] = m.e[k];
+}
+
 // ---- local updates: Los Alamos (LosAlamos.cpp:13-95) and Jacobi (Jacobi.cpp:13-80)
 // The over-relaxation draw of one site of one checkerboard pass: splitmix64's finaliser (Steele, Lea &
 // Flood, OOPSLA 2014) over (seed, 2 * iteration + pass, site), uniform in [0, 1).  Counter-based, so
@@ -817,9 +953,11 @@ cudaError_t finish_fields(const GaugeFixArgs& a) {
   return cudaStreamSynchronize(a.stream);
 }
 
+// n_start > 0: the final FP64 sweeps after the FP32 ones of run_mixed (the fields already copied, log
+// rows and the iteration count continued)
 template <typename T>
 int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
-             double* log, int* iterations, std::string* err) {
+             double* log, int* iterations, std::string* err, int n_start = 0) {
   const Geometry& g = a.g;
   cudaStream_t st = a.stream;
   cx<T>* G = static_cast<cx<T>*>(a.G);
@@ -829,7 +967,7 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
     return GLASMA_ERR_CUDA;
   };
   cudaError_t e;
-  if ((e = copy_fields<T>(a)) != cudaSuccess) return cuda_err(e, "copy fields");
+  if (n_start == 0 && (e = copy_fields<T>(a)) != cudaSuccess) return cuda_err(e, "copy fields");
   auto transform_links = [&]() { return transform_links_all<T>(a); };
   if ((e = transform_links()) != cudaSuccess) return cuda_err(e, "transform links");
 
@@ -841,7 +979,7 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
   double* res = a.scratch + (size_t)nb * 7;     // 8 results
   double h[8];
   double gmax = 1.0;
-  int n = 0;
+  int n = n_start;
   int status = GLASMA_OK;
   const double minf0 = 2.0 * 3 * (1.0 / (g.a[0] * g.a[0]) + 1.0 / (g.a[1] * g.a[1]) + 1.0 / (g.a[2] * g.a[2]));
   const bool fft32 = (flags & GLASMA_GF_FFT_FP32) != 0;
@@ -902,6 +1040,124 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
   if (status != GLASMA_OK) return status;
   if ((e = finish_fields<T>(a)) != cudaSuccess) return cuda_err(e, "final transform");
   return GLASMA_OK;
+}
+
+// GLASMA_GF_MIXED on FP64 handles: the sweeps on FP32 copies of U and G until the FP32 maximum
+// deviation reaches kMixedSwitch or stops falling (its rounding floor), then G widened and projected
+// onto SU(3) in FP64 and the FP64 sweeps to the stopping rule (run_impl, continuing the count and log).
+constexpr double kMixedSwitch = 1e-5;  // max |Delta| at which the FP32 sweeps hand over
+constexpr int kMixedStall = 20;        // or after this many FP32 sweeps without a 5 % better maximum
+constexpr float kMixedGuard = 1e-5f;   // unitarity guard of the FP32 update
+
+struct Fp32Copies {
+  cx<float>* U = nullptr;
+  cx<float>* G = nullptr;
+  cx<float>* UG = nullptr;
+  cudaStream_t stream = nullptr;
+  ~Fp32Copies() {
+    if (stream) cudaStreamSynchronize(stream);
+    cudaFree(U);
+    cudaFree(G);
+    cudaFree(UG);
+  }
+};
+
+int run_mixed(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iters, double tol, unsigned flags,
+              double* log, int* iterations, std::string* err) {
+  const Geometry& g = a.g;
+  cudaStream_t st = a.stream;
+  auto cuda_err = [&](cudaError_t e, const char* where) {
+    *err = std::string(where) + ": " + cudaGetErrorString(e);
+    return GLASMA_ERR_CUDA;
+  };
+  Fp32Copies c;
+  c.stream = st;
+  cudaError_t e = cudaMalloc(&c.U, sizeof(cx<float>) * 27 * g.S);
+  if (e == cudaSuccess) e = cudaMalloc(&c.G, sizeof(cx<float>) * 9 * g.S);
+  if (e == cudaSuccess) e = cudaMalloc(&c.UG, sizeof(cx<float>) * 27 * g.S);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *err = std::string("cudaMalloc FP32 gauge-fixing copies: ") + cudaGetErrorString(e);
+    return GLASMA_ERR_OUT_OF_MEMORY;
+  }
+  if ((e = copy_fields<double>(a)) != cudaSuccess) return cuda_err(e, "copy fields");
+  narrow_kernel<<<(unsigned)((27 * g.S + 255) / 256), 256, 0, st>>>(static_cast<const cx<double>*>(a.U), c.U, 27 * g.S);
+  narrow_kernel<<<(unsigned)((9 * g.S + 255) / 256), 256, 0, st>>>(static_cast<const cx<double>*>(a.G), c.G, 9 * g.S);
+  const unsigned tb = (unsigned)((g.vol + 127) / 128);
+  auto transform32 = [&]() {
+    transform_links32_kernel<<<tb, 128, 0, st>>>(g, c.U, c.G, c.UG);
+    cudaError_t x = cudaGetLastError();
+    if (x == cudaSuccess) x = launch_sync_ghosts<cx<float>>(g, c.G, 9, st);
+    return x;
+  };
+  if ((e = transform32()) != cudaSuccess) return cuda_err(e, "FP32 transform links");
+  if ((e = ensure_twiddles32(s, st)) != cudaSuccess) return cuda_err(e, "FP32 twiddles");
+  const float cw[3] = {(float)((a.a_scale / g.a[0]) * (a.a_scale / g.a[0])),
+                       (float)((a.a_scale / g.a[1]) * (a.a_scale / g.a[1])),
+                       g.nz > 1 ? (float)((a.a_scale / g.a[2]) * (a.a_scale / g.a[2])) : 0.f};
+  const unsigned nb = blocks_for(g.vol, kGfThreads, kGfBlocks);
+  double* part_dev = a.scratch;
+  double* part_upd = a.scratch + (size_t)nb * 4;
+  double* res = a.scratch + (size_t)nb * 7;
+  const double minf0 = 2.0 * 3 * (1.0 / (g.a[0] * g.a[0]) + 1.0 / (g.a[1] * g.a[1]) + 1.0 / (g.a[2] * g.a[2]));
+  float2* X32 = static_cast<float2*>(s->X);
+  const long long tot = 4 * g.vol;
+  const int project = (flags & GLASMA_GF_PROJECT_ZERO_MODE) ? 1 : 0;
+  const int open_top = (flags & GLASMA_GF_OPEN_Z) ? 1 : 0;
+  double h[8];
+  double gmax = 1.0, best = 1e300;
+  int n = 0, since_best = 0;
+  while (n < max_iters && gmax > tol) {
+    deviation32_kernel<<<nb, kGfThreads, 0, st>>>(g, c.UG, cw[0], cw[1], cw[2], X32, part_dev, open_top);
+    red::finish_kernel<4><<<1, red::kThreads, 0, st>>>(part_dev, (int)nb, 1 | (0 << 2) | (2 << 4) | (0 << 6), res);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "FP32 deviation");
+    if ((e = fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft forward");
+    accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2],
+                                                                              X32, project);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
+    if ((e = fft3d_t<float2>(s, X32, 4, 1, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft backward");
+    update32_kernel<<<nb, kGfThreads, 0, st>>>(g, X32, c.G, (float)alpha, part_upd, kMixedGuard);
+    red::finish_kernel<3><<<1, red::kThreads, 0, st>>>(part_upd, (int)nb, 1 | (0 << 2) | (0 << 4), res + 4);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "FP32 update");
+    if ((e = transform32()) != cudaSuccess) return cuda_err(e, "FP32 transform links");
+    if ((e = cudaMemcpyAsync(h, res, sizeof(double) * 7, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+      return cuda_err(e, "monitor copy");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_err(e, "monitor sync");
+    const double V = (double)g.vol;
+    gmax = h[0];
+    if (log) {
+      double* o = log + 7 * (size_t)n;
+      o[0] = n;
+      o[1] = h[0];
+      o[2] = sqrt(h[1] / (8.0 * V));
+      o[3] = h[4];
+      o[4] = sqrt(h[5] / (8.0 * V));
+      o[5] = h[2] < minf0 ? h[2] : minf0;
+      o[6] = h[3] / V;
+    }
+    n++;
+    if (h[6] > 0.0) {
+      *iterations = n;
+      *err = "FP32 gauge update left SU(3) by more than 1e-5";
+      return GLASMA_ERR_NUMERICAL;
+    }
+    if (gmax < 0.95 * best) {
+      best = gmax;
+      since_best = 0;
+    } else if (++since_best >= kMixedStall) {
+      break;
+    }
+    if (gmax <= kMixedSwitch) break;
+  }
+  // hand over: G from the FP32 sweeps, widened and projected, then the FP64 sweeps
+  widen_gauge_kernel<<<(unsigned)((g.S + 255) / 256), 256, 0, st>>>(c.G, static_cast<cx<double>*>(a.G), g.S);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "widen gauge");
+  *iterations = n;
+  if (gmax <= tol && n > 0) {
+    if ((e = finish_fields<double>(a)) != cudaSuccess) return cuda_err(e, "final transform");
+    return GLASMA_OK;
+  }
+  return run_impl<double>(s, a, alpha, max_iters, tol, flags, log, iterations, err, n);
 }
 
 // SetCoulombGauge with the Los Alamos (los_alamos != 0) or the Jacobi update: per iteration one pass
@@ -982,6 +1238,13 @@ int gaugefix_run(GaugeFixState** state, const GaugeFixArgs& a, double alpha, int
   if (a.scratch_doubles < (size_t)kGfBlocks * 7 + 16) {
     *err = "scratch too small";
     return GLASMA_ERR_INVALID_ARGUMENT;
+  }
+  if (flags & GLASMA_GF_MIXED) {
+    if (a.precision != GLASMA_FP64) {
+      *err = "GLASMA_GF_MIXED applies to FP64 handles (FP32 handles store FP32 fields already)";
+      return GLASMA_ERR_UNSUPPORTED;
+    }
+    return run_mixed(*state, a, alpha, max_iters, tol, flags, log, iterations, err);
   }
   return a.precision == GLASMA_FP64 ? run_impl<double>(*state, a, alpha, max_iters, tol, flags, log, iterations, err)
                                     : run_impl<float>(*state, a, alpha, max_iters, tol, flags, log, iterations, err);

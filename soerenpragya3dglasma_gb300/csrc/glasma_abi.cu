@@ -918,7 +918,7 @@ int glasma_coulomb_fix(glasma_lattice* h, double alpha, int max_iters, double to
                        int* iterations) {
   GLASMA_CHECK_HANDLE(h);
   if (max_iters < 0) return fail(GLASMA_ERR_INVALID_ARGUMENT, "max_iters < 0");
-  if (flags & ~(GLASMA_GF_PROJECT_ZERO_MODE | GLASMA_GF_FFT_FP32 | GLASMA_GF_OPEN_Z))
+  if (flags & ~(GLASMA_GF_PROJECT_ZERO_MODE | GLASMA_GF_FFT_FP32 | GLASMA_GF_OPEN_Z | GLASMA_GF_MIXED))
     return fail(GLASMA_ERR_INVALID_ARGUMENT, "unknown gauge-fixing flag");
   int st;
   for (int f : {GLASMA_FIELD_G, GLASMA_FIELD_UG, GLASMA_FIELD_EG})

@@ -355,17 +355,18 @@ class Lattice:
 
     # -- Coulomb gauge fixing (S/GAUGETRANSFORMATION)
     def coulomb_fix(self, alpha, max_iters, tol=1e-15, project_zero_mode=False, fft_fp32=False,
-                    algorithm="fourier", seed=0, open_z=False):
+                    algorithm="fourier", seed=0, open_z=False, mixed=False):
         """Coulomb gauge fixing; returns the per-iteration log rows (n, max dev, avg dev, max step,
         avg step, min functional, functional / V).  algorithm: "fourier" (alpha = the step size of the
         Fourier-accelerated update), "los_alamos" (alpha = the over-relaxation probability; seed picks
         the draws) or "jacobi" (alpha = the step size).  open_z: the open-z functional
         (GLASMA_GF_OPEN_Z, Fourier only), which converges where the reference's iteration does not.
+        mixed: FP32 sweeps first, FP64 for the final ones (GLASMA_GF_MIXED, FP64 handles).
         On failure the GlasmaError carries the rows of the iterations that ran (`log`)."""
         log = np.zeros((max(int(max_iters), 1), 7))
         n = ctypes.c_int()
         flags = (_lib.GF_PROJECT_ZERO_MODE if project_zero_mode else 0) | (_lib.GF_FFT_FP32 if fft_fp32 else 0) | \
-            (_lib.GF_OPEN_Z if open_z else 0)
+            (_lib.GF_OPEN_Z if open_z else 0) | (_lib.GF_MIXED if mixed else 0)
         st = self.lib.glasma_coulomb_fix_algorithm(self.h, _lib.GF_ALGORITHMS[algorithm], float(alpha), int(seed),
                                                    int(max_iters), float(tol), flags, log.ctypes.data_as(_lib._D),
                                                    ctypes.byref(n))

@@ -270,3 +270,34 @@ def test_charge_transformation_matches_oracle(oracle, precision):
         got = lat.transform_charge("JpStat")
         want = oracle.transform_charge(Gd, lat.download("JpStat"), N)
         assert np.max(np.abs(got - want)) < tol * max(1.0, np.max(np.abs(want)))
+
+
+def test_mixed_precision_sweeps_reach_the_fp64_gauge(oracle, golden_dir):
+    """GLASMA_GF_MIXED with the open-z functional on the reference's MV state: FP32 sweeps until the
+    maximum deviation is <= 1e-5 (or stalls), then FP64 sweeps to the reference's stop rule.  It
+    converges to the gauge the FP64 iteration reaches (the oracle's converged run), up to one global
+    rotation R close to the identity (the FP32 sweeps move the iterate along the gauge's global
+    freedom): G_mixed(x) = R G_oracle(x) at every site, and the gauge-fixed fields' gauge-invariant
+    content (theta, the functional) matches."""
+    g, N, a, alpha = _coulomb_mv(golden_dir)
+    f = {"U": g["s_U"].copy(), "E": g["s_E"].copy()}
+    G = O.identity_gauge(N)
+    st, olog, UG, EG = oracle.coulomb_fix(f, G, N, a, alpha, 1000, flags=O.GF_OPEN_Z)
+    assert st == 0
+    with Lattice(N, a) as lat:
+        lat.upload("U", f["U"])
+        lat.upload("E", f["E"])
+        log = lat.coulomb_fix(alpha, 1000, open_z=True, mixed=True)
+        Gg, UGg = lat.download("G"), lat.download("UG")
+    assert log[-1, 1] <= 1e-15 and len(log) < 1000
+    n32 = int(np.argmax(log[:, 1] <= 1e-5))  # the FP32 sweeps end at the first row at or below 1e-5
+    assert 0 < n32 < len(log) - 1
+    Mg, Mo = O.links_as_matrices(Gg)[1:-1], O.links_as_matrices(G)[1:-1]
+    R = Mg @ np.swapaxes(Mo.conj(), -1, -2)
+    assert np.max(np.abs(R - R[0, 0, 0])) < 1e-9 and np.max(np.abs(R[0, 0, 0] - np.eye(3))) < 1e-3
+    # the final functional (sum Re tr UG / V) is invariant under R
+    assert abs(log[-1, 6] - olog[-1, 6]) < 1e-12 * abs(olog[-1, 6])
+    with Lattice(N, a, precision="fp32") as lat:
+        lat.upload("U", f["U"])
+        with pytest.raises(GlasmaError):
+            lat.coulomb_fix(alpha, 10, open_z=True, mixed=True)
