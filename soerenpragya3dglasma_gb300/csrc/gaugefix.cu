@@ -161,17 +161,27 @@ __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const
 }
 
 // ---- momentum-space acceleration of the 4 colour-pair planes
+// lattice momenta per axis, (2 - 2 cos(2 pi k / n)) / a^2 for k < n: tab[0 .. nx), then ny, then nz
+__global__ void p2_table_kernel(int nx, int ny, int nz, double ax, double ay, double az, double* tab) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nx)
+    tab[i] = (2.0 - 2.0 * cospi(2.0 * i / (double)nx)) / (ax * ax);
+  else if (i < nx + ny)
+    tab[i] = (2.0 - 2.0 * cospi(2.0 * (i - nx) / (double)ny)) / (ay * ay);
+  else if (i < nx + ny + nz)
+    tab[i] = (2.0 - 2.0 * cospi(2.0 * (i - nx - ny) / (double)nz)) / (az * az);
+}
+// p^2 from the per-axis table: the same three terms summed in the same order as evaluating them here,
+// without three FP64 cosines per element on GB300's FP64 pipe
 template <typename C>
-__global__ void accelerate_kernel(int nx, int ny, int nz, double ax, double ay, double az, C* X, int project_zero) {
+__global__ void accelerate_kernel(int nx, int ny, int nz, const double* __restrict__ tab, C* X, int project_zero) {
   const long long V = (long long)nx * ny * nz;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 4 * V) return;
   const long long site = i % V;
   const long long r = site / nx;
   const int px = (int)(site - r * nx), pz = (int)(r / ny), py = (int)(r - (long long)pz * ny);
-  const double p2 = (2.0 - 2.0 * cospi(2.0 * px / (double)nx)) / (ax * ax) +
-                    (2.0 - 2.0 * cospi(2.0 * py / (double)ny)) / (ay * ay) +
-                    (2.0 - 2.0 * cospi(2.0 * pz / (double)nz)) / (az * az);
+  const double p2 = tab[px] + tab[nx + py] + tab[nx + ny + pz];
   if (p2 > 0.0) {
     const double f = 1.0 / ((double)V * p2);
     C v = X[i];
@@ -845,6 +855,8 @@ struct GaugeFixState {
   Geometry g;
   int precision = -1;
   void* X = nullptr;  // 8 V complex doubles: the gauge update uses 4 colour-pair planes of it
+  double* p2tab = nullptr;  // per-axis lattice momenta squared (p2_table_kernel), nx + ny + nz
+  double p2a[3] = {0, 0, 0};  // the spacings the table was made for
   std::map<int, double2*> twiddles;
   std::map<int, float2*> twiddles32;
   std::vector<double> host_results;
@@ -874,6 +886,25 @@ cudaError_t ensure_twiddles32(GaugeFixState* s, cudaStream_t stream) {
     if (e != cudaSuccess) return e;
     twiddle_narrow_kernel<<<(count + 255) / 256, 256, 0, stream>>>(kv.second, tw, count);
     s->twiddles32[kv.first] = tw;
+  }
+  return cudaGetLastError();
+}
+
+// the acceleration step's per-axis momentum table, for this lattice's spacings
+cudaError_t ensure_p2tab(GaugeFixState* s, const Geometry& g, cudaStream_t stream) {
+  const int n = g.nx + g.ny + g.nz;
+  if (!s->p2tab) {
+    cudaError_t e = cudaMalloc(&s->p2tab, sizeof(double) * n);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      s->p2tab = nullptr;
+      return e;
+    }
+    s->p2a[0] = s->p2a[1] = s->p2a[2] = 0.0;
+  }
+  if (s->p2a[0] != g.a[0] || s->p2a[1] != g.a[1] || s->p2a[2] != g.a[2]) {
+    p2_table_kernel<<<(n + 127) / 128, 128, 0, stream>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2], s->p2tab);
+    for (int k = 0; k < 3; k++) s->p2a[k] = g.a[k];
   }
   return cudaGetLastError();
 }
@@ -984,6 +1015,7 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
   const double minf0 = 2.0 * 3 * (1.0 / (g.a[0] * g.a[0]) + 1.0 / (g.a[1] * g.a[1]) + 1.0 / (g.a[2] * g.a[2]));
   const bool fft32 = (flags & GLASMA_GF_FFT_FP32) != 0;
   if (fft32 && (e = ensure_twiddles32(s, st)) != cudaSuccess) return cuda_err(e, "FP32 twiddles");
+  if ((e = ensure_p2tab(s, g, st)) != cudaSuccess) return cuda_err(e, "momentum table");
   double2* X64 = static_cast<double2*>(s->X);
   float2* X32 = static_cast<float2*>(s->X);
   const long long tot = 4 * g.vol;
@@ -999,11 +1031,9 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
     e = fft32 ? fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 0, s->twiddles, st);
     if (e != cudaSuccess) return cuda_err(e, "fft forward");
     if (fft32)
-      accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2],
-                                                                                X32, project);
+      accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab, X32, project);
     else
-      accelerate_kernel<double2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1],
-                                                                                 g.a[2], X64, project);
+      accelerate_kernel<double2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab, X64, project);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
     e = fft32 ? fft3d_t<float2>(s, X32, 4, 1, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 1, s->twiddles, st);
     if (e != cudaSuccess) return cuda_err(e, "fft backward");
@@ -1092,6 +1122,7 @@ int run_mixed(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_ite
   };
   if ((e = transform32()) != cudaSuccess) return cuda_err(e, "FP32 transform links");
   if ((e = ensure_twiddles32(s, st)) != cudaSuccess) return cuda_err(e, "FP32 twiddles");
+  if ((e = ensure_p2tab(s, g, st)) != cudaSuccess) return cuda_err(e, "momentum table");
   const float cw[3] = {(float)((a.a_scale / g.a[0]) * (a.a_scale / g.a[0])),
                        (float)((a.a_scale / g.a[1]) * (a.a_scale / g.a[1])),
                        g.nz > 1 ? (float)((a.a_scale / g.a[2]) * (a.a_scale / g.a[2])) : 0.f};
@@ -1112,8 +1143,7 @@ int run_mixed(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_ite
     red::finish_kernel<4><<<1, red::kThreads, 0, st>>>(part_dev, (int)nb, 1 | (0 << 2) | (2 << 4) | (0 << 6), res);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "FP32 deviation");
     if ((e = fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft forward");
-    accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2],
-                                                                              X32, project);
+    accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab, X32, project);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
     if ((e = fft3d_t<float2>(s, X32, 4, 1, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft backward");
     update32_kernel<<<nb, kGfThreads, 0, st>>>(g, X32, c.G, (float)alpha, part_upd, kMixedGuard);
@@ -1279,6 +1309,7 @@ cudaError_t launch_transform_charge(const GaugeFixArgs& a, const void* J, double
 void gaugefix_destroy(GaugeFixState* s) {
   if (!s) return;
   if (s->X) cudaFree(s->X);
+  if (s->p2tab) cudaFree(s->p2tab);
   for (auto& kv : s->twiddles) cudaFree(kv.second);
   for (auto& kv : s->twiddles32) cudaFree(kv.second);
   delete s;
