@@ -521,9 +521,14 @@ __device__ __forceinline__ void expi_impl(T c, const Alg<T>& al, Mat<T>& X) {
     f1 = mk<T>(f1r, f1i);
     f2 = mk<T>(f2r, f2i);
   } else if (c1 < Trig<T>::taylor_c1()) {
-    f0 = mk<T>(kMinusOne ? -(c0 * c0 / T(720)) : T(1) - c0 * c0 / T(720), -c0 / T(6) + c1 * c0 / T(120));
-    f1 = mk<T>(c0 / T(24) - c0 * c1 / T(360), T(1) - c1 / T(6) + c1 * c1 / T(120));
-    f2 = mk<T>(T(-0.5) + c1 / T(24) - c1 * c1 / T(720), c0 / T(120));
+    // the Taylor coefficients as products with folded reciprocals: a division by a constant whose
+    // reciprocal is inexact compiles to a full division, which GB300 runs on its FP64 pipe (ten per
+    // exponential here, on most links of weak fields)
+    constexpr T r6 = T(1) / T(6), r24 = T(1) / T(24), r120 = T(1) / T(120), r360 = T(1) / T(360),
+                r720 = T(1) / T(720);
+    f0 = mk<T>(kMinusOne ? -(c0 * c0 * r720) : T(1) - c0 * c0 * r720, -c0 * r6 + c1 * c0 * r120);
+    f1 = mk<T>(c0 * r24 - c0 * c1 * r360, T(1) - c1 * r6 + c1 * c1 * r120);
+    f2 = mk<T>(T(-0.5) + c1 * r24 - c1 * c1 * r720, c0 * r120);
   } else {
     const bool neg = c0 < T(0);
     const T ac0 = neg ? -c0 : c0;
@@ -541,7 +546,8 @@ __device__ __forceinline__ void expi_impl(T c, const Alg<T>& al, Mat<T>& X) {
     Trig<T>::sincos_(w, &sw, &cw);
     T xi0;
     if (w < T(0.05)) {
-      xi0 = T(1) - w2 / T(6) * (T(1) - w2 / T(20) * (T(1) - w2 / T(42) * (T(1) - w2 / T(72))));
+      xi0 = T(1) - w2 * (T(1) / T(6)) *
+                       (T(1) - w2 * (T(1) / T(20)) * (T(1) - w2 * (T(1) / T(42)) * (T(1) - w2 * (T(1) / T(72)))));
     } else {
       xi0 = sw / w;
     }
