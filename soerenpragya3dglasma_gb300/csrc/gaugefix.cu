@@ -173,6 +173,30 @@ __global__ void p2_table_kernel(int nx, int ny, int nz, double ax, double ay, do
 }
 // p^2 from the per-axis table: the same three terms summed in the same order as evaluating them here,
 // without three FP64 cosines per element on GB300's FP64 pipe
+__global__ void narrow_table_kernel(const double* __restrict__ tab, float* __restrict__ tab32, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) tab32[i] = (float)tab[i];
+}
+// FP32 planes (FP32 transforms, the FP32 sweeps): the factor in FP32 from an FP32 table, so that no
+// element costs an FP64 division and FP64 products on GB300's FP64 pipe
+__global__ void accelerate32_kernel(int nx, int ny, int nz, const float* __restrict__ tab, float2* X, int project_zero) {
+  const long long V = (long long)nx * ny * nz;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 4 * V) return;
+  const long long site = i % V;
+  const long long r = site / nx;
+  const int px = (int)(site - r * nx), pz = (int)(r / ny), py = (int)(r - (long long)pz * ny);
+  const float p2 = tab[px] + tab[nx + py] + tab[nx + ny + pz];
+  if (p2 > 0.f) {
+    const float f = 1.f / ((float)V * p2);
+    float2 v = X[i];
+    v.x *= f;
+    v.y *= f;
+    X[i] = v;
+  } else if (project_zero) {
+    X[i] = make_float2(0.f, 0.f);
+  }
+}
 template <typename C>
 __global__ void accelerate_kernel(int nx, int ny, int nz, const double* __restrict__ tab, C* X, int project_zero) {
   const long long V = (long long)nx * ny * nz;
@@ -300,14 +324,18 @@ __global__ void __launch_bounds__(kGfThreads) deviation32_kernel(Geometry g, con
     }
     Alg<float> dev;
     retr_itg(w, 1.f, dev);
+    // per site in FP32, across sites in FP64 (each conversion is an FP64-pipe instruction on GB300)
+    float dmax = 0.f, dsq = 0.f;
 #pragma unroll
     for (int a = 0; a < 8; a++) {
-      v[0] = fmax(v[0], (double)fabsf(dev.a[a]));
-      v[1] += (double)dev.a[a] * (double)dev.a[a];
+      dmax = fmaxf(dmax, fabsf(dev.a[a]));
+      dsq = fmaf(dev.a[a], dev.a[a], dsq);
     }
+    v[0] = fmax(v[0], (double)dmax);
+    v[1] += (double)dsq;
 #pragma unroll
     for (int q = 0; q < 4; q++) X[(long long)q * g.vol + idx] = make_float2(dev.a[2 * q], dev.a[2 * q + 1]);
-    const double lf = (double)w.e[0].re + (double)w.e[4].re + (double)w.e[8].re;
+    const double lf = (double)(w.e[0].re + w.e[4].re + w.e[8].re);
     v[2] = fmin(v[2], lf);
     v[3] += lf;
   }
@@ -332,11 +360,10 @@ __global__ void __launch_bounds__(kGfThreads) update32_kernel(Geometry g, const 
     Mat<float> wt, gm, gn;
     expi(-alpha, upd, wt);
     if (!(unitarity_norm(wt) <= guard)) v[2] += 1.0;
-    const double sr = 3.0 - (double)wt.e[0].re - (double)wt.e[4].re - (double)wt.e[8].re;
-    const double si = -((double)wt.e[0].im + (double)wt.e[4].im + (double)wt.e[8].im);
-    const double step = sqrt(sr * sr + si * si);
-    v[0] = fmax(v[0], step);
-    v[1] += step * step;
+    const float sr = 3.f - wt.e[0].re - wt.e[4].re - wt.e[8].re, si = -(wt.e[0].im + wt.e[4].im + wt.e[8].im);
+    const float step2 = sr * sr + si * si;
+    v[0] = fmax(v[0], (double)sqrtf(step2));
+    v[1] += (double)step2;
     const long long s = idx + g.plane;
     ld_f(G, g.S, 0, s, gm);
     mul_dn(wt, gm, gn);
@@ -856,6 +883,7 @@ struct GaugeFixState {
   int precision = -1;
   void* X = nullptr;  // 8 V complex doubles: the gauge update uses 4 colour-pair planes of it
   double* p2tab = nullptr;  // per-axis lattice momenta squared (p2_table_kernel), nx + ny + nz
+  float* p2tab32 = nullptr;  // the same rounded to FP32, for the FP32 planes
   double p2a[3] = {0, 0, 0};  // the spacings the table was made for
   std::map<int, double2*> twiddles;
   std::map<int, float2*> twiddles32;
@@ -895,15 +923,19 @@ cudaError_t ensure_p2tab(GaugeFixState* s, const Geometry& g, cudaStream_t strea
   const int n = g.nx + g.ny + g.nz;
   if (!s->p2tab) {
     cudaError_t e = cudaMalloc(&s->p2tab, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s->p2tab32, sizeof(float) * n);
     if (e != cudaSuccess) {
       cudaGetLastError();
+      cudaFree(s->p2tab);
       s->p2tab = nullptr;
+      s->p2tab32 = nullptr;
       return e;
     }
     s->p2a[0] = s->p2a[1] = s->p2a[2] = 0.0;
   }
   if (s->p2a[0] != g.a[0] || s->p2a[1] != g.a[1] || s->p2a[2] != g.a[2]) {
     p2_table_kernel<<<(n + 127) / 128, 128, 0, stream>>>(g.nx, g.ny, g.nz, g.a[0], g.a[1], g.a[2], s->p2tab);
+    narrow_table_kernel<<<(n + 127) / 128, 128, 0, stream>>>(s->p2tab, s->p2tab32, n);
     for (int k = 0; k < 3; k++) s->p2a[k] = g.a[k];
   }
   return cudaGetLastError();
@@ -1031,7 +1063,7 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
     e = fft32 ? fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 0, s->twiddles, st);
     if (e != cudaSuccess) return cuda_err(e, "fft forward");
     if (fft32)
-      accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab, X32, project);
+      accelerate32_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab32, X32, project);
     else
       accelerate_kernel<double2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab, X64, project);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
@@ -1143,7 +1175,7 @@ int run_mixed(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_ite
     red::finish_kernel<4><<<1, red::kThreads, 0, st>>>(part_dev, (int)nb, 1 | (0 << 2) | (2 << 4) | (0 << 6), res);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "FP32 deviation");
     if ((e = fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft forward");
-    accelerate_kernel<float2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab, X32, project);
+    accelerate32_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab32, X32, project);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
     if ((e = fft3d_t<float2>(s, X32, 4, 1, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft backward");
     update32_kernel<<<nb, kGfThreads, 0, st>>>(g, X32, c.G, (float)alpha, part_upd, kMixedGuard);
@@ -1310,6 +1342,7 @@ void gaugefix_destroy(GaugeFixState* s) {
   if (!s) return;
   if (s->X) cudaFree(s->X);
   if (s->p2tab) cudaFree(s->p2tab);
+  if (s->p2tab32) cudaFree(s->p2tab32);
   for (auto& kv : s->twiddles) cudaFree(kv.second);
   for (auto& kv : s->twiddles32) cudaFree(kv.second);
   delete s;
