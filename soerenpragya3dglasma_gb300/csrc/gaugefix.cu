@@ -98,6 +98,23 @@ __device__ __forceinline__ long long nbr(const Geometry& g, int x, int y, int z,
   return site_index(g, xx, yy, z + dz);
 }
 
+// (x, y, z) of index idx = x + nx (y + ny z), in 32-bit arithmetic when every index fits: a 64-bit
+// integer division here kept the FP32 acceleration kernel's FP64 pipe 30 % busy on GB300 (ncu), and the
+// FP64 kernels are bound by that pipe
+__device__ __forceinline__ void gf_decode(long long idx, int nx, int ny, long long total, int& x, int& y, int& z) {
+  if (total < (1LL << 31)) {
+    const unsigned u = (unsigned)idx, r = u / (unsigned)nx;
+    x = (int)(u - r * (unsigned)nx);
+    z = (int)(r / (unsigned)ny);
+    y = (int)(r - (unsigned)z * (unsigned)ny);
+  } else {
+    const long long r = idx / nx;
+    x = (int)(idx - r * nx);
+    z = (int)(r / ny);
+    y = (int)(r - (long long)z * ny);
+  }
+}
+
 // w(x) = sum_mu c_mu (UG_mu(x) + UG_mu^d(x - mu)) at interior site s = (x, y, z); c2 = 0 when Nz = 1
 // (GET_LOCAL_GAUGE_VIOLATION, S/GAUGETRANSFORMATION/CoulombGaugeDeviation.cpp:23-41).
 // open_top (GLASMA_GF_OPEN_Z): the forward z link of the top slice, which points into the ghost slice,
@@ -138,8 +155,8 @@ __global__ void __launch_bounds__(kGfThreads) deviation_kernel(Geometry g, const
   const int op[4] = {1, 0, 2, 0};
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
        idx += (long long)gridDim.x * blockDim.x) {
-    const long long r = idx / g.nx;
-    const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+    int x, y, z;
+    gf_decode(idx, g.nx, g.ny, g.vol, x, y, z);
     const long long s = idx + g.plane;
     Mat<double> w;
     site_w(g, UG, x, y, z, s, c0, c1, c2, w, open_top);
@@ -179,16 +196,18 @@ __global__ void narrow_table_kernel(const double* __restrict__ tab, float* __res
 }
 // FP32 planes (FP32 transforms, the FP32 sweeps): the factor in FP32 from an FP32 table, so that no
 // element costs an FP64 division and FP64 products on GB300's FP64 pipe
-__global__ void accelerate32_kernel(int nx, int ny, int nz, const float* __restrict__ tab, float2* X, int project_zero) {
+__global__ void accelerate32_kernel(int nx, int ny, int nz, float vf, const float* __restrict__ tab, float2* X,
+                                    int project_zero) {
   const long long V = (long long)nx * ny * nz;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 4 * V) return;
-  const long long site = i % V;
-  const long long r = site / nx;
-  const int px = (int)(site - r * nx), pz = (int)(r / ny), py = (int)(r - (long long)pz * ny);
+  int px, py, pz;
+  gf_decode(i, nx, ny * nz, 4 * V, px, py, pz);  // (x, y + ny z, plane): the plane index is not needed
+  pz = py / ny;
+  py -= pz * ny;
   const float p2 = tab[px] + tab[nx + py] + tab[nx + ny + pz];
   if (p2 > 0.f) {
-    const float f = 1.f / ((float)V * p2);
+    const float f = 1.f / (vf * p2);
     float2 v = X[i];
     v.x *= f;
     v.y *= f;
@@ -198,16 +217,18 @@ __global__ void accelerate32_kernel(int nx, int ny, int nz, const float* __restr
   }
 }
 template <typename C>
-__global__ void accelerate_kernel(int nx, int ny, int nz, const double* __restrict__ tab, C* X, int project_zero) {
+__global__ void accelerate_kernel(int nx, int ny, int nz, double vd, const double* __restrict__ tab, C* X,
+                                  int project_zero) {
   const long long V = (long long)nx * ny * nz;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 4 * V) return;
-  const long long site = i % V;
-  const long long r = site / nx;
-  const int px = (int)(site - r * nx), pz = (int)(r / ny), py = (int)(r - (long long)pz * ny);
+  int px, py, pz;
+  gf_decode(i, nx, ny * nz, 4 * V, px, py, pz);  // (x, y + ny z, plane)
+  pz = py / ny;
+  py -= pz * ny;
   const double p2 = tab[px] + tab[nx + py] + tab[nx + ny + pz];
   if (p2 > 0.0) {
-    const double f = 1.0 / ((double)V * p2);
+    const double f = 1.0 / (vd * p2);
     C v = X[i];
     v.x *= f;
     v.y *= f;
@@ -277,8 +298,8 @@ __global__ void __launch_bounds__(128) transform_links32_kernel(Geometry g, cons
                                                                 cx<float>* UG) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.vol) return;
-  const long long r = idx / g.nx;
-  const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+  int x, y, z;
+  gf_decode(idx, g.nx, g.ny, g.vol, x, y, z);
   const long long s = idx + g.plane;
   const long long fwd[3] = {nbr(g, x, y, z, 1, 0, 0), nbr(g, x, y, z, 0, 1, 0), s + g.plane};
   Mat<float> gx, u, gy, t, o;
@@ -295,13 +316,16 @@ __global__ void __launch_bounds__(128) transform_links32_kernel(Geometry g, cons
 // deviation_kernel in FP32 (site_w's sum, the projection and X); partials in FP64
 __global__ void __launch_bounds__(kGfThreads) deviation32_kernel(Geometry g, const cx<float>* UG, float c0, float c1,
                                                                  float c2, float2* X, double* partials, int open_top) {
-  double v[4] = {0.0, 0.0, 1.0e300, 0.0};
+  // each thread's sites summed in FP32 (a few dozen terms), the block and grid sums in FP64: FP64
+  // arithmetic and conversions run on GB300's slow FP64 pipe, which this kernel then leaves alone
+  double v[4];
+  float tmax = 0.f, tsq = 0.f, tmin = 3.0e38f, tlf = 0.f;
   const int op[4] = {1, 0, 2, 0};
   const float c[3] = {c0, c1, c2};
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
        idx += (long long)gridDim.x * blockDim.x) {
-    const long long r = idx / g.nx;
-    const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+    int x, y, z;
+    gf_decode(idx, g.nx, g.ny, g.vol, x, y, z);
     const long long s = idx + g.plane;
     const long long back[3] = {nbr(g, x, y, z, -1, 0, 0), nbr(g, x, y, z, 0, -1, 0), s - g.plane};
     const float fwd2 = (open_top && z == g.nz - 1) ? 0.f : 1.f;
@@ -324,21 +348,21 @@ __global__ void __launch_bounds__(kGfThreads) deviation32_kernel(Geometry g, con
     }
     Alg<float> dev;
     retr_itg(w, 1.f, dev);
-    // per site in FP32, across sites in FP64 (each conversion is an FP64-pipe instruction on GB300)
-    float dmax = 0.f, dsq = 0.f;
 #pragma unroll
     for (int a = 0; a < 8; a++) {
-      dmax = fmaxf(dmax, fabsf(dev.a[a]));
-      dsq = fmaf(dev.a[a], dev.a[a], dsq);
+      tmax = fmaxf(tmax, fabsf(dev.a[a]));
+      tsq = fmaf(dev.a[a], dev.a[a], tsq);
     }
-    v[0] = fmax(v[0], (double)dmax);
-    v[1] += (double)dsq;
 #pragma unroll
     for (int q = 0; q < 4; q++) X[(long long)q * g.vol + idx] = make_float2(dev.a[2 * q], dev.a[2 * q + 1]);
-    const double lf = (double)(w.e[0].re + w.e[4].re + w.e[8].re);
-    v[2] = fmin(v[2], lf);
-    v[3] += lf;
+    const float lf = w.e[0].re + w.e[4].re + w.e[8].re;
+    tmin = fminf(tmin, lf);
+    tlf += lf;
   }
+  v[0] = tmax;
+  v[1] = tsq;
+  v[2] = tmin;
+  v[3] = tlf;
   red::block_reduce_store<4>(v, op, partials + (long long)blockIdx.x * 4);
 }
 
@@ -346,7 +370,9 @@ __global__ void __launch_bounds__(kGfThreads) deviation32_kernel(Geometry g, con
 // unitary to ~1e-7): it trips at `guard`, which still catches the runaway the reference's guard exists for.
 __global__ void __launch_bounds__(kGfThreads) update32_kernel(Geometry g, const float2* X, cx<float>* G, float alpha,
                                                               double* partials, float guard) {
-  double v[3] = {0.0, 0.0, 0.0};
+  // per-thread sums in FP32, block and grid sums in FP64 (as deviation32_kernel)
+  double v[3];
+  float tmax = 0.f, tsq = 0.f, tbad = 0.f;
   const int op[3] = {1, 0, 0};
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.vol;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -359,16 +385,19 @@ __global__ void __launch_bounds__(kGfThreads) update32_kernel(Geometry g, const 
     }
     Mat<float> wt, gm, gn;
     expi(-alpha, upd, wt);
-    if (!(unitarity_norm(wt) <= guard)) v[2] += 1.0;
+    if (!(unitarity_norm(wt) <= guard)) tbad += 1.f;
     const float sr = 3.f - wt.e[0].re - wt.e[4].re - wt.e[8].re, si = -(wt.e[0].im + wt.e[4].im + wt.e[8].im);
     const float step2 = sr * sr + si * si;
-    v[0] = fmax(v[0], (double)sqrtf(step2));
-    v[1] += (double)step2;
+    tmax = fmaxf(tmax, sqrtf(step2));
+    tsq += step2;
     const long long s = idx + g.plane;
     ld_f(G, g.S, 0, s, gm);
     mul_dn(wt, gm, gn);
     st_f(G, g.S, 0, s, gn);
   }
+  v[0] = tmax;
+  v[1] = tsq;
+  v[2] = tbad;
   red::block_reduce_store<3>(v, op, partials + (long long)blockIdx.x * 3);
 }
 
@@ -464,8 +493,8 @@ __global__ void __launch_bounds__(kGfThreads) local_update_kernel(Geometry g, co
   const long long n = (long long)hx * g.ny * g.nz;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
        idx += (long long)gridDim.x * blockDim.x) {
-    const long long r = idx / hx;
-    const int k = (int)(idx - r * hx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+    int k, y, z;
+    gf_decode(idx, hx, g.ny, n, k, y, z);
     const int x = pass < 0 ? k : (((pass + y + z) & 1) + 2 * k);
     if (x >= g.nx) continue;
     const long long s = site_index(g, x, y, z);
@@ -509,8 +538,8 @@ template <typename T>
 __global__ void __launch_bounds__(128) transform_links_kernel(Geometry g, const cx<T>* U, const cx<T>* G, cx<T>* UG) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.vol) return;
-  const long long r = idx / g.nx;
-  const int x = (int)(idx - r * g.nx), z = (int)(r / g.ny), y = (int)(r - (long long)z * g.ny);
+  int x, y, z;
+  gf_decode(idx, g.nx, g.ny, g.vol, x, y, z);
   const long long s = idx + g.plane;
   const long long fwd[3] = {nbr(g, x, y, z, 1, 0, 0), nbr(g, x, y, z, 0, 1, 0), s + g.plane};
   Mat<double> gx, u, gy, t, o;
@@ -1063,9 +1092,11 @@ int run_impl(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_iter
     e = fft32 ? fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 0, s->twiddles, st);
     if (e != cudaSuccess) return cuda_err(e, "fft forward");
     if (fft32)
-      accelerate32_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab32, X32, project);
+      accelerate32_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, (float)g.vol, s->p2tab32, X32,
+                                                                         project);
     else
-      accelerate_kernel<double2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab, X64, project);
+      accelerate_kernel<double2><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, (double)g.vol, s->p2tab,
+                                                                          X64, project);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
     e = fft32 ? fft3d_t<float2>(s, X32, 4, 1, s->twiddles32, st) : fft3d_t<double2>(s, X64, 4, 1, s->twiddles, st);
     if (e != cudaSuccess) return cuda_err(e, "fft backward");
@@ -1175,7 +1206,8 @@ int run_mixed(GaugeFixState* s, const GaugeFixArgs& a, double alpha, int max_ite
     red::finish_kernel<4><<<1, red::kThreads, 0, st>>>(part_dev, (int)nb, 1 | (0 << 2) | (2 << 4) | (0 << 6), res);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "FP32 deviation");
     if ((e = fft3d_t<float2>(s, X32, 4, 0, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft forward");
-    accelerate32_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, s->p2tab32, X32, project);
+    accelerate32_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.nx, g.ny, g.nz, (float)g.vol, s->p2tab32, X32,
+                                                                         project);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "accelerate");
     if ((e = fft3d_t<float2>(s, X32, 4, 1, s->twiddles32, st)) != cudaSuccess) return cuda_err(e, "fft backward");
     update32_kernel<<<nb, kGfThreads, 0, st>>>(g, X32, c.G, (float)alpha, part_upd, kMixedGuard);

@@ -122,11 +122,32 @@ __global__ void finish_slices_kernel(const double* __restrict__ partials, int nz
   out[i] = v;
 }
 
+// Index decodes in 32-bit arithmetic whenever the indices fit: GB300 runs the 64-bit integer
+// division sequence partly on its FP64 pipe (measured on the gauge fixer's FP32 kernels), the pipe
+// the FP64 observables are bound by.
 __device__ __forceinline__ void decode_vol(const Geometry& g, long long idx, int& x, int& y, int& z) {
+  if (g.vol < (1LL << 31)) {
+    const unsigned u = (unsigned)idx, r = u / (unsigned)g.nx;
+    x = (int)(u - r * (unsigned)g.nx);
+    z = (int)(r / (unsigned)g.ny);
+    y = (int)(r - (unsigned)z * (unsigned)g.ny);
+    return;
+  }
   const long long r = idx / g.nx;
   x = (int)(idx - r * g.nx);
   z = (int)(r / g.ny);
   y = (int)(r - (long long)z * g.ny);
+}
+// (x, y) of r = x + nx y within a transverse plane
+__device__ __forceinline__ void decode_plane(const Geometry& g, long long r, int& x, int& y) {
+  if (g.plane < (1LL << 31)) {
+    const unsigned u = (unsigned)r;
+    y = (int)(u / (unsigned)g.nx);
+    x = (int)(u - (unsigned)y * (unsigned)g.nx);
+    return;
+  }
+  y = (int)(r / g.nx);
+  x = (int)(r - (long long)y * g.nx);
 }
 
 // Re tr(a b c^d d^d) = Re sum_ij (a b)_ij conj((d c)_ij): two products and a dot product instead of
@@ -248,7 +269,8 @@ __global__ void __launch_bounds__(kRedThreads) gauss_kernel(Geometry g, FieldPtr
   const int z = blockIdx.y;
   const long long S = g.S;
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < g.plane; r += (long long)gridDim.x * blockDim.x) {
-    const int y = (int)(r / g.nx), x = (int)(r - (long long)y * g.nx);
+    int x, y;
+    decode_plane(g, r, x, y);
     const long long s = site_index(g, x, y, z);
     Mat<double> u;
     Alg<double> e, down, tot;
@@ -282,7 +304,7 @@ __global__ void __launch_bounds__(kRedThreads) unitarity_kernel(Geometry g, cons
   const bool is_max[2] = {false, true};
   const long long n = g.vol * 3;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int mu = (int)(i / g.vol);
+    const int mu = i < g.vol ? 0 : (i < 2 * g.vol ? 1 : 2);
     const long long s = i - (long long)mu * g.vol + g.plane;
     Mat<double> u;
     load_link_d(U, g.S, mu, s, u);
@@ -362,7 +384,8 @@ __global__ void __launch_bounds__(kRedThreads) emt_kernel(Geometry g, FieldPtrs<
   for (int mu = 0; mu < 3; mu++) q[mu] = g.a[mu] * aScale * aScale / a3;
   const double inv = 1.0 / ((double)g.nx * g.ny);
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < g.plane; r += (long long)gridDim.x * blockDim.x) {
-    const int y = (int)(r / g.nx), x = (int)(r - (long long)y * g.nx);
+    int x, y;
+    decode_plane(g, r, x, y);
     const long long s = site_index(g, x, y, z);
     // magnetic: clover averages of UOld in the planes yz (B0), zx (B1), xy (B2)
     Alg<double> B[3];
